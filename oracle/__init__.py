@@ -1,0 +1,2 @@
+"""Test infrastructure (the oracle).  Imported only by tests/, __graft_entry__.smoke() and the CPU
+baseline leg of bench.py, as the checker.  The product package never imports it."""
