@@ -1,0 +1,124 @@
+/*
+ * searay_uppe.h - C ABI of the GB300 (sm_103a) UPPE z-step library, libsearay_uppe.so.
+ *
+ * The library is a drop-in for the device side of SeaRay's unidirectional pulse propagation
+ * (UPPE) path: modules/uppe_kernel.py (Material, Source, load_source, update_current, propagator,
+ * finish) together with the OpenCL kernels it enqueues (kernels/uppe.cl, kernels/fft.cl,
+ * kernels/ionization.cl, kernels/paraxial.cl:27-58).  The host side that parses the volume input
+ * dictionary (uppe_kernel.track) stays in Python (searay_gb300/uppe.py) and calls these entry
+ * points with plain pointers and sizes.
+ *
+ * Conventions
+ *   - Every call returns an int status: 0 on success, a negative UPPE_E* code on error.  Nothing
+ *     traps; uppe_last_error() gives the message of the last failure on a handle.
+ *   - Field arrays are complex64 (interleaved float pairs) in the reference layout [w][x|r][y|phi],
+ *     C order, N0 x N1 x N2 elements, and live in device memory owned by the caller.  Host-side
+ *     tables (frequencies, eigenvalues, Hankel basis, material) are FP64 host arrays, copied in.
+ *   - Work buffers are owned by the handle.  All work of a handle is issued on its stream, in
+ *     order.  A handle is not thread-safe; distinct handles are independent.
+ */
+#ifndef SEARAY_UPPE_H
+#define SEARAY_UPPE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UPPE_OK 0
+#define UPPE_E_ARG (-1)      /* invalid argument, shape or state */
+#define UPPE_E_CUDA (-2)     /* a CUDA runtime call failed */
+#define UPPE_E_NOMEM (-3)    /* device allocation failed */
+#define UPPE_E_RANGE (-4)    /* a value lies outside what the mixed-precision path represents */
+#define UPPE_E_NONFINITE (-5) /* the field holds NaN or Inf */
+
+/* Precision forms. */
+#define UPPE_PREC_MIXED 0 /* FP32 transforms/sources; float-float phase and density scan */
+#define UPPE_PREC_FP32 1  /* everything in FP32, including phase and density scan */
+
+/* Ionization rate forms (kernels/ionization.cl). */
+#define UPPE_RATE_NONE 0
+#define UPPE_RATE_EXPLICIT 1 /* ExplicitRate, ionization.cl:22-44 */
+#define UPPE_RATE_SERIES 2   /* ExplicitRateSeries, ionization.cl:71-97 */
+
+typedef struct UppeConfig {
+    int n0;            /* frequency nodes, 2^n + 1 (uppe_kernel.py:354-356) */
+    int n1;            /* x nodes (Cartesian) or radial nodes (cylindrical), 2^n */
+    int n2;            /* y nodes (Cartesian) or azimuthal nodes (cylindrical), 2^n */
+    int radial_modes;  /* Nk <= n1 for cylindrical (grid_tools.py:254-258); ignored for Cartesian */
+    int cylindrical;   /* 0: FourierTransformTool, 1: HankelTransformTool */
+    int precision;     /* UPPE_PREC_* */
+    double dt;         /* pi / max(w)  (uppe_kernel.py:96) */
+    double chi3_over_nref; /* chi3 / density reference (uppe_kernel.py:52) */
+    int nl_cut_on;     /* int(NL_band[0]/dw) (uppe_kernel.py:122) */
+    int nl_cut_off;    /* int(NL_band[1]/dw) (uppe_kernel.py:123) */
+    int rate_form;     /* UPPE_RATE_* */
+    double field_conv; /* field_sim_to_au(1) (ionization.py:132) */
+    double rate_conv;  /* rate_au_to_sim(1) (ionization.py:133) */
+    double field_cutoff; /* 1e-3 a.u. (ionization.py:102) */
+    double c_pre, c_pow, c_exp; /* explicit form coefficients */
+    double clog[6];    /* series form coefficients */
+    double damping;    /* iDtSpectral damping, 0.1 (uppe_kernel.py:171) */
+    int window_cutoff; /* SoftTimeWindow cutoff, 4 (uppe_kernel.py:168) */
+    int window_width;  /* SoftTimeWindow width, 64 */
+} UppeConfig;
+
+typedef struct UppeHandle UppeHandle;
+
+/* Allocate a propagator for one grid.  Replaces the buffer set-up of Source.__init__
+ * (uppe_kernel.py:95-129), Material.__init__ (:35-66) and TransverseModeTool.AllocateDeviceMemory
+ * (grid_tools.py:299-303). */
+int uppe_create(const UppeConfig* cfg, UppeHandle** out);
+
+/* Release a handle and its device buffers (grid_tools.py:304-307). */
+int uppe_destroy(UppeHandle* h);
+
+/* Issue the handle's work on this CUDA stream (cudaStream_t; NULL = legacy default stream). */
+int uppe_set_stream(UppeHandle* h, void* stream);
+
+/* Grid tables, once per handle.  w: N0 frequencies (caustic_tools.py:88-96); kr2: the transverse
+ * eigenvalues, N1*N2 values (Cartesian FD k^2, grid_tools.py:245-250, or -vals of the Hankel
+ * basis, grid_tools.py:357-358); H: Hankel basis (Nk, Nr, N2) and Lambda (Nr) for cylindrical
+ * grids (grid_tools.py:252-294), NULL for Cartesian.  Replaces the H/L uploads of
+ * HankelTransformTool.AllocateDeviceMemory (grid_tools.py:299-303). */
+int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, const double* H, const double* Lambda);
+
+/* Material at the current subcycle.  w2n2: N0 complex values w^2 (1 + chi0(w)) as interleaved
+ * doubles; kg: N0 values -w/v_window; ng: N1*N2 gas densities n_ref*dens.  Builds kz on the device
+ * with the reference's guards (Im kz >= 0; Re kz == 0 -> 1).  Replaces Material.UpdateMaterial's
+ * kz/kg/ng uploads (uppe_kernel.py:67-90). */
+int uppe_set_material(UppeHandle* h, const double* w2n2, const double* kg, const double* ng);
+
+/* Load the incoming field a (device, real space, complex64) and transform it to the transverse
+ * spectral representation q.  Replaces Source(...) + T.kspacex(qw) (uppe_kernel.py:290-291). */
+int uppe_load_field(UppeHandle* h, const void* a);
+
+/* One classic RK4 step of the interaction-picture amplitude (uppe_kernel.py:304-325 body).
+ * z_phase: local coordinate of the step start used in the propagator phase (z0 - zi + z);
+ * L: subcycle length; z_sub: position of the step inside the subcycle; dzmin: minimum step.
+ * The adaptive estimate (paraxial.cl:27-58, uppe_kernel.py:217-232) runs only when dzmin < L - z_sub;
+ * otherwise dz = L - z_sub.  *dz_out receives the step taken. */
+int uppe_rk4_step(UppeHandle* h, double z_phase, double L, double z_sub, double dzmin, double* dz_out);
+
+/* Final phase to z_phase, inverse transverse transform and source diagnostics (uppe_kernel.py:234-258).
+ * Device outputs, complex64 [N0][N1][N2]: A (real-space vector potential), J (real-space current),
+ * chi_w = rfft_t(chi), ne_w = rfft_t(ne).  Any output may be NULL. */
+int uppe_finish(UppeHandle* h, double z_phase, void* A, void* J, void* chi_w, void* ne_w);
+
+/* One right-hand-side evaluation S(q, z) = load_source (uppe_kernel.py:188-216), for tests:
+ * q_in and S_out are device complex64 [N0][N1][N2] in the transverse spectral representation. */
+int uppe_eval_rhs(UppeHandle* h, const void* q_in, double z_phase, void* S_out);
+
+/* Copy the current spectral amplitude q to a device buffer (complex64 [N0][N1][N2]). */
+int uppe_get_field(UppeHandle* h, void* q_out);
+
+/* Set *nonfinite to 1 if the current q holds NaN or Inf (the '!' check of uppe_kernel.py:219-220). */
+int uppe_check_finite(UppeHandle* h, int* nonfinite);
+
+/* Message of the last error on h (or of the last failed uppe_create when h is NULL). */
+const char* uppe_last_error(const UppeHandle* h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEARAY_UPPE_H */

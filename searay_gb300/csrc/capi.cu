@@ -1,0 +1,403 @@
+// C ABI of libsearay_uppe (include/searay_uppe.h): handle management and the orchestration of one
+// RK4 step, one right-hand-side evaluation and the diagnostic finish.  Mirrors the control flow of
+// SeaRay's modules/uppe_kernel.py:188-331 with device-resident state and no per-step host sync
+// unless the adaptive step estimate is required.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <new>
+#include <vector>
+
+#include "common.cuh"
+#include "uppe_internal.h"
+
+static char g_create_error[512] = "";
+
+int uppe_set_error(UppeHandle* h, const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    char* dst = h ? h->err : g_create_error;
+    vsnprintf(dst, 512, fmt, ap);
+    va_end(ap);
+    return 0;
+}
+
+#define CUDA_TRY(h, expr)                                                                         \
+    do {                                                                                          \
+        cudaError_t e_ = (expr);                                                                  \
+        if (e_ != cudaSuccess) {                                                                  \
+            uppe_set_error((h), "%s failed: %s", #expr, cudaGetErrorString(e_));                  \
+            return (e_ == cudaErrorMemoryAllocation) ? UPPE_E_NOMEM : UPPE_E_CUDA;                \
+        }                                                                                         \
+    } while (0)
+
+static bool is_pow2(long n) { return n > 0 && (n & (n - 1)) == 0; }
+
+static StepArgs split_z(const UppeHandle* h, double z) {
+    StepArgs s;
+    s.zhi = (float)z;
+    s.zlo = (float)(z - (double)s.zhi);
+    s.plain = (h->cfg.precision == UPPE_PREC_FP32);
+    return s;
+}
+
+static void free_buffers(UppeHandle* h) {
+    void* ptrs[] = {h->q, h->qi, h->qf, h->k1, h->E, h->J, h->scratch, h->op, h->ng, h->tw, h->w, h->nlfilt,
+                    h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+}
+
+extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
+    if (!cfg || !out) {
+        uppe_set_error(nullptr, "uppe_create: null argument");
+        return UPPE_E_ARG;
+    }
+    *out = nullptr;
+    const UppeConfig& c = *cfg;
+    if (c.n0 < 17 || !is_pow2(c.n0 - 1)) {
+        uppe_set_error(nullptr, "UPPE propagator requires 2**n+1 w-nodes with n >= 4 (got %d)", c.n0);
+        return UPPE_E_ARG;
+    }
+    if (!is_pow2(c.n1) || !is_pow2(c.n2)) {
+        uppe_set_error(nullptr, "UPPE propagator requires 2**n x-nodes and y-nodes (got %d, %d)", c.n1, c.n2);
+        return UPPE_E_ARG;
+    }
+    const int Nt = 2 * c.n0 - 2;
+    if (Nt > 8192) {
+        uppe_set_error(nullptr, "time axis of %d samples exceeds the 8192 supported by the time pass", Nt);
+        return UPPE_E_ARG;
+    }
+    const long S = (long)c.n1 * c.n2;
+    if (!c.cylindrical && (S < 16 || S > 16384)) {
+        uppe_set_error(nullptr, "Cartesian slice of %ld points outside the supported 16..16384 (128x128)", S);
+        return UPPE_E_ARG;
+    }
+    if (c.cylindrical && (c.radial_modes < 1 || c.radial_modes > c.n1)) {
+        uppe_set_error(nullptr, "radial modes %d must lie in [1, %d]", c.radial_modes, c.n1);
+        return UPPE_E_ARG;
+    }
+    if (c.precision != UPPE_PREC_MIXED && c.precision != UPPE_PREC_FP32) {
+        uppe_set_error(nullptr, "unknown precision form %d", c.precision);
+        return UPPE_E_ARG;
+    }
+    if (c.rate_form < UPPE_RATE_NONE || c.rate_form > UPPE_RATE_SERIES) {
+        uppe_set_error(nullptr, "unknown rate form %d", c.rate_form);
+        return UPPE_E_ARG;
+    }
+    UppeHandle* h = new (std::nothrow) UppeHandle();
+    if (!h) {
+        uppe_set_error(nullptr, "out of host memory");
+        return UPPE_E_NOMEM;
+    }
+    memset(h, 0, sizeof(UppeHandle));
+    h->cfg = c;
+    h->N0 = c.n0;
+    h->N1 = c.n1;
+    h->N2 = c.n2;
+    h->Nk = c.cylindrical ? c.radial_modes : c.n1;
+    h->Nt = Nt;
+    h->M = c.n0 - 1;
+    h->S = (int)S;
+    h->P = (size_t)c.n0 * S;
+    int tc = 8192 / Nt;
+    if (tc < 1) tc = 1;
+    if (tc > 16) tc = 16;
+    if (tc > h->S) tc = h->S;
+    h->time_cols = tc;
+    int nt = Nt;
+    if (c.n1 > nt) nt = c.n1;
+    if (c.n2 > nt) nt = c.n2;
+    h->twLog = ilog2_exact(nt);
+    h->stream = 0;
+
+    const size_t fbytes = h->P * sizeof(float2);
+    cudaError_t e = cudaSuccess;
+#define ALLOC(ptr, bytes)                                           \
+    if (e == cudaSuccess) e = cudaMalloc((void**)&(ptr), (bytes));
+    ALLOC(h->q, fbytes);
+    ALLOC(h->qi, fbytes);
+    ALLOC(h->qf, fbytes);
+    ALLOC(h->k1, fbytes);
+    ALLOC(h->E, fbytes);
+    ALLOC(h->J, fbytes);
+    if (c.cylindrical && c.n2 > 1) ALLOC(h->scratch, fbytes);
+    ALLOC(h->op, h->P * sizeof(float4));
+    ALLOC(h->ng, (size_t)S * sizeof(float));
+    ALLOC(h->tw, ((size_t)1 << h->twLog) * sizeof(float2));
+    ALLOC(h->w, (size_t)c.n0 * sizeof(float));
+    ALLOC(h->nlfilt, (size_t)c.n0 * sizeof(float));
+    if (c.cylindrical) {
+        ALLOC(h->Minv, (size_t)c.n2 * c.n1 * h->Nk * sizeof(float));
+        ALLOC(h->Mfwd, (size_t)c.n2 * c.n1 * c.n1 * sizeof(float));
+    }
+    ALLOC(h->kr2_d, (size_t)S * sizeof(double));
+    ALLOC(h->w2n2_d, (size_t)2 * c.n0 * sizeof(double));
+    ALLOC(h->kg_d, (size_t)c.n0 * sizeof(double));
+    ALLOC(h->red, 4 * sizeof(float));
+#undef ALLOC
+    if (e != cudaSuccess) {
+        uppe_set_error(nullptr, "device allocation failed: %s", cudaGetErrorString(e));
+        free_buffers(h);
+        delete h;
+        return UPPE_E_NOMEM;
+    }
+    // twiddle table tw[j] = exp(-2 pi i j / NT), computed in FP64
+    const int NT = 1 << h->twLog;
+    std::vector<float2> tw(NT);
+    for (int j = 0; j < NT; ++j) {
+        double a = -2.0 * M_PI * (double)j / (double)NT;
+        tw[j] = make_float2((float)cos(a), (float)sin(a));
+    }
+    e = cudaMemcpy(h->tw, tw.data(), NT * sizeof(float2), cudaMemcpyHostToDevice);
+    // Allow the kernels that stage a whole slice / time tile in shared memory the full 227 KB; each
+    // launch still requests only what its grid needs.
+    if (e == cudaSuccess) e = uppe_configure_slice_kernels(227 * 1024);
+    if (e == cudaSuccess) e = uppe_configure_time_kernel(227 * 1024);
+    if (e != cudaSuccess) {
+        uppe_set_error(nullptr, "device set-up failed: %s", cudaGetErrorString(e));
+        free_buffers(h);
+        delete h;
+        return UPPE_E_CUDA;
+    }
+    *out = h;
+    return UPPE_OK;
+}
+
+extern "C" int uppe_destroy(UppeHandle* h) {
+    if (!h) return UPPE_OK;
+    free_buffers(h);
+    delete h;
+    return UPPE_OK;
+}
+
+extern "C" int uppe_set_stream(UppeHandle* h, void* stream) {
+    if (!h) return UPPE_E_ARG;
+    h->stream = (cudaStream_t)stream;
+    return UPPE_OK;
+}
+
+extern "C" int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, const double* H, const double* Lambda) {
+    if (!h || !w || !kr2) return h ? (uppe_set_error(h, "uppe_set_grid: null table"), UPPE_E_ARG) : UPPE_E_ARG;
+    const UppeConfig& c = h->cfg;
+    if (w[0] != 0.0) {
+        uppe_set_error(h, "UPPE propagator requires frequency range [0,...]");
+        return UPPE_E_ARG;
+    }
+    std::vector<float> wf(h->N0), filt(h->N0);
+    for (int k = 0; k < h->N0; ++k) {
+        wf[k] = (float)w[k];
+        filt[k] = (k < c.nl_cut_on || k >= c.nl_cut_off) ? 0.f : 1.f;
+    }
+    CUDA_TRY(h, cudaMemcpy(h->w, wf.data(), h->N0 * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(h->nlfilt, filt.data(), h->N0 * sizeof(float), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(h->kr2_d, kr2, (size_t)h->S * sizeof(double), cudaMemcpyHostToDevice));
+    if (c.cylindrical) {
+        if (!H || !Lambda) {
+            uppe_set_error(h, "cylindrical grid needs the Hankel basis and root-volume weights");
+            return UPPE_E_ARG;
+        }
+        const int Nr = h->N1, Nk = h->Nk, Nm = h->N2;
+        std::vector<float> Minv((size_t)Nm * Nr * Nk), Mfwd((size_t)Nm * Nr * Nr, 0.f);
+        // H layout (Nk, Nr, Nm) (grid_tools.py:294)
+        for (int m = 0; m < Nm; ++m)
+            for (int k = 0; k < Nk; ++k)
+                for (int r = 0; r < Nr; ++r) {
+                    double hv = H[((size_t)k * Nr + r) * Nm + m];
+                    Minv[((size_t)m * Nr + r) * Nk + k] = (float)(hv * Lambda[k] / Lambda[r]);
+                    Mfwd[((size_t)m * Nr + k) * Nr + r] = (float)(hv * Lambda[r] / Lambda[k]);
+                }
+        CUDA_TRY(h, cudaMemcpy(h->Minv, Minv.data(), Minv.size() * sizeof(float), cudaMemcpyHostToDevice));
+        CUDA_TRY(h, cudaMemcpy(h->Mfwd, Mfwd.data(), Mfwd.size() * sizeof(float), cudaMemcpyHostToDevice));
+    }
+    h->have_grid = 1;
+    return UPPE_OK;
+}
+
+extern "C" int uppe_set_material(UppeHandle* h, const double* w2n2, const double* kg, const double* ng) {
+    if (!h) return UPPE_E_ARG;
+    if (!h->have_grid) {
+        uppe_set_error(h, "uppe_set_material before uppe_set_grid");
+        return UPPE_E_ARG;
+    }
+    if (!w2n2 || !kg || !ng) {
+        uppe_set_error(h, "uppe_set_material: null table");
+        return UPPE_E_ARG;
+    }
+    std::vector<float> ngf(h->S);
+    for (int s = 0; s < h->S; ++s) ngf[s] = (float)ng[s];
+    CUDA_TRY(h, cudaMemcpyAsync(h->w2n2_d, w2n2, 2 * h->N0 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->kg_d, kg, h->N0 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->ng, ngf.data(), h->S * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, launch_build_operator(h));
+    // exact max |Re kz + kg| and max Im kz of the new operator, for the range checks
+    const float init[4] = {0.f, 0.f, 0.f, 0.f};
+    CUDA_TRY(h, cudaMemcpyAsync(h->red, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, launch_operator_bounds(h));
+    float red[4];
+    CUDA_TRY(h, cudaMemcpyAsync(red, h->red, sizeof(red), cudaMemcpyDeviceToHost, h->stream));
+    // the pageable host tables above must be consumed before returning
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    h->max_abs_K = red[0];
+    h->max_Ki = red[1];
+    h->have_material = 1;
+    return UPPE_OK;
+}
+
+static int check_ready(UppeHandle* h, bool need_field) {
+    if (!h->have_grid || !h->have_material) {
+        uppe_set_error(h, "grid and material must be set before propagating");
+        return UPPE_E_ARG;
+    }
+    if (need_field && !h->have_field) {
+        uppe_set_error(h, "no field loaded");
+        return UPPE_E_ARG;
+    }
+    return UPPE_OK;
+}
+
+static cudaError_t real_pass(UppeHandle* h, int mode, const float2* src, float2* A_out, StepArgs z) {
+    return h->cfg.cylindrical ? launch_real_cyl(h, mode, src, A_out, z) : launch_real_cart(h, mode, src, A_out, z);
+}
+
+static cudaError_t spec_pass(UppeHandle* h, int mode, const float2* src, float2* q_out, float2* qf, const float2* qi,
+                             float Cs, float Ce, StepArgs z) {
+    return h->cfg.cylindrical ? launch_spec_cyl(h, mode, src, q_out, qf, qi, Cs, Ce, z)
+                              : launch_spec_cart(h, mode, src, q_out, qf, qi, Cs, Ce, z);
+}
+
+// One source evaluation: J = sources(T^-1(...q...)) on the real side.
+static cudaError_t eval_to_J(UppeHandle* h, const float2* qsrc, StepArgs z) {
+    cudaError_t e = real_pass(h, REAL_E, qsrc, nullptr, z);
+    if (e != cudaSuccess) return e;
+    return launch_time_pass(h, TIME_J, h->E, h->J, nullptr);
+}
+
+extern "C" int uppe_load_field(UppeHandle* h, const void* a) {
+    if (!h || !a) return UPPE_E_ARG;
+    int rc = check_ready(h, false);
+    if (rc) return rc;
+    StepArgs z = split_z(h, 0.0);
+    CUDA_TRY(h, spec_pass(h, SPEC_LOAD, (const float2*)a, h->qi, nullptr, nullptr, 0.f, 0.f, z));
+    h->have_field = 1;
+    return UPPE_OK;
+}
+
+// Range limits of the representation, checked on the host before work is issued:
+//  - the float-float phase reduction is exact while |K z| < 2^24 rad (about 1.6e7 rad);
+//  - the interaction-picture amplitude grows as exp(Im kz z), which must stay inside FP32 range.
+static int check_range(UppeHandle* h, double z) {
+    const double az = fabs(z);
+    if (h->cfg.precision == UPPE_PREC_MIXED && h->max_abs_K * az >= 1.6e7) {
+        uppe_set_error(h, "propagator phase |(kz+kg) z| = %.3g rad exceeds the 1.6e7 rad of the float-float phase",
+                       h->max_abs_K * az);
+        return UPPE_E_RANGE;
+    }
+    if (h->max_Ki * az > 80.0) {
+        uppe_set_error(h, "Im(kz) z = %.3g: the interaction-picture amplitude exp(Im(kz) z) leaves FP32 range",
+                       h->max_Ki * az);
+        return UPPE_E_RANGE;
+    }
+    return UPPE_OK;
+}
+
+extern "C" int uppe_rk4_step(UppeHandle* h, double z_phase, double L, double z_sub, double dzmin, double* dz_out) {
+    if (!h) return UPPE_E_ARG;
+    int rc = check_ready(h, true);
+    if (rc) return rc;
+    if (!(L > 0.0)) {
+        uppe_set_error(h, "subcycle length must be positive");
+        return UPPE_E_ARG;
+    }
+    double dz;
+    const bool adaptive = !(dzmin >= L - z_sub);
+    rc = check_range(h, z_phase + (L - z_sub));
+    if (rc) return rc;
+    if (adaptive) {
+        StepArgs z = split_z(h, z_phase);
+        CUDA_TRY(h, eval_to_J(h, h->qi, z));
+        CUDA_TRY(h, spec_pass(h, SPEC_STORE_K, h->J, h->k1, nullptr, nullptr, 0.f, 0.f, z));
+        const float init[4] = {0.f, INFINITY, 0.f, 0.f};
+        CUDA_TRY(h, cudaMemcpyAsync(h->red, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+        CUDA_TRY(h, launch_absmax(h, h->qi));
+        CUDA_TRY(h, launch_step_size(h, h->qi, h->k1, L, 0.4, 1e-2));
+        float red[4];
+        CUDA_TRY(h, cudaMemcpyAsync(red, h->red, sizeof(red), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        dz = (double)red[1];
+        if (dz < dzmin) dz = dzmin;
+        if (z_sub + dz > L) dz = L - z_sub;
+        CUDA_TRY(h, launch_apply_stage1(h, (float)(dz / 6), (float)(dz / 2)));
+    } else {
+        dz = L - z_sub;
+        StepArgs z = split_z(h, z_phase);
+        CUDA_TRY(h, eval_to_J(h, h->qi, z));
+        CUDA_TRY(h, spec_pass(h, SPEC_STAGE1, h->J, h->q, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z));
+    }
+    {
+        StepArgs z = split_z(h, z_phase + 0.5 * dz);
+        CUDA_TRY(h, eval_to_J(h, h->q, z));
+        CUDA_TRY(h, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), z));
+        CUDA_TRY(h, eval_to_J(h, h->q, z));
+        CUDA_TRY(h, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)dz, z));
+    }
+    {
+        StepArgs z = split_z(h, z_phase + dz);
+        CUDA_TRY(h, eval_to_J(h, h->q, z));
+        CUDA_TRY(h, spec_pass(h, SPEC_FINISH, h->J, h->qi, h->qf, nullptr, (float)(dz / 6), 0.f, z));
+    }
+    if (dz_out) *dz_out = dz;
+    return UPPE_OK;
+}
+
+extern "C" int uppe_finish(UppeHandle* h, double z_phase, void* A, void* J, void* chi_w, void* ne_w) {
+    if (!h) return UPPE_E_ARG;
+    int rc = check_ready(h, true);
+    if (rc) return rc;
+    rc = check_range(h, z_phase);
+    if (rc) return rc;
+    StepArgs z = split_z(h, z_phase);
+    CUDA_TRY(h, real_pass(h, REAL_FINISH, h->qi, (float2*)A, z));
+    CUDA_TRY(h, launch_time_pass(h, TIME_J, h->E, J ? (float2*)J : h->J, nullptr));
+    if (chi_w || ne_w) CUDA_TRY(h, launch_time_pass(h, TIME_CHI_NE, h->E, (float2*)chi_w, (float2*)ne_w));
+    return UPPE_OK;
+}
+
+extern "C" int uppe_eval_rhs(UppeHandle* h, const void* q_in, double z_phase, void* S_out) {
+    if (!h || !q_in || !S_out) return UPPE_E_ARG;
+    int rc = check_ready(h, false);
+    if (rc) return rc;
+    rc = check_range(h, z_phase);
+    if (rc) return rc;
+    StepArgs z = split_z(h, z_phase);
+    CUDA_TRY(h, eval_to_J(h, (const float2*)q_in, z));
+    CUDA_TRY(h, spec_pass(h, SPEC_STORE_K, h->J, (float2*)S_out, nullptr, nullptr, 0.f, 0.f, z));
+    return UPPE_OK;
+}
+
+extern "C" int uppe_get_field(UppeHandle* h, void* q_out) {
+    if (!h || !q_out) return UPPE_E_ARG;
+    int rc = check_ready(h, true);
+    if (rc) return rc;
+    CUDA_TRY(h, cudaMemcpyAsync(q_out, h->qi, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
+    return UPPE_OK;
+}
+
+extern "C" int uppe_check_finite(UppeHandle* h, int* nonfinite) {
+    if (!h || !nonfinite) return UPPE_E_ARG;
+    int rc = check_ready(h, true);
+    if (rc) return rc;
+    const float init[4] = {0.f, INFINITY, 0.f, 0.f};
+    CUDA_TRY(h, cudaMemcpyAsync(h->red, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, launch_absmax(h, h->qi));
+    float red[4];
+    CUDA_TRY(h, cudaMemcpyAsync(red, h->red, sizeof(red), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    *nonfinite = (red[2] != 0.f) ? 1 : 0;
+    return UPPE_OK;
+}
+
+extern "C" const char* uppe_last_error(const UppeHandle* h) { return h ? h->err : g_create_error; }

@@ -1,0 +1,106 @@
+// Shared device helpers for the GB300 UPPE propagator: complex arithmetic on float2, float-float
+// ("double-single") arithmetic for the FP64-grade islands, and the propagator phase.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define UPPE_DEV __device__ __forceinline__
+
+UPPE_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+UPPE_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+UPPE_DEV float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+UPPE_DEV float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+UPPE_DEV float2 cconj(float2 a) { return make_float2(a.x, -a.y); }
+// multiply by +i / -i
+UPPE_DEV float2 cmul_i(float2 a) { return make_float2(-a.y, a.x); }
+UPPE_DEV float2 cmul_mi(float2 a) { return make_float2(a.y, -a.x); }
+// a / b for complex b
+UPPE_DEV float2 cdiv(float2 a, float2 b) {
+    float d = b.x * b.x + b.y * b.y;
+    return make_float2((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+// ---------------------------------------------------------------------------------------------
+// float-float arithmetic.  GB300 runs FP64 at a small fraction of its FP32 rate, so the two places
+// that need more than FP32 (the (kz+kg)z phase over long z and the time-integrated ionization
+// density) carry a value as an unevaluated sum hi + lo of two floats, about 48 significant bits.
+// Error-free transformations: Knuth's two-sum and the FMA-based two-product.
+// ---------------------------------------------------------------------------------------------
+struct ffloat {
+    float hi, lo;
+};
+
+UPPE_DEV ffloat ff_two_sum(float a, float b) {
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return {s, e};
+}
+
+UPPE_DEV ffloat ff_quick(float a, float b) {
+    float s = a + b;
+    float e = b - (s - a);
+    return {s, e};
+}
+
+UPPE_DEV ffloat ff_add(ffloat a, ffloat b) {
+    ffloat s = ff_two_sum(a.hi, b.hi);
+    float e = s.lo + (a.lo + b.lo);
+    return ff_quick(s.hi, e);
+}
+
+UPPE_DEV ffloat ff_add_f(ffloat a, float b) {
+    ffloat s = ff_two_sum(a.hi, b);
+    float e = s.lo + a.lo;
+    return ff_quick(s.hi, e);
+}
+
+UPPE_DEV float ff_value(ffloat a) { return a.hi + a.lo; }
+
+// 2*pi split in three floats (Cody-Waite): TWO_PI_A has its low bits clear enough that n*TWO_PI_A
+// subtracted from a float phase with an FMA is exact for |phase| < 2^24.
+#define UPPE_TWO_PI_A 6.28318548202514648437e+00f
+#define UPPE_TWO_PI_B -1.74845553146951715461e-07f
+#define UPPE_INV_TWO_PI 1.59154943091895335769e-01f
+
+// Phase (K z) mod 2*pi from K = Khi + Klo and z = zhi + zlo, each a float-float value.
+// The product is formed with an exact two-product of the high parts; the result is accurate to
+// about 3e-7 rad for |K z| up to ~1e8 rad.
+UPPE_DEV float ff_phase(float Khi, float Klo, float zhi, float zlo) {
+    float p = Khi * zhi;
+    float e = fmaf(Khi, zhi, -p);
+    e = fmaf(Khi, zlo, e);
+    e = fmaf(Klo, zhi, e);
+    float n = rintf(p * UPPE_INV_TWO_PI);
+    float r = fmaf(-n, UPPE_TWO_PI_A, p);
+    r = fmaf(-n, UPPE_TWO_PI_B, r);
+    return r + e;
+}
+
+// Per-point linear operator, built once per material update:
+//   x = high part of K = Re(kz) + kg,  y = low part of K,  z = Re(kz),  w = Im(kz)
+// The propagator factor exp(i (kz + kg) z) = exp(-Im(kz) z) * exp(i K z).
+struct PhaseArgs {
+    float zhi, zlo;  // z as float-float
+    int plain;       // 1: plain FP32 phase K*z (no float-float), for the plain-FP32 form
+};
+
+UPPE_DEV float2 propagator_factor(float4 op, PhaseArgs pa, float sign) {
+    float ph;
+    if (pa.plain) {
+        ph = op.x * (pa.zhi + pa.zlo);
+    } else {
+        ph = ff_phase(op.x, op.y, pa.zhi, pa.zlo);
+    }
+    float s, c;
+    sincosf(ph, &s, &c);
+    // sign=+1: exp(i K z) exp(-Ki z);  sign=-1: exp(-i K z) exp(+Ki z)
+    float amp = expf(-sign * op.w * (pa.zhi + pa.zlo));
+    return make_float2(amp * c, sign * amp * s);
+}
+
+__host__ __device__ inline int ilog2_exact(int n) {
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    return l;
+}

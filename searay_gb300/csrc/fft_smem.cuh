@@ -1,0 +1,142 @@
+// In-place, mixed-radix Stockham FFT on data held in shared memory, executed cooperatively by all
+// threads of a CTA.  Used by every transform of the propagator: the transverse 2D FFTs of one
+// frequency slice and the time-axis real FFTs of a tile of transverse points.
+//
+// Data: `nb` transforms of length N = 2^logN; element e of transform b sits at buf[b*bs + e*es].
+// One radix-R stage (p = product of the radices already applied, k = i mod p):
+//     u_r = buf[i + r N/R] * W_{pR}^{r k},  y = DFT_R(u),  buf'[(i-k)R + k + s p] = y_s
+// which leaves the result in natural order after the last stage.  Each stage reads all of its
+// inputs into registers, synchronises, then writes in place, so no second buffer is needed.
+// Twiddles come from a table tw[j] = exp(-2 pi i j / NT) (computed in FP64 on the host), NT = 2^twLog
+// >= N; the inverse transform uses conjugated twiddles and is unnormalised.
+#pragma once
+#include "common.cuh"
+
+#define UPPE_SQRT1_2 0.70710678118654752440f
+
+template <int R>
+UPPE_DEV void dft_small(float2 (&u)[R], bool inv);
+
+template <>
+UPPE_DEV void dft_small<2>(float2 (&u)[2], bool) {
+    float2 a = u[0], b = u[1];
+    u[0] = cadd(a, b);
+    u[1] = csub(a, b);
+}
+
+template <>
+UPPE_DEV void dft_small<4>(float2 (&u)[4], bool inv) {
+    float2 a0 = cadd(u[0], u[2]), a1 = csub(u[0], u[2]);
+    float2 a2 = cadd(u[1], u[3]), a3 = csub(u[1], u[3]);
+    // forward: y1 = a1 - i a3, y3 = a1 + i a3; inverse: signs swapped
+    float2 t = inv ? cmul_i(a3) : cmul_mi(a3);
+    u[0] = cadd(a0, a2);
+    u[2] = csub(a0, a2);
+    u[1] = cadd(a1, t);
+    u[3] = csub(a1, t);
+}
+
+template <>
+UPPE_DEV void dft_small<8>(float2 (&u)[8], bool inv) {
+    float2 e[4] = {u[0], u[2], u[4], u[6]};
+    float2 o[4] = {u[1], u[3], u[5], u[7]};
+    dft_small<4>(e, inv);
+    dft_small<4>(o, inv);
+    const float sg = inv ? 1.f : -1.f;
+    // W8^s = exp(sg * 2 pi i s / 8)
+    float2 w1 = make_float2(UPPE_SQRT1_2, sg * UPPE_SQRT1_2);
+    float2 w3 = make_float2(-UPPE_SQRT1_2, sg * UPPE_SQRT1_2);
+    float2 t0 = o[0];
+    float2 t1 = cmul(o[1], w1);
+    float2 t2 = inv ? cmul_i(o[2]) : cmul_mi(o[2]);
+    float2 t3 = cmul(o[3], w3);
+    u[0] = cadd(e[0], t0);
+    u[4] = csub(e[0], t0);
+    u[1] = cadd(e[1], t1);
+    u[5] = csub(e[1], t1);
+    u[2] = cadd(e[2], t2);
+    u[6] = csub(e[2], t2);
+    u[3] = cadd(e[3], t3);
+    u[7] = csub(e[3], t3);
+}
+
+// One radix-R stage over all nb transforms; thread `tid` of `nthr` handles ITEMS butterflies.
+// batch_fast: consecutive threads take consecutive transforms (use when es != 1 so that the
+// accesses of a warp are contiguous in shared memory).
+template <int R, int ITEMS>
+UPPE_DEV void stockham_stage(float2* buf, int logN, int logp, int lognb, int bs, int es,
+                             const float2* __restrict__ tw, int twLog, bool inv, bool batch_fast,
+                             int tid, int nthr) {
+    constexpr int LOGR = (R == 2) ? 1 : (R == 4) ? 2 : 3;
+    const int logq = logN - LOGR;
+    const int nq = 1 << logq;
+    const int p = 1 << logp;
+    float2 u[ITEMS][R];
+    int dst[ITEMS];
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+        const int g = tid + it * nthr;
+        int b, i;
+        if (batch_fast) {
+            b = g & ((1 << lognb) - 1);
+            i = g >> lognb;
+        } else {
+            i = g & (nq - 1);
+            b = g >> logq;
+        }
+        const int k = i & (p - 1);
+        const float2* base = buf + b * bs;
+#pragma unroll
+        for (int r = 0; r < R; ++r) u[it][r] = base[(i + r * nq) * es];
+        if (logp > 0) {
+            const int sh = twLog - logp - LOGR;  // NT / (p R)
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 w = __ldg(&tw[(r * k) << sh]);
+                if (inv) w.y = -w.y;
+                u[it][r] = cmul(u[it][r], w);
+            }
+        }
+        dft_small<R>(u[it], inv);
+        dst[it] = b * bs + (((i - k) << LOGR) + k) * es;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) buf[dst[it] + r * p * es] = u[it][r];
+    }
+    __syncthreads();
+}
+
+// Full transform along one axis.  ET = elements per thread = nb*N/nthr (compile time); radix 8
+// stages first, then one radix-4 or radix-2 stage for the remainder.
+template <int ET>
+UPPE_DEV void fft_axis(float2* buf, int logN, int lognb, int bs, int es, const float2* __restrict__ tw,
+                       int twLog, bool inv, int tid, int nthr) {
+    const bool batch_fast = (es != 1);
+    int logp = 0;
+    while (logp < logN) {
+        const int rem = logN - logp;
+        if constexpr (ET >= 8) {
+            if (rem >= 3) {
+                stockham_stage<8, ET / 8>(buf, logN, logp, lognb, bs, es, tw, twLog, inv, batch_fast, tid, nthr);
+                logp += 3;
+                continue;
+            }
+        }
+        if constexpr (ET >= 4) {
+            if (rem >= 2) {
+                stockham_stage<4, ET / 4>(buf, logN, logp, lognb, bs, es, tw, twLog, inv, batch_fast, tid, nthr);
+                logp += 2;
+                continue;
+            }
+        }
+        if constexpr (ET >= 2) {
+            stockham_stage<2, ET / 2>(buf, logN, logp, lognb, bs, es, tw, twLog, inv, batch_fast, tid, nthr);
+            logp += 1;
+        } else {
+            break;  // unreachable for valid launches (ET >= 2 whenever logN >= 1)
+        }
+    }
+}

@@ -1,0 +1,81 @@
+// Internal interfaces between the translation units of libsearay_uppe: the handle and the launch
+// wrappers of each kernel family.  Not part of the C ABI (see include/searay_uppe.h).
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/searay_uppe.h"
+
+// Modes of the spectral-side kernels.
+enum UppeSpecMode {
+    SPEC_LOAD = 0,      // initial kspacex of the incoming field: q <- T(a)
+    SPEC_STORE_K = 1,   // k1 <- S(J)                               (adaptive first stage)
+    SPEC_STAGE1 = 2,    // q <- qi + Ce S ; qf <- qi + Cs S
+    SPEC_STAGE23 = 3,   // q <- qi + Ce S ; qf <- qf + Cs S
+    SPEC_FINISH = 4,    // qi <- qf + Cs S
+};
+
+// Modes of the real-side kernels (inverse transverse transform).
+enum UppeRealMode {
+    REAL_E = 0,       // E <- T^-1( i kz exp(i(kz+kg)z) q )
+    REAL_FINISH = 1,  // A <- T^-1( exp(i(kz+kg)z) q ) and E <- i kz A   (uppe_kernel.py:250-253)
+};
+
+// Modes of the time-axis pass.
+enum UppeTimeMode {
+    TIME_J = 0,       // J(w) from E(w): Kerr + plasma current, NL filter
+    TIME_CHI_NE = 1,  // rfft of chi(t) and ne(t) (diagnostic outputs of finish)
+};
+
+struct StepArgs {
+    float zhi, zlo;
+    int plain;
+};
+
+struct UppeHandle {
+    UppeConfig cfg;
+    int N0, N1, N2, Nk, Nt, M, S;  // S = N1*N2 transverse points
+    size_t P;                      // N0*N1*N2
+    int twLog;                     // twiddle table size 2^twLog
+    int time_cols;                 // transverse points per CTA in the time pass
+    cudaStream_t stream;
+    // library-owned device buffers
+    float2 *q, *qi, *qf, *k1, *E, *J, *scratch;
+    float4* op;
+    float* ng;
+    float2* tw;
+    float* w;        // omega per bin (FP32)
+    float* nlfilt;   // NL filter per bin
+    float* Minv;     // cylindrical: [N2][Nr][Nk]
+    float* Mfwd;     // cylindrical: [N2][Nr][Nr] (rows >= Nk zero)
+    double* kr2_d;   // [S] transverse eigenvalues (FP64)
+    double* w2n2_d;  // [N0] complex w^2 (1 + chi0) interleaved
+    double* kg_d;    // [N0]
+    float* red;      // reduction scalars: [0] max|q|, [1] min dz, [2] nonfinite flag
+    int have_grid, have_material, have_field;
+    double max_abs_K;   // max |Re kz + kg| of the current operator
+    double max_Ki;      // max Im kz of the current operator
+    char err[512];
+};
+
+int uppe_set_error(UppeHandle* h, const char* fmt, ...);
+
+// ---- kernel launch wrappers (uppe_kernels.cu) ----
+cudaError_t launch_build_operator(UppeHandle* h);
+cudaError_t launch_operator_bounds(UppeHandle* h);  // red[0] = max |K|, red[1] = max Im kz
+cudaError_t uppe_configure_slice_kernels(size_t smem_bytes);
+cudaError_t uppe_configure_time_kernel(size_t smem_bytes);
+cudaError_t launch_real_cart(UppeHandle* h, int mode, const float2* src, float2* A_out, StepArgs z);
+cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, float2* q_out, float2* qf_io,
+                             const float2* qi, float Cs, float Ce, StepArgs z);
+cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1);
+cudaError_t launch_absmax(UppeHandle* h, const float2* q);
+cudaError_t launch_step_size(UppeHandle* h, const float2* q, const float2* k, double L, double dphi, double rel_amin);
+cudaError_t launch_apply_stage1(UppeHandle* h, float Cs, float Ce);
+cudaError_t launch_ikz(UppeHandle* h, const float2* A, float2* E);
+
+// ---- cylindrical transverse transform (hankel.cu) ----
+cudaError_t launch_real_cyl(UppeHandle* h, int mode, const float2* src, float2* A_out, StepArgs z);
+cudaError_t launch_spec_cyl(UppeHandle* h, int mode, const float2* src_real, float2* q_out, float2* qf_io,
+                            const float2* qi, float Cs, float Ce, StepArgs z);

@@ -1,0 +1,273 @@
+"""Host side of the GB300 UPPE propagator: a drop-in for SeaRay's ``modules/uppe_kernel.py``.
+
+``track(cl, xp, eikonal, vg, vol_dict)`` keeps the reference's signature, input-dictionary keys,
+checks and return values (``uppe_kernel.py:333-424``), so ``volume.nonuniform_volume.Propagate``
+(``modules/volume.py:606-612``) can call it in place of ``uppe_kernel.track``.  The device work
+goes through the C ABI of ``libsearay_uppe.so`` (``include/searay_uppe.h``); there is no CPU
+fallback.  Device memory and the stream come from PyTorch.
+
+Extra, optional dictionary keys (ignored by the reference):
+  ``'precision'``: ``'mixed'`` (default: FP32 transforms and sources, float-float phase and
+  density scan) or ``'fp32'`` (plain FP32 everywhere).
+"""
+import ctypes
+import logging
+
+import numpy as np
+import torch
+
+from . import _native
+from .grid import VolumeGrid, cell_centers, cell_walls
+from .ionization import RateCoefficients
+
+_POW2 = [2 ** i for i in range(32)]
+
+
+def _check_grid(N):
+    """The grid checks of uppe_kernel.py:354-360."""
+    if N[0] - 1 not in _POW2:
+        raise ValueError("UPPE propagator requires 2**n+1 w-nodes")
+    if N[1] not in _POW2:
+        raise ValueError("UPPE propagator requires 2**n x-nodes")
+    if N[2] not in _POW2:
+        raise ValueError("UPPE propagator requires 2**n y-nodes")
+
+
+class DeviceGrid:
+    """A C handle for one volume grid plus its device field buffers (Source of uppe_kernel.py:92-129)."""
+
+    def __init__(self, grid, vol_dict, rates=None, precision="mixed", stream=None):
+        lib = _native.lib()
+        if not torch.cuda.is_available():
+            raise RuntimeError("the GB300 UPPE propagator needs a CUDA device")
+        self.grid = grid
+        self.N = grid.N
+        nl = vol_dict["nonlinear band"]
+        cfg = _native.UppeConfig()
+        cfg.n0, cfg.n1, cfg.n2 = grid.N[0], grid.N[1], grid.N[2]
+        cfg.radial_modes = 0 if grid.cartesian else grid.Nk
+        cfg.cylindrical = 0 if grid.cartesian else 1
+        if precision not in ("mixed", "fp32"):
+            raise ValueError("precision must be 'mixed' or 'fp32'")
+        cfg.precision = _native.PREC_MIXED if precision == "mixed" else _native.PREC_FP32
+        cfg.dt = grid.dt
+        cfg.chi3_over_nref = vol_dict.get("chi3", 0.0) / vol_dict["density reference"]
+        cfg.nl_cut_on = int(nl[0] / grid.dw)
+        cfg.nl_cut_off = int(nl[1] / grid.dw)
+        cfg.damping = 0.1
+        cfg.window_cutoff = 4
+        cfg.window_width = 64
+        cfg.field_cutoff = 1e-3
+        if rates is None:
+            cfg.rate_form = _native.RATE_NONE
+        else:
+            cfg.field_conv = rates.field_conv
+            cfg.rate_conv = rates.rate_conv
+            cfg.field_cutoff = rates.cutoff
+            if rates.explicit:
+                cfg.rate_form = _native.RATE_EXPLICIT
+                cfg.c_pre, cfg.c_pow, cfg.c_exp = rates.C1, rates.C2, rates.C3
+            else:
+                cfg.rate_form = _native.RATE_SERIES
+                for i in range(6):
+                    cfg.clog[i] = float(rates.clog[i])
+        self.cfg = cfg
+        h = ctypes.c_void_p()
+        _native.check(lib.uppe_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self.lib = lib
+        s = torch.cuda.current_stream() if stream is None else stream
+        self.stream = s
+        self._check(lib.uppe_set_stream(h, ctypes.c_void_p(s.cuda_stream)))
+        w = np.ascontiguousarray(grid.w, dtype=np.float64)
+        kr2 = np.ascontiguousarray(grid.kr2, dtype=np.float64)
+        H = None if grid.H is None else np.ascontiguousarray(grid.H, dtype=np.float64)
+        lam = None if grid.Lambda is None else np.ascontiguousarray(grid.Lambda, dtype=np.float64)
+        self._check(lib.uppe_set_grid(h, _native.dptr(w), _native.dptr(kr2), _native.dptr(H), _native.dptr(lam)))
+        self._last_material = None
+
+    def _check(self, rc):
+        return _native.check(rc, self.h)
+
+    def close(self):
+        if getattr(self, "h", None) is not None and self.h.value:
+            self.lib.uppe_destroy(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- device calls ----
+    def set_material(self, w2n2, kg, ng):
+        key = (w2n2.tobytes(), kg.tobytes(), ng.tobytes())
+        if key == self._last_material:
+            return False
+        w2n2 = np.ascontiguousarray(np.stack([w2n2.real, w2n2.imag], axis=-1).reshape(-1), dtype=np.float64)
+        self._check(self.lib.uppe_set_material(self.h, _native.dptr(w2n2), _native.dptr(np.ascontiguousarray(kg, dtype=np.float64)),
+                                               _native.dptr(np.ascontiguousarray(ng, dtype=np.float64))))
+        self._last_material = key
+        return True
+
+    def load_field(self, a_dev):
+        assert a_dev.dtype == torch.complex64 and a_dev.is_contiguous() and tuple(a_dev.shape) == tuple(self.N[:3])
+        self._check(self.lib.uppe_load_field(self.h, ctypes.c_void_p(a_dev.data_ptr())))
+
+    def rk4_step(self, z_phase, L, z_sub, dzmin):
+        dz = ctypes.c_double()
+        self._check(self.lib.uppe_rk4_step(self.h, z_phase, L, z_sub, dzmin, ctypes.byref(dz)))
+        return dz.value
+
+    def finish(self, z_phase, A=None, J=None, chi=None, ne=None):
+        p = lambda t: None if t is None else ctypes.c_void_p(t.data_ptr())
+        self._check(self.lib.uppe_finish(self.h, z_phase, p(A), p(J), p(chi), p(ne)))
+
+    def eval_rhs(self, q_dev, z_phase, S_dev):
+        self._check(self.lib.uppe_eval_rhs(self.h, ctypes.c_void_p(q_dev.data_ptr()), z_phase, ctypes.c_void_p(S_dev.data_ptr())))
+
+    def get_field(self, q_dev):
+        self._check(self.lib.uppe_get_field(self.h, ctypes.c_void_p(q_dev.data_ptr())))
+
+    def nonfinite(self):
+        flag = ctypes.c_int()
+        self._check(self.lib.uppe_check_finite(self.h, ctypes.byref(flag)))
+        return bool(flag.value)
+
+    def empty_field(self):
+        return torch.empty(tuple(self.N[:3]), dtype=torch.complex64, device="cuda")
+
+
+class Material:
+    """Medium at one z: chi0(w), kz, kGalileo and the gas density plane (uppe_kernel.py:32-90).
+    The host computes the density plane and chi0; kz is built on the device (uppe_set_material)."""
+
+    def __init__(self, dev, grid, coords, vol, chi, chi3, nref, vg, density_lambda=None):
+        N = grid.N
+        self.dev = dev
+        self.grid = grid
+        self.chi = chi
+        self.w = grid.w
+        self.redchi3 = chi3 / nref
+        self.n_ref = nref
+        self.vg = vg
+        self.xp_eff = np.zeros((N[1], N[2], 8))
+        if coords == "cartesian":
+            self.xp_eff[..., 1] = np.outer(grid.x1, np.ones(N[2]))
+            self.xp_eff[..., 2] = np.outer(np.ones(N[1]), grid.x2)
+        else:
+            self.xp_eff[..., 1] = np.outer(grid.x1, np.cos(grid.x2))
+            self.xp_eff[..., 2] = np.outer(grid.x1, np.sin(grid.x2))
+        if vol is not None and hasattr(vol, "GetRelDensity"):
+            self.rel_density = vol.GetRelDensity
+        elif density_lambda is not None:
+            def rel(xp):
+                r2 = np.einsum("...i,...i", xp[..., 1:3], xp[..., 1:3])
+                return density_lambda(xp[..., 1], xp[..., 2], xp[..., 3], r2)
+            self.rel_density = rel
+        else:
+            raise ValueError("the volume needs an 'object' with GetRelDensity or a 'density lambda'")
+        self.kg = np.ascontiguousarray(-self.w / self.vg, dtype=np.float64)
+
+    def UpdateMaterial(self, z):
+        self.xp_eff[..., 3] = z
+        dens = self.rel_density(self.xp_eff)
+        chi0 = np.copy(self.chi)
+        chi0[np.where(np.real(self.chi) > 0.0)] *= np.min(dens)
+        chi0[np.where(np.real(self.chi) < 0.0)] *= np.max(dens)
+        w2n2 = self.w ** 2 * (1 + chi0)
+        ng = np.ascontiguousarray(self.n_ref * np.broadcast_to(dens, self.grid.N[1:3]), dtype=np.float64)
+        return self.dev.set_material(np.asarray(w2n2, dtype=np.complex128), self.kg, ng)
+
+
+def propagator(dev, mat, a_dev, subcycles, zi, zf, dzmin, outputs=None):
+    """Advance the real-space field a to the next diagnostic plane (uppe_kernel.py:260-331).
+    Returns device tensors (A, J, chiNL_w, ne_w) and the number of RHS evaluations."""
+    if dev.grid.w[0] != 0.0:
+        raise ValueError("UPPE propagator requires frequency range [0,...]")
+    if dev.N[0] == 1:
+        raise ValueError("UPPE propagator cannot be used for monochromatic radiation.")
+    L = (zf - zi) / subcycles
+    dev.load_field(a_dev)
+    iterations = 0
+    for sub in range(subcycles):
+        z0 = zi + sub * L
+        z = 0.0
+        mat.UpdateMaterial(z0 + 0.5 * L)
+        while z < L and (z - L) ** 2 > (L / 1e6) ** 2:
+            dz = dev.rk4_step(z0 - zi + z, L, z, dzmin)
+            iterations += 1
+            z += dz
+    if outputs is None:
+        outputs = tuple(dev.empty_field() for _ in range(4))
+    A, J, chi, ne = outputs
+    dev.finish(zf - zi, A, J, chi, ne)
+    if dev.nonfinite():
+        logging.warning("UPPE field holds NaN or Inf after propagating to z=%g", zf)
+    return A, J, chi, ne, 4 * iterations
+
+
+def track(cl, xp, eikonal, vg, vol_dict):
+    """Propagate the UPPE volume's wave through its diagnostic planes (uppe_kernel.py:333-424).
+
+    :param cl: ignored (the reference's OpenCL bundle); the device is CUDA device 0 / current.
+    :param numpy.array xp: ray phase space (bundles, rays, 8), only used by the ray relaunch.
+    :param numpy.array eikonal: ray eikonal data (bundles, 4).
+    :param numpy.array vg: ray group velocity (bundles, rays, 4).
+    :param dict vol_dict: the volume's input dictionary.
+    :returns: A, J, chiNL, ne (complex128, shape ``wave grid``) and dom4d (8,)."""
+    band = vol_dict["frequency band"]
+    size = (band[1] - band[0],) + tuple(vol_dict["size"])
+    N = tuple(vol_dict["wave grid"])
+    diagnostic_steps = N[3] - 1
+    subcycles = vol_dict["subcycles"]
+    steps = diagnostic_steps * subcycles
+    A = np.zeros(N).astype(np.cdouble)
+    J = np.zeros(N).astype(np.cdouble)
+    chiNL = np.zeros(N).astype(np.cdouble)
+    ne = np.zeros(N).astype(np.cdouble)
+    _check_grid(N)
+    window_speed = vol_dict.get("window speed", 1.0)
+    chi3 = vol_dict.get("chi3", 0.0)
+
+    grid = VolumeGrid(vol_dict)
+    if "incoming wave" not in vol_dict:
+        raise NotImplementedError("UPPE start from ray data (GetBoundaryFields) is not built; "
+                                  "give the volume an 'incoming wave'")
+    logging.info("Start UPPE propagation using wave data")
+    A[..., 0] = vol_dict["incoming wave"](grid.w, grid.x1, grid.x2)
+
+    chi = vol_dict["dispersion inside"].chi(grid.w).astype(np.cdouble)
+    rates = None
+    if vol_dict.get("ionizer", None) is not None:
+        rates = RateCoefficients(vol_dict["ionizer"])
+    if vol_dict.get("rotator", None) is not None:
+        raise NotImplementedError("rotational Raman response (rotator) is not built in the GB300 propagator")
+
+    dev = DeviceGrid(grid, vol_dict, rates, vol_dict.get("precision", "mixed"))
+    try:
+        mat = Material(dev, grid, vol_dict["wave coordinates"], vol_dict.get("object", None), chi, chi3,
+                       vol_dict["density reference"], window_speed, vol_dict.get("density lambda", None))
+        dens_nodes = cell_centers(-size[3] / 2, size[3] / 2, steps)
+        field_walls = cell_walls(dens_nodes[0], dens_nodes[-1], steps)
+        diagnostic_walls = np.linspace(-size[3] / 2, size[3] / 2, N[3])
+        dzmin = vol_dict["minimum step"]
+        dom4d = np.concatenate((grid.plot_ext, [field_walls[0], field_walls[-1]]))
+
+        a_dev = torch.from_numpy(np.ascontiguousarray(A[..., 0], dtype=np.complex64)).to("cuda")
+        outs = tuple(dev.empty_field() for _ in range(4))
+        for k in range(diagnostic_steps):
+            zi = diagnostic_walls[k]
+            zf = diagnostic_walls[k + 1]
+            logging.info("Advancing to diagnostic plane %d", k + 1)
+            A0, J0, c0, n0, evals = propagator(dev, mat, a_dev, subcycles, zi, zf, dzmin, outs)
+            logging.info("%d evaluations of j(w,kx,ky)", evals)
+            A[..., k + 1] = A0.cpu().numpy()
+            J[..., k + 1] = J0.cpu().numpy()
+            chiNL[..., k + 1] = c0.cpu().numpy()
+            ne[..., k + 1] = n0.cpu().numpy()
+            a_dev, outs = A0, (dev.empty_field(), J0, c0, n0)
+    finally:
+        dev.close()
+    return A, J, chiNL, ne, dom4d

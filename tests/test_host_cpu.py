@@ -1,0 +1,85 @@
+"""Host-side set-up of the GB300 propagator against the oracle and the reference's fixtures and
+known answers (no GPU)."""
+import numpy as np
+import pytest
+
+import replay
+from oracle import uppe_oracle as O
+from searay_gb300 import dispersion, grid, ionization, uppe
+
+
+@pytest.mark.parametrize("name", replay.CASE_NAMES)
+def test_grid_matches_oracle(name):
+    vd, _ = replay.load_case(name)
+    g = grid.VolumeGrid(vd)
+    go = O.Grid(vd)
+    for attr in ("w", "x1", "x2", "kr2", "plot_ext"):
+        np.testing.assert_array_equal(getattr(g, attr), getattr(go, attr))
+    assert g.dt == go.dt and g.dw == go.dw
+    if not g.cartesian:
+        np.testing.assert_array_equal(g.H, go.H)
+        np.testing.assert_array_equal(g.Lambda, go.Lambda)
+
+
+def test_hankel_basis_matches_reference():
+    d = np.load(replay.HERE / "hankel_bases.npz")
+    for (Nr, dr, mmax, Nk) in ((32, 25.0, 0, 24), (16, 37.5, 2, 12)):
+        key = f"Nr{Nr}_mmax{mmax}_Nk{Nk}"
+        H, vals, lam = grid.hankel_eigenbasis(Nr, dr, mmax, Nk)
+        np.testing.assert_allclose(H, d[key + "_H"], rtol=0, atol=1e-13)
+        np.testing.assert_allclose(vals, d[key + "_vals"], rtol=1e-13)
+        # orthogonality H H^T = I for a full basis
+        Hf, _, _ = grid.hankel_eigenbasis(Nr, dr, mmax, Nr)
+        for m in range(Hf.shape[2]):
+            np.testing.assert_allclose(Hf[:, :, m] @ Hf[:, :, m].T, np.eye(Nr), atol=1e-12)
+
+
+@pytest.mark.parametrize("name", ["cart_ion", "cyl_az_adk", "cart_series"])
+def test_rate_coefficients_match_reference(name):
+    vd, exp = replay.load_case(name)
+    rc = ionization.RateCoefficients(vd["ionizer"])
+    ro = O.RateCoefficients(vd["ionizer"])
+    assert (rc.C1, rc.C2, rc.C3) == (ro.C1, ro.C2, ro.C3)
+    assert rc.field_conv == ro.field_conv and rc.rate_conv == ro.rate_conv
+    if not rc.explicit:
+        np.testing.assert_allclose(rc.clog, exp["rate"]["clog_reference"], rtol=1e-9)
+
+
+def test_simple_air_matches_reference_chi():
+    d = np.load(replay.HERE / "uppe_cart_ion.npz")
+    air = dispersion.SimpleAir(0.8e-6 / (2 * np.pi))
+    np.testing.assert_allclose(air.chi(d["w_nodes"]), d["chi_w"].real, rtol=1e-14, atol=0)
+
+
+def test_ionization_known_answers():
+    """The rate known answers of the reference's test/ionization_test.py:6-15."""
+    h = ionization.HydrogenAU(False, 0.5, 1.0, 0, 0, 0, 0)
+    assert h.Rate(0.1 - h.cutoff_field) == pytest.approx(0.0509, 1e-3)
+    au = ionization.AtomicUnits()
+    adk = ionization.ADKAU(True, au.energy_to_au(24.58741), 1.0)
+    assert adk.Rate(0.1 - adk.cutoff_field) == pytest.approx(4.546e-7, 1e-2)
+
+
+def test_rate_models_match_reference_classes():
+    from oracle.refshim import runner
+    if not runner.available():
+        pytest.skip("reference tree not present")
+    m = runner.modules()
+    x1 = 0.8e-6 / (2 * np.pi)
+    helper = m["input_tools"].InputHelper(x1)
+    U = helper.dnum("12.07 eV")
+    for mine, theirs in ((ionization.PPT_Tunneling(x1, False, U, 0.53), m["ionization"].PPT_Tunneling(x1, False, U, 0.53)),
+                         (ionization.ADK(x1, False, U, 1.0), m["ionization"].ADK(x1, False, U, 1.0))):
+        np.testing.assert_allclose(mine.GetCoeff(), theirs.GetCoeff(), rtol=1e-13)
+    air_ref = m["dispersion"].SimpleAir(x1)
+    w = np.linspace(0.1, 2.5, 50)
+    np.testing.assert_allclose(dispersion.SimpleAir(x1).GroupVelocityMagnitude(w), air_ref.GroupVelocityMagnitude(w), rtol=1e-13)
+
+
+def test_track_rejects_bad_grids_before_device_use():
+    vd, _ = replay.load_case("cart_ion")
+    for N, msg in (((128, 16, 16, 2), "w-nodes"), ((129, 12, 16, 2), "x-nodes"), ((129, 16, 24, 2), "y-nodes")):
+        v = dict(vd)
+        v["wave grid"] = N
+        with pytest.raises(ValueError, match=msg):
+            uppe.track(None, None, None, None, v)
