@@ -1,0 +1,344 @@
+"""Benchmark of the GB300 UPPE z-step: grid-pt*steps/s on the Cartesian filament workload.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload cart_filament_128] [--precision mixed|fp32]
+
+A "step" is one classic RK4 z-step (four right-hand-side evaluations) over the whole grid.
+The default workload is the Cartesian 128 x 128 x 513 filament (Kerr + O2 tunneling ionization +
+plasma current, 400 fixed steps over 10 cm; searay_gb300/workloads.py).
+
+value: P * K / (device time of K steps), fields resident in HBM, CUDA events on the library's stream.
+e2e:   the same metric through the reference-facing call searay_gb300.track() with host (NumPy)
+       input and outputs, host<->device copies and set-up inside the timed region.
+roofline: the kernel class with the largest share of the step, algorithmic bytes per launch over its
+       average event-timed duration, against the measured HBM copy bandwidth.
+cpu_baseline: the FP64 NumPy oracle (a restatement of the reference path) timed on the host cores
+       for one RK4 step of the same grid.
+--impl reference: the reference arm.  The reference (SeaRay) runs through PyOpenCL, which is not
+       available on the GPU machine; its CPU path is timed as the oracle port, one bounded RK4 step
+       per bench step.
+Multi-GPU (torchrun): the path does not shard; every rank runs an independent replica and value is
+the sum over ranks divided by the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "UPPE grid-pt*steps/s (RK4 z-step)"
+UNIT = "grid-pt*steps/s"
+# algorithmic HBM bytes per grid point per launch of each kernel class (complex64 fields,
+# 16-byte per-point operator {K_hi, K_lo, Re kz, Im kz})
+ALGO_BYTES = {
+    "transverse_inverse": 8 + 16 + 8,           # read q, op; write E
+    "time_pass": 8 + 8,                         # read E; write J
+    "transverse_forward_rk": (48 + 56 + 56 + 40) / 4.0,  # read J, op, qi|qf; write q, qf (stage mix)
+}
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.15)
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in out.strip().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 8:
+                continue
+            try:
+                sm.append(float(p[0]))
+                smax.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload):
+    """Per-launch DRAM bytes per kernel class from the committed ncu summary, if any."""
+    p = ROOT / "profiles" / f"traffic_{workload}.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {}
+
+
+def build_device(vd, precision):
+    from searay_gb300 import grid, ionization, uppe
+    g = grid.VolumeGrid(vd)
+    rates = ionization.RateCoefficients(vd["ionizer"]) if vd.get("ionizer") is not None else None
+    dev = uppe.DeviceGrid(g, vd, rates, precision)
+    chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+    mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0), vd["density reference"],
+                        vd.get("window speed", 1.0), vd["density lambda"])
+    return g, dev, mat
+
+
+def run_device(args, vd, ws, rank, local):
+    import torch
+    g, dev, mat = build_device(vd, args.precision)
+    P = int(np.prod(g.N[:3]))
+    Lz = vd["size"][2]
+    nsteps_cfg = vd["subcycles"]
+    dz = Lz / nsteps_cfg
+    a = vd["incoming wave"](g.w, g.x1, g.x2)
+    a_dev = torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex64)).cuda()
+    mat.UpdateMaterial(-Lz / 2 + 0.5 * dz)
+    dev.load_field(a_dev)
+    step = [0]
+
+    def one_step():
+        # fixed step: minimum step = subcycle length, so dz = L/steps exactly (uppe_kernel.py:224-227)
+        dev.rk4_step(step[0] * dz, dz, 0.0, dz)
+        step[0] += 1
+
+    for _ in range(args.warmup):
+        one_step()
+    torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = dev.launches()
+    stream = torch.cuda.current_stream()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t0.record(stream)
+    for _ in range(args.steps):
+        one_step()
+    t1.record(stream)
+    torch.cuda.synchronize()
+    ms = t0.elapsed_time(t1)
+    launches = dev.launches() - l0
+    if ws > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    finite = not dev.nonfinite()
+    # per-kernel-class timing (separate region; event records between launches)
+    nprof = min(args.steps, 20)
+    dev.profile(True)
+    for _ in range(nprof):
+        one_step()
+    prof = dev.profile_read()
+    dev.profile(False)
+    dev.close()
+    return P, ms, launches, clk, prof, finite
+
+
+def run_e2e(args, vd):
+    """K steps through track() with host input/outputs (one diagnostic interval)."""
+    import torch
+    from searay_gb300 import uppe
+    Lz = vd["size"][2]
+    dz = Lz / vd["subcycles"]
+    v = dict(vd)
+    v["size"] = (vd["size"][0], vd["size"][1], dz * args.steps)
+    v["subcycles"] = args.steps
+    v["minimum step"] = dz
+    warm = dict(v)
+    warm["size"] = (vd["size"][0], vd["size"][1], dz * 2)
+    warm["subcycles"] = 2
+    uppe.track(None, None, None, None, warm)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    A, J, chi, ne, dom = uppe.track(None, None, None, None, v)
+    wall = time.perf_counter() - t
+    N = v["wave grid"]
+    P = int(np.prod(N[:3]))
+    h2d = P * 8 + (2 * N[0] + N[0]) * 8 + N[1] * N[2] * 8
+    d2h = 4 * P * 8
+    return P * args.steps / wall, h2d, d2h, bool(np.isfinite(A[..., -1]).all())
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def oracle_step_time(vd, n_perp=None):
+    """Seconds for one FP64 oracle RK4 step (four RHS evaluations + stage arithmetic)."""
+    from oracle import uppe_oracle as O
+    O.set_workers(cpu_cores())
+    v = dict(vd)
+    if n_perp is not None and n_perp != v["wave grid"][1]:
+        N = v["wave grid"]
+        f = n_perp / N[1]
+        v["wave grid"] = (N[0], n_perp, n_perp if N[2] > 1 else 1, N[3])
+        v["size"] = (v["size"][0] * f, v["size"][1] * (f if N[2] > 1 else 1), v["size"][2])
+    orc = O.Oracle(v)
+    g = orc.g
+    orc.mat.update(0.0)
+    q = g.kspace(vd["incoming wave"](g.w, g.x1, g.x2))
+    dz = v["size"][2] / v["subcycles"]
+    t = time.perf_counter()
+    k1 = orc.load_source(q, 0.0)
+    qf = q + dz / 6 * k1
+    qw = (q + dz / 2 * k1) * orc.conditioner[:, None, None]
+    k2 = orc.load_source(qw, dz / 2)
+    qf = qf + dz / 3 * k2
+    qw = (q + dz / 2 * k2) * orc.conditioner[:, None, None]
+    k3 = orc.load_source(qw, dz / 2)
+    qf = qf + dz / 3 * k3
+    qw = (q + dz * k3) * orc.conditioner[:, None, None]
+    k4 = orc.load_source(qw, dz)
+    q = (qf + dz / 6 * k4) * orc.conditioner[:, None, None]
+    return time.perf_counter() - t, int(np.prod(g.N[:3])), g.N
+
+
+def reference_arm(args, vd, ws, rank):
+    if rank != 0:
+        return
+    # size the per-step sample so the whole run stays within a few minutes
+    budget = 150.0
+    chosen = None
+    for n in (128, 64, 32, 16, 8):
+        t, P, N = oracle_step_time(vd, n)
+        chosen = (n, t, P, N)
+        if t * (args.steps + args.warmup) <= budget:
+            break
+    n, _, P, N = chosen
+    for _ in range(max(0, args.warmup - 1)):
+        oracle_step_time(vd, n)
+    tot = 0.0
+    for _ in range(args.steps):
+        t, P, N = oracle_step_time(vd, n)
+        tot += t
+    value = P * args.steps / tot
+    cores = cpu_cores()
+    sample = f"one FP64 RK4 step per bench step on a {N[0]}x{N[1]}x{N[2]} sub-grid of the workload (same physics, box scaled)"
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": args.workload, "grid": list(vd["wave grid"][:3]), "sample_grid": list(N[:3])},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "SeaRay's UPPE path needs PyOpenCL + an OpenCL runtime, absent on the GPU machine; its CPU path is "
+                "timed as the FP64 oracle port (pinned to the reference's own outputs at 1e-12).",
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="cart_filament_128")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    from searay_gb300 import workloads
+    vd = workloads.WORKLOADS[args.workload]()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        reference_arm(args, vd, ws, rank)
+        return
+    import torch
+    if ws > 1:
+        torch.cuda.set_device(local)
+        torch.distributed.init_process_group("nccl")
+    else:
+        torch.cuda.set_device(0)
+    P, ms, launches, clk, prof, finite = run_device(args, vd, ws, rank, local)
+    if ws > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = P * args.steps * ws / (ms / 1e3)
+    peak, peak_kind = measured_peaks()
+    kernels = {}
+    for name, (tms, cnt) in prof.items():
+        if cnt == 0:
+            continue
+        entry = {"launch_regions": cnt, "total_ms": tms, "avg_us": 1e3 * tms / cnt}
+        if name in ALGO_BYTES:
+            gbs = ALGO_BYTES[name] * P / (tms / cnt / 1e3) / 1e9
+            entry.update({"algo_bytes_per_launch": ALGO_BYTES[name] * P, "achieved_GBs": gbs, "frac": gbs / peak})
+        kernels[name] = entry
+    dom = max((k for k in kernels if k in ALGO_BYTES), key=lambda k: kernels[k]["total_ms"])
+    traffic = ncu_traffic(args.workload).get(dom)
+    roof = {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["achieved_GBs"], "peak": peak, "unit": "GB/s",
+            "frac": kernels[dom]["frac"], "traffic": traffic, "peak_source": peak_kind,
+            "share": kernels[dom]["total_ms"] / sum(v["total_ms"] for v in kernels.values())}
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (float-float phase and density scan)" if args.precision == "mixed" else "f32",
+        "data": "synthetic",
+        "config": {"workload": args.workload, "grid": [513, 128, 128] if args.workload == "cart_filament_128" else list(vd["wave grid"][:3]),
+                   "precision": args.precision, "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "working set (q, qi, qf, op, E, J: ~470 MB) larger than the 129 MB L2"},
+        "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk, "finite": finite,
+    }
+    if rank == 0 and not args.no_e2e:
+        e2e, h2d, d2h, ok = run_e2e(args, vd)
+        line["e2e"] = {"value": e2e * ws, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
+                       "d2h_bytes_per_step": d2h / args.steps, "call": "searay_gb300.track (host NumPy in/out)"}
+    if rank == 0 and not args.no_cpu_baseline and ws == 1:
+        t, Ps, Ns = oracle_step_time(vd)
+        line["cpu_baseline"] = {"value": Ps / t, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+                                "sample": f"one FP64 oracle RK4 step on the full {Ns[0]}x{Ns[1]}x{Ns[2]} grid ({t:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -114,6 +114,30 @@ int uppe_get_field(UppeHandle* h, void* q_out);
 /* Set *nonfinite to 1 if the current q holds NaN or Inf (the '!' check of uppe_kernel.py:219-220). */
 int uppe_check_finite(UppeHandle* h, int* nonfinite);
 
+/* Timing classes of the kernels, for uppe_profile_read. */
+#define UPPE_NCLASS 6
+#define UPPE_CLASS_OPERATOR 0   /* kz build (UpdateMaterial) */
+#define UPPE_CLASS_TRANSVERSE_INV 1 /* propagator phase + i kz + inverse transverse transform */
+#define UPPE_CLASS_TIME 2       /* time-axis pass: irfft, sources, density scan, rfft */
+#define UPPE_CLASS_TRANSVERSE_FWD 3 /* forward transverse transform + ODE RHS + RK4 stage */
+#define UPPE_CLASS_STEP_SIZE 4  /* adaptive step estimate */
+#define UPPE_CLASS_OTHER 5
+
+/* Record CUDA events on the handle's stream around every kernel class (enable=1), or stop
+ * (enable=0).  Enabling clears the accumulated times.  Adds event records between launches, so
+ * time headline numbers with profiling off.  (SeaRay has only a wall-clock print, rays.py:85,136.) */
+int uppe_profile_enable(UppeHandle* h, int enable);
+
+/* Synchronise the stream and return, per class, the summed milliseconds and the number of timed
+ * regions since profiling was enabled (arrays of UPPE_NCLASS entries). */
+int uppe_profile_read(UppeHandle* h, double* ms, long long* count);
+
+/* Number of kernels this handle has launched since it was created. */
+int uppe_launch_count(UppeHandle* h, long long* n);
+
+/* Name of a timing class. */
+const char* uppe_class_name(int cls);
+
 /* Message of the last error on h (or of the last failed uppe_create when h is NULL). */
 const char* uppe_last_error(const UppeHandle* h);
 

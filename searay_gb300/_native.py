@@ -25,7 +25,9 @@ RATE_SERIES = 2
 
 EXPORTS = ("uppe_create", "uppe_destroy", "uppe_set_stream", "uppe_set_grid", "uppe_set_material",
            "uppe_load_field", "uppe_rk4_step", "uppe_finish", "uppe_eval_rhs", "uppe_get_field",
-           "uppe_check_finite", "uppe_last_error")
+           "uppe_check_finite", "uppe_profile_enable", "uppe_profile_read", "uppe_launch_count",
+           "uppe_class_name", "uppe_last_error")
+NCLASS = 6
 
 
 class UppeConfig(ctypes.Structure):
@@ -73,10 +75,15 @@ def lib():
     L.uppe_eval_rhs.argtypes = [vp, vp, ctypes.c_double, vp]
     L.uppe_get_field.argtypes = [vp, vp]
     L.uppe_check_finite.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
+    L.uppe_profile_enable.argtypes = [vp, ctypes.c_int]
+    L.uppe_profile_read.argtypes = [vp, _dp, ctypes.POINTER(ctypes.c_longlong)]
+    L.uppe_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    L.uppe_class_name.argtypes = [ctypes.c_int]
+    L.uppe_class_name.restype = ctypes.c_char_p
     L.uppe_last_error.argtypes = [vp]
     L.uppe_last_error.restype = ctypes.c_char_p
     for name in EXPORTS:
-        if name != "uppe_last_error":
+        if name not in ("uppe_last_error", "uppe_class_name"):
             getattr(L, name).restype = ctypes.c_int
     _LIB = L
     return L

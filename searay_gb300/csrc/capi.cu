@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include <new>
+#include <utility>
 #include <vector>
 
 #include "common.cuh"
@@ -32,6 +33,67 @@ int uppe_set_error(UppeHandle* h, const char* fmt, ...) {
             uppe_set_error((h), "%s failed: %s", #expr, cudaGetErrorString(e_));                  \
             return (e_ == cudaErrorMemoryAllocation) ? UPPE_E_NOMEM : UPPE_E_CUDA;                \
         }                                                                                         \
+    } while (0)
+
+// ---- optional per-class timing with CUDA events on the handle's stream ----
+struct ProfState {
+    std::vector<cudaEvent_t> pool;
+    std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+    double ms[UPPE_NCLASS];
+    long long count[UPPE_NCLASS];
+    size_t next;
+};
+
+static cudaEvent_t prof_event(ProfState* ps) {
+    if (ps->next == ps->pool.size()) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+        ps->pool.push_back(e);
+    }
+    return ps->pool[ps->next++];
+}
+
+static cudaError_t prof_resolve(UppeHandle* h) {
+    ProfState* ps = (ProfState*)h->prof;
+    if (!ps) return cudaSuccess;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return e;
+    for (auto& p : ps->pending) {
+        float ms = 0.f;
+        e = cudaEventElapsedTime(&ms, p.second.first, p.second.second);
+        if (e != cudaSuccess) return e;
+        ps->ms[p.first] += ms;
+        ps->count[p.first] += 1;
+    }
+    ps->pending.clear();
+    ps->next = 0;
+    return cudaSuccess;
+}
+
+struct ProfScope {
+    UppeHandle* h;
+    int cls;
+    cudaEvent_t b, e;
+    ProfScope(UppeHandle* h_, int c) : h(h_), cls(c), b(nullptr), e(nullptr) {
+        ProfState* ps = (ProfState*)h->prof;
+        if (!ps) return;
+        if (ps->pending.size() > 4096) prof_resolve(h);
+        b = prof_event(ps);
+        e = prof_event(ps);
+        if (b) cudaEventRecord(b, h->stream);
+    }
+    ~ProfScope() {
+        ProfState* ps = (ProfState*)h->prof;
+        if (!ps || !b || !e) return;
+        cudaEventRecord(e, h->stream);
+        ps->pending.push_back({cls, {b, e}});
+    }
+};
+
+#define PROF_TRY(h, cls, expr)      \
+    do {                            \
+        ProfScope ps_((h), (cls));  \
+        CUDA_TRY((h), (expr));      \
     } while (0)
 
 static bool is_pow2(long n) { return n > 0 && (n & (n - 1)) == 0; }
@@ -169,6 +231,12 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
 
 extern "C" int uppe_destroy(UppeHandle* h) {
     if (!h) return UPPE_OK;
+    if (h->prof) {
+        ProfState* ps = (ProfState*)h->prof;
+        for (cudaEvent_t e : ps->pool) cudaEventDestroy(e);
+        delete ps;
+        h->prof = nullptr;
+    }
     free_buffers(h);
     delete h;
     return UPPE_OK;
@@ -232,11 +300,11 @@ extern "C" int uppe_set_material(UppeHandle* h, const double* w2n2, const double
     CUDA_TRY(h, cudaMemcpyAsync(h->w2n2_d, w2n2, 2 * h->N0 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->kg_d, kg, h->N0 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->ng, ngf.data(), h->S * sizeof(float), cudaMemcpyHostToDevice, h->stream));
-    CUDA_TRY(h, launch_build_operator(h));
+    PROF_TRY(h, UPPE_CLASS_OPERATOR, launch_build_operator(h));
     // exact max |Re kz + kg| and max Im kz of the new operator, for the range checks
     const float init[4] = {0.f, 0.f, 0.f, 0.f};
     CUDA_TRY(h, cudaMemcpyAsync(h->red, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
-    CUDA_TRY(h, launch_operator_bounds(h));
+    PROF_TRY(h, UPPE_CLASS_OPERATOR, launch_operator_bounds(h));
     float red[4];
     CUDA_TRY(h, cudaMemcpyAsync(red, h->red, sizeof(red), cudaMemcpyDeviceToHost, h->stream));
     // the pageable host tables above must be consumed before returning
@@ -271,17 +339,24 @@ static cudaError_t spec_pass(UppeHandle* h, int mode, const float2* src, float2*
 
 // One source evaluation: J = sources(T^-1(...q...)) on the real side.
 static cudaError_t eval_to_J(UppeHandle* h, const float2* qsrc, StepArgs z) {
-    cudaError_t e = real_pass(h, REAL_E, qsrc, nullptr, z);
+    cudaError_t e;
+    {
+        ProfScope ps(h, UPPE_CLASS_TRANSVERSE_INV);
+        e = real_pass(h, REAL_E, qsrc, nullptr, z);
+    }
     if (e != cudaSuccess) return e;
+    ProfScope ps(h, UPPE_CLASS_TIME);
     return launch_time_pass(h, TIME_J, h->E, h->J, nullptr);
 }
 
 extern "C" int uppe_load_field(UppeHandle* h, const void* a) {
     if (!h || !a) return UPPE_E_ARG;
-    int rc = check_ready(h, false);
-    if (rc) return rc;
+    if (!h->have_grid) {
+        uppe_set_error(h, "uppe_load_field before uppe_set_grid");
+        return UPPE_E_ARG;
+    }
     StepArgs z = split_z(h, 0.0);
-    CUDA_TRY(h, spec_pass(h, SPEC_LOAD, (const float2*)a, h->qi, nullptr, nullptr, 0.f, 0.f, z));
+    PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_LOAD, (const float2*)a, h->qi, nullptr, nullptr, 0.f, 0.f, z));
     h->have_field = 1;
     return UPPE_OK;
 }
@@ -319,35 +394,35 @@ extern "C" int uppe_rk4_step(UppeHandle* h, double z_phase, double L, double z_s
     if (adaptive) {
         StepArgs z = split_z(h, z_phase);
         CUDA_TRY(h, eval_to_J(h, h->qi, z));
-        CUDA_TRY(h, spec_pass(h, SPEC_STORE_K, h->J, h->k1, nullptr, nullptr, 0.f, 0.f, z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STORE_K, h->J, h->k1, nullptr, nullptr, 0.f, 0.f, z));
         const float init[4] = {0.f, INFINITY, 0.f, 0.f};
         CUDA_TRY(h, cudaMemcpyAsync(h->red, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
-        CUDA_TRY(h, launch_absmax(h, h->qi));
-        CUDA_TRY(h, launch_step_size(h, h->qi, h->k1, L, 0.4, 1e-2));
+        PROF_TRY(h, UPPE_CLASS_STEP_SIZE, launch_absmax(h, h->qi));
+        PROF_TRY(h, UPPE_CLASS_STEP_SIZE, launch_step_size(h, h->qi, h->k1, L, 0.4, 1e-2));
         float red[4];
         CUDA_TRY(h, cudaMemcpyAsync(red, h->red, sizeof(red), cudaMemcpyDeviceToHost, h->stream));
         CUDA_TRY(h, cudaStreamSynchronize(h->stream));
         dz = (double)red[1];
         if (dz < dzmin) dz = dzmin;
         if (z_sub + dz > L) dz = L - z_sub;
-        CUDA_TRY(h, launch_apply_stage1(h, (float)(dz / 6), (float)(dz / 2)));
+        PROF_TRY(h, UPPE_CLASS_STEP_SIZE, launch_apply_stage1(h, (float)(dz / 6), (float)(dz / 2)));
     } else {
         dz = L - z_sub;
         StepArgs z = split_z(h, z_phase);
         CUDA_TRY(h, eval_to_J(h, h->qi, z));
-        CUDA_TRY(h, spec_pass(h, SPEC_STAGE1, h->J, h->q, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STAGE1, h->J, h->q, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z));
     }
     {
         StepArgs z = split_z(h, z_phase + 0.5 * dz);
         CUDA_TRY(h, eval_to_J(h, h->q, z));
-        CUDA_TRY(h, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), z));
         CUDA_TRY(h, eval_to_J(h, h->q, z));
-        CUDA_TRY(h, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)dz, z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)dz, z));
     }
     {
         StepArgs z = split_z(h, z_phase + dz);
         CUDA_TRY(h, eval_to_J(h, h->q, z));
-        CUDA_TRY(h, spec_pass(h, SPEC_FINISH, h->J, h->qi, h->qf, nullptr, (float)(dz / 6), 0.f, z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_FINISH, h->J, h->qi, h->qf, nullptr, (float)(dz / 6), 0.f, z));
     }
     if (dz_out) *dz_out = dz;
     return UPPE_OK;
@@ -360,9 +435,9 @@ extern "C" int uppe_finish(UppeHandle* h, double z_phase, void* A, void* J, void
     rc = check_range(h, z_phase);
     if (rc) return rc;
     StepArgs z = split_z(h, z_phase);
-    CUDA_TRY(h, real_pass(h, REAL_FINISH, h->qi, (float2*)A, z));
-    CUDA_TRY(h, launch_time_pass(h, TIME_J, h->E, J ? (float2*)J : h->J, nullptr));
-    if (chi_w || ne_w) CUDA_TRY(h, launch_time_pass(h, TIME_CHI_NE, h->E, (float2*)chi_w, (float2*)ne_w));
+    PROF_TRY(h, UPPE_CLASS_OTHER, real_pass(h, REAL_FINISH, h->qi, (float2*)A, z));
+    PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_pass(h, TIME_J, h->E, J ? (float2*)J : h->J, nullptr));
+    if (chi_w || ne_w) PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_pass(h, TIME_CHI_NE, h->E, (float2*)chi_w, (float2*)ne_w));
     return UPPE_OK;
 }
 
@@ -374,7 +449,7 @@ extern "C" int uppe_eval_rhs(UppeHandle* h, const void* q_in, double z_phase, vo
     if (rc) return rc;
     StepArgs z = split_z(h, z_phase);
     CUDA_TRY(h, eval_to_J(h, (const float2*)q_in, z));
-    CUDA_TRY(h, spec_pass(h, SPEC_STORE_K, h->J, (float2*)S_out, nullptr, nullptr, 0.f, 0.f, z));
+    PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STORE_K, h->J, (float2*)S_out, nullptr, nullptr, 0.f, 0.f, z));
     return UPPE_OK;
 }
 
@@ -398,6 +473,56 @@ extern "C" int uppe_check_finite(UppeHandle* h, int* nonfinite) {
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     *nonfinite = (red[2] != 0.f) ? 1 : 0;
     return UPPE_OK;
+}
+
+extern "C" int uppe_profile_enable(UppeHandle* h, int enable) {
+    if (!h) return UPPE_E_ARG;
+    if (enable) {
+        if (!h->prof) h->prof = new (std::nothrow) ProfState();
+        if (!h->prof) return UPPE_E_NOMEM;
+        ProfState* ps = (ProfState*)h->prof;
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        ps->pending.clear();
+        ps->next = 0;
+        for (int i = 0; i < UPPE_NCLASS; ++i) {
+            ps->ms[i] = 0.0;
+            ps->count[i] = 0;
+        }
+    } else if (h->prof) {
+        CUDA_TRY(h, prof_resolve(h));
+        ProfState* ps = (ProfState*)h->prof;
+        for (cudaEvent_t e : ps->pool) cudaEventDestroy(e);
+        delete ps;
+        h->prof = nullptr;
+    }
+    return UPPE_OK;
+}
+
+extern "C" int uppe_profile_read(UppeHandle* h, double* ms, long long* count) {
+    if (!h || !ms || !count) return UPPE_E_ARG;
+    ProfState* ps = (ProfState*)h->prof;
+    if (!ps) {
+        uppe_set_error(h, "profiling is not enabled");
+        return UPPE_E_ARG;
+    }
+    CUDA_TRY(h, prof_resolve(h));
+    for (int i = 0; i < UPPE_NCLASS; ++i) {
+        ms[i] = ps->ms[i];
+        count[i] = ps->count[i];
+    }
+    return UPPE_OK;
+}
+
+extern "C" int uppe_launch_count(UppeHandle* h, long long* n) {
+    if (!h || !n) return UPPE_E_ARG;
+    *n = h->launches;
+    return UPPE_OK;
+}
+
+extern "C" const char* uppe_class_name(int cls) {
+    static const char* names[UPPE_NCLASS] = {"operator", "transverse_inverse", "time_pass", "transverse_forward_rk",
+                                             "step_size", "finish"};
+    return (cls >= 0 && cls < UPPE_NCLASS) ? names[cls] : "unknown";
 }
 
 extern "C" const char* uppe_last_error(const UppeHandle* h) { return h ? h->err : g_create_error; }

@@ -154,6 +154,7 @@ static cudaError_t launch_azimuth(UppeHandle* h, const float2* in, float2* out, 
     const size_t n = rows * h->N2;
     unsigned blocks = (unsigned)((n + 255) / 256);
     if (blocks > 152 * 16) blocks = 152 * 16;
+    h->launches++;
     k_azimuth_dft<<<blocks, 256, 0, h->stream>>>(in, out, rows, h->N2, logN2, inv, inv ? 1.f / h->N2 : 1.f, h->tw,
                                                   h->twLog);
     return cudaGetLastError();
@@ -162,6 +163,7 @@ static cudaError_t launch_azimuth(UppeHandle* h, const float2* in, float2* out, 
 template <int AMODE, int CMODE>
 static cudaError_t run_gemm(UppeHandle* h, GemmArgs& g) {
     dim3 grid((g.NI + GBN - 1) / GBN, (g.N0 + GBM - 1) / GBM, g.N2);
+    h->launches++;
     k_hankel_gemm<AMODE, CMODE><<<grid, 256, 0, h->stream>>>(g);
     return cudaGetLastError();
 }

@@ -56,6 +56,8 @@ struct UppeHandle {
     int have_grid, have_material, have_field;
     double max_abs_K;   // max |Re kz + kg| of the current operator
     double max_Ki;      // max Im kz of the current operator
+    long long launches; // kernels launched by this handle
+    void* prof;         // profiling state (capi.cu), NULL when off
     char err[512];
 };
 

@@ -61,6 +61,7 @@ cudaError_t launch_build_operator(UppeHandle* h) {
     size_t n = h->P;
     int threads = 256;
     unsigned blocks = (unsigned)((n + threads - 1) / threads);
+    h->launches++;
     k_build_operator<<<blocks, threads, 0, h->stream>>>(h->w2n2_d, h->kg_d, h->kr2_d, h->op, h->N0, h->S);
     return cudaGetLastError();
 }
@@ -84,6 +85,7 @@ __global__ void k_operator_bounds(const float4* __restrict__ op, size_t n, float
 
 cudaError_t launch_operator_bounds(UppeHandle* h) {
     size_t b = (h->P + 255) / 256;
+    h->launches++;
     k_operator_bounds<<<(unsigned)(b < 1216 ? b : 1216), 256, 0, h->stream>>>(h->op, h->P, h->red);
     return cudaGetLastError();
 }
@@ -198,6 +200,7 @@ cudaError_t uppe_configure_slice_kernels(size_t smem_bytes) {
 cudaError_t launch_real_cart(UppeHandle* h, int mode, const float2* src, float2* A_out, StepArgs z) {
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     size_t smem = (size_t)h->S * sizeof(float2);
+    h->launches++;
     k_real_cart<<<h->N0, slice_threads(h), smem, h->stream>>>(mode, src, h->op, h->E, A_out, logN1, logN2, h->tw,
                                                                h->twLog, z);
     return cudaGetLastError();
@@ -207,6 +210,7 @@ cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, fl
                              const float2* qi, float Cs, float Ce, StepArgs z) {
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     size_t smem = (size_t)h->S * sizeof(float2);
+    h->launches++;
     k_spec_cart<<<h->N0, slice_threads(h), smem, h->stream>>>(mode, src_real, h->op, q_out, qf_io, qi, Cs, Ce,
                                                                logN1, logN2, h->tw, h->twLog, z);
     return cudaGetLastError();
@@ -383,7 +387,8 @@ __global__ void __launch_bounds__(256) k_time(int mode, const float2* __restrict
         float2 Ck = Y[k * C + cc];
         float2 Cm = cconj(Y[((Nt - k) & (Nt - 1)) * C + cc]);
         float2 P = cscale(cadd(Ck, Cm), 0.5f);
-        float2 Q = cscale(cmul_mi(csub(Ck, Cm)), 0.5f);
+        // without a rate model the imaginary channel holds only rounding: keep it exactly zero
+        float2 Q = (tp.rate_form != UPPE_RATE_NONE) ? cscale(cmul_mi(csub(Ck, Cm)), 0.5f) : make_float2(0.f, 0.f);
         const size_t o = (size_t)k * S + col0 + cc;
         if (mode == TIME_J) {
             const float wk = wv[k];
@@ -428,6 +433,7 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
     tp.plain = (c.precision == UPPE_PREC_FP32);
     const int T = h->Nt * h->time_cols / TIME_SPT;
     const size_t smem = (size_t)h->Nt * h->time_cols * sizeof(float2) + (size_t)T * sizeof(ffloat);
+    h->launches++;
     k_time<<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw, h->twLog,
                                                          tp);
     return cudaGetLastError();
@@ -498,6 +504,7 @@ static unsigned reduce_blocks(size_t n) {
 }
 
 cudaError_t launch_absmax(UppeHandle* h, const float2* q) {
+    h->launches++;
     k_absmax<<<reduce_blocks(h->P), 256, 0, h->stream>>>(q, h->P, h->red);
     return cudaGetLastError();
 }
@@ -505,6 +512,7 @@ cudaError_t launch_absmax(UppeHandle* h, const float2* q) {
 cudaError_t launch_step_size(UppeHandle* h, const float2* q, const float2* k, double L, double dphi,
                              double rel_amin) {
     float minRate = (float)(0.5 * dphi / L);
+    h->launches++;
     k_step_size<<<reduce_blocks(h->P), 256, 0, h->stream>>>(q, k, h->P, h->red, minRate, (float)dphi,
                                                              (float)rel_amin);
     return cudaGetLastError();
@@ -522,6 +530,7 @@ __global__ void k_apply_stage1(const float2* __restrict__ qi, const float2* __re
 }
 
 cudaError_t launch_apply_stage1(UppeHandle* h, float Cs, float Ce) {
+    h->launches++;
     k_apply_stage1<<<reduce_blocks(h->P) * 2, 256, 0, h->stream>>>(h->qi, h->k1, h->q, h->qf, h->P, h->S, Cs, Ce);
     return cudaGetLastError();
 }
@@ -535,6 +544,7 @@ __global__ void k_ikz(const float2* __restrict__ A, const float4* __restrict__ o
 }
 
 cudaError_t launch_ikz(UppeHandle* h, const float2* A, float2* E) {
+    h->launches++;
     k_ikz<<<reduce_blocks(h->P) * 2, 256, 0, h->stream>>>(A, h->op, E, h->P);
     return cudaGetLastError();
 }

@@ -135,6 +135,20 @@ class DeviceGrid:
         self._check(self.lib.uppe_check_finite(self.h, ctypes.byref(flag)))
         return bool(flag.value)
 
+    def profile(self, enable):
+        self._check(self.lib.uppe_profile_enable(self.h, 1 if enable else 0))
+
+    def profile_read(self):
+        ms = (ctypes.c_double * _native.NCLASS)()
+        cnt = (ctypes.c_longlong * _native.NCLASS)()
+        self._check(self.lib.uppe_profile_read(self.h, ms, cnt))
+        return {self.lib.uppe_class_name(i).decode(): (ms[i], cnt[i]) for i in range(_native.NCLASS)}
+
+    def launches(self):
+        n = ctypes.c_longlong()
+        self._check(self.lib.uppe_launch_count(self.h, ctypes.byref(n)))
+        return n.value
+
     def empty_field(self):
         return torch.empty(tuple(self.N[:3]), dtype=torch.complex64, device="cuda")
 

@@ -1,0 +1,184 @@
+"""UPPE volumes for the benchmark workloads, built from synthetic analytic inputs.
+
+No public dataset is involved: every input is an analytic pulse in a dispersive, Kerr and
+ionizing medium.  Units follow SeaRay: lengths in mks_length = lambda0 / (2 pi), so the carrier
+has w = 1.  Unit conversions restate SeaRay's ``InputHelper.dnum`` (``modules/input_tools.py:5-61``).
+
+Workloads (sizes as the reference's volume dictionaries spell them, ``'wave grid' = (N0, N1, N2, N3)``
+with N0 = 2^n + 1 frequency nodes):
+
+* ``cyl_kerr_64``: cylindrical, N0 = 257 (Nt = 512, 400 fs window), Nr = Nk = 64 over R = 1 mm,
+  800 nm 50 fs Gaussian, w0 = 200 um, 1e13 W/cm^2, two-term air, n2 = 3e-19 cm^2/W, Kerr only,
+  100 RK4 steps over 10 cm.
+* ``cart_filament_128``: Cartesian 128 x 128 over 2 mm, N0 = 513 (band 0-4 w0), 800 nm 35 fs pulse
+  at 5 critical powers, 8-mode seeded transverse phase (0.05 rad, numpy default_rng(0)), Kerr
+  (n2 = 3e-19 cm^2/W) + O2 tunneling ionization (PPT, Ip = 12.07 eV, Z = 0.53) at 5.4e18 cm^-3 +
+  plasma current, 400 RK4 steps over 10 cm.
+* ``cyl_silica_512``: cylindrical Nr = Nk = 512 over R = 0.5 mm, N0 = 2049, 1 um 100 fs pulse at
+  1e14 W/cm^2 in fused silica (Malitson Sellmeier, n2 = 2.5e-16 cm^2/W), PPT tunneling with
+  Ip = 9 eV (Z = 1 assumed) at 2.2e22 cm^-3, 100 RK4 steps over 1 cm.
+"""
+import numpy as np
+from scipy import constants as C
+
+from . import dispersion, ionization
+
+
+class Units:
+    """Simulation-unit conversions (input_tools.py:5-61)."""
+
+    def __init__(self, mks_length):
+        self.x1 = mks_length
+        self.t1 = mks_length / C.c
+        self.w1 = 1 / self.t1
+        self.E1 = C.m_e * C.c * self.w1 / C.e
+        self.n1 = C.epsilon_0 * C.m_e * self.w1 ** 2 / C.e ** 2
+        self.u1 = C.m_e * C.c ** 2
+        self.N1 = self.n1 * self.x1 ** 3
+
+    def fs(self, v):
+        return v * 1e-15 / self.t1
+
+    def um(self, v):
+        return v * 1e-6 / self.x1
+
+    def mm(self, v):
+        return v * 1e-3 / self.x1
+
+    def cm(self, v):
+        return v * 1e-2 / self.x1
+
+    def W_cm2(self, v):
+        return v * 1e4 * self.t1 * self.x1 ** 2 / self.N1 / self.u1
+
+    def m2_W(self, v):
+        return v * self.N1 * self.u1 / self.x1 ** 2 / self.t1
+
+    def eV(self, v):
+        return v * C.e / self.u1
+
+    def cm3(self, v):
+        return v * 1e6 / self.n1
+
+    def chi3(self, n0, n2_m2_W):
+        """chi3 = (4/3) n0^2 n2 (input_tools.py:110-111)."""
+        return (4 / 3) * n0 ** 2 * self.m2_W(n2_m2_W)
+
+
+def seeded_phase_screen(n_modes, amp, size, seed):
+    """Transverse phase: sum of n_modes cosine gratings, random directions and phases from
+    numpy default_rng(seed), wavenumbers up to 3 cycles across the box."""
+    rng = np.random.default_rng(seed)
+    kx = rng.uniform(-3, 3, n_modes) * 2 * np.pi / size
+    ky = rng.uniform(-3, 3, n_modes) * 2 * np.pi / size
+    ph = rng.uniform(0, 2 * np.pi, n_modes)
+
+    def screen(x1, x2):
+        X = x1[:, None]
+        Y = x2[None, :]
+        out = np.zeros((x1.shape[0], x2.shape[0]))
+        for i in range(n_modes):
+            out += amp * np.cos(kx[i] * X + ky[i] * Y + ph[i])
+        return out
+    return screen
+
+
+def gaussian_pulse(E0, tau, r0, cylindrical=False, screen=None, w0=1.0):
+    """Incoming wave (w, x1, x2) -> complex (N0, N1, N2): a transform-limited Gaussian pulse
+    E(t) = E0 exp(-t^2/tau^2) cos(w0 t) centred in the time window, Gaussian transverse profile of
+    1/e field radius r0, optional transverse phase screen."""
+    def wave(w, x1, x2):
+        dwn = w[1] - w[0]
+        Nt = 2 * w.shape[0] - 2
+        dw = 2.0 / tau
+        amp = E0 * Nt / (2.0 * np.sqrt(np.pi) * (dw / dwn) * w0)
+        T = 2 * np.pi / dwn
+        spec = amp * np.exp(-(w - w0) ** 2 / dw ** 2) * np.exp(1j * w * 0.5 * T)
+        if cylindrical:
+            tr = np.exp(-(x1[:, None] ** 2) / r0 ** 2) * np.ones((1, x2.shape[0]))
+        else:
+            tr = np.exp(-(x1[:, None] ** 2 + x2[None, :] ** 2) / r0 ** 2)
+        if screen is not None:
+            tr = tr * np.exp(1j * screen(x1, x2))
+        return spec[:, None, None] * tr[None, :, :]
+    return wave
+
+
+def field_from_intensity(u, I_W_cm2):
+    """Peak field (simulation units) of a linearly polarised wave of intensity I: E = sqrt(2 I)."""
+    return np.sqrt(2 * u.W_cm2(I_W_cm2))
+
+
+def critical_power_W(lam_m, n0, n2_m2_W):
+    """Marburger critical power 3.77 lambda^2 / (8 pi n0 n2)."""
+    return 3.77 * lam_m ** 2 / (8 * np.pi * n0 * n2_m2_W)
+
+
+def cyl_kerr_64(steps=100):
+    x1 = 0.8e-6 / (2 * np.pi)
+    u = Units(x1)
+    air = dispersion.SimpleAir(x1)
+    N0 = 257
+    W = 2 * np.pi * N0 / u.fs(400.0)
+    L = u.cm(10.0)
+    E0 = field_from_intensity(u, 1e13)
+    vd = {
+        "wave grid": (N0, 64, 1, 2), "wave coordinates": "cylindrical", "radial modes": 64,
+        "frequency band": (0.0, W), "nonlinear band": (0.0, W),
+        "size": (2 * u.mm(1.0), 2 * u.mm(1.0), L), "subcycles": steps, "minimum step": L / steps,
+        "chi3": u.chi3(1.0, 3e-23), "density reference": 1.0,
+        "window speed": air.GroupVelocityMagnitude(1.0),
+        "dispersion inside": air, "ionizer": None,
+        "density lambda": lambda x, y, z, r2: np.ones(x.shape),
+        "incoming wave": gaussian_pulse(E0, u.fs(50.0), u.um(200.0), cylindrical=True),
+    }
+    return vd
+
+
+def cart_filament_128(steps=400, n_perp=128):
+    x1 = 0.8e-6 / (2 * np.pi)
+    u = Units(x1)
+    air = dispersion.SimpleAir(x1)
+    n2 = 3e-23
+    r0 = u.mm(0.3)
+    P = 5 * critical_power_W(0.8e-6, 1.0, n2)
+    I0 = 2 * P / (np.pi * (0.3e-3) ** 2) * 1e-4  # W/cm^2
+    E0 = field_from_intensity(u, I0)
+    L = u.cm(10.0)
+    box = u.mm(2.0)
+    vd = {
+        "wave grid": (513, n_perp, n_perp, 2), "wave coordinates": "cartesian",
+        "frequency band": (0.0, 4.0), "nonlinear band": (0.0, 3.5),
+        "size": (box, box, L), "subcycles": steps, "minimum step": L / steps,
+        "chi3": u.chi3(1.0, n2), "density reference": u.cm3(5.4e18),
+        "window speed": air.GroupVelocityMagnitude(1.0),
+        "dispersion inside": air,
+        "ionizer": ionization.PPT_Tunneling(x1, False, u.eV(12.07), 0.53),
+        "density lambda": lambda x, y, z, r2: np.ones(x.shape),
+        "incoming wave": gaussian_pulse(E0, u.fs(35.0), r0, screen=seeded_phase_screen(8, 0.05, box, 0)),
+    }
+    return vd
+
+
+def cyl_silica_512(steps=100):
+    x1 = 1.0e-6 / (2 * np.pi)
+    u = Units(x1)
+    glass = dispersion.FusedSilica(x1)
+    n0 = float(np.sqrt(1 + glass.chi(np.array([1.0]))[0]))
+    L = u.cm(1.0)
+    E0 = field_from_intensity(u, 1e14) / np.sqrt(n0)
+    vd = {
+        "wave grid": (2049, 512, 1, 2), "wave coordinates": "cylindrical", "radial modes": 512,
+        "frequency band": (0.0, 4.0), "nonlinear band": (0.0, 3.5),
+        "size": (2 * u.mm(0.5), 2 * u.mm(0.5), L), "subcycles": steps, "minimum step": L / steps,
+        "chi3": u.chi3(n0, 2.5e-20), "density reference": u.cm3(2.2e22),
+        "window speed": glass.GroupVelocityMagnitude(1.0),
+        "dispersion inside": glass,
+        "ionizer": ionization.PPT_Tunneling(x1, False, u.eV(9.0), 1.0),
+        "density lambda": lambda x, y, z, r2: np.ones(x.shape),
+        "incoming wave": gaussian_pulse(E0, u.fs(100.0), u.um(60.0), cylindrical=True),
+    }
+    return vd
+
+
+WORKLOADS = {"cyl_kerr_64": cyl_kerr_64, "cart_filament_128": cart_filament_128, "cyl_silica_512": cyl_silica_512}
