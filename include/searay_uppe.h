@@ -138,6 +138,31 @@ int uppe_launch_count(UppeHandle* h, long long* n);
 /* Name of a timing class. */
 const char* uppe_class_name(int cls);
 
+/* Adaptive step-size estimate without any device allocation.  This entry point has no
+ * counterpart in the reference; it exists for callers that may not allocate device memory once
+ * they run.  Examples: a host program that reserves all GPU memory at start-up and forbids later
+ * cudaMalloc, or a loop in which an allocation would synchronise the device.  Such a caller cannot
+ * create a handle, which allocates its work buffers.
+ *
+ * From q and S = dq/dz (device complex64 arrays of n points, caller-owned) it writes to *dz_out
+ * (one float in device memory) the unclamped estimate min over the grid of dphi / K, computed as in
+ * uppe_rk4_step's adaptive step: amin = rel_amin * max|q|, K = 0.5 dphi/L + |Im(S q*)|/(|q|^2 +
+ * amin^2) - min(Re(S q*)/(|q|^2 + amin^2), 0)  (paraxial.cl:40-58, uppe_kernel.py:217-223).  The
+ * caller applies the dzmin and end-of-subcycle clamps.
+ *
+ * Its reduction scratch is one fixed array in device memory, about 128 KB, held by every GPU
+ * that loads this library until the process exits.  Limits and rules:
+ *   - n may not exceed UPPE_NOALLOC_MAX_POINTS; larger grids get UPPE_E_RANGE and a message.
+ *   - The first call on each device looks up the array's device address with that device
+ *     current.  Make that first call before any CUDA stream capture.
+ *   - All calls share the one array, which keeps the contents of the last call.  Calls whose work
+ *     overlaps on the GPU (for example on two streams at once) race; serialise them.
+ * Work is issued on `stream` (cudaStream_t, NULL = legacy default stream).  Errors are reported by
+ * uppe_last_error(NULL). */
+#define UPPE_NOALLOC_MAX_POINTS (1LL << 27)
+int uppe_step_size_noalloc(const void* q, const void* S, long long n, double L, double dphi, double rel_amin,
+                           void* dz_out, void* stream);
+
 /* Message of the last error on h (or of the last failed uppe_create when h is NULL). */
 const char* uppe_last_error(const UppeHandle* h);
 
