@@ -36,12 +36,16 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "UPPE grid-pt*steps/s (RK4 z-step)"
 UNIT = "grid-pt*steps/s"
-# algorithmic HBM bytes per grid point per launch of each kernel class (complex64 fields,
-# 16-byte per-point operator {K_hi, K_lo, Re kz, Im kz})
+# algorithmic HBM bytes per grid point per launch of each kernel class on a Cartesian grid
+# (complex64 fields, 8-byte per-point operator K = Re kz + kg as float-float):
+#   transverse_inverse: read q, K; write E
+#   time_pass: read E; write J
+#   transverse_forward_rk (fused slice pass): read J, K, qi and/or qf; write qf or qi; write E for the
+#   next evaluation -- 40 / 48 / 48 / 40 bytes for the four RK stages
 ALGO_BYTES = {
-    "transverse_inverse": 8 + 16 + 8,           # read q, op; write E
-    "time_pass": 8 + 8,                         # read E; write J
-    "transverse_forward_rk": (48 + 56 + 56 + 40) / 4.0,  # read J, op, qi|qf; write q, qf (stage mix)
+    "transverse_inverse": 8 + 8 + 8,
+    "time_pass": 8 + 8,
+    "transverse_forward_rk": (40 + 48 + 48 + 40) / 4.0,
 }
 
 

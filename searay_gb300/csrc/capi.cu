@@ -107,8 +107,8 @@ static StepArgs split_z(const UppeHandle* h, double z) {
 }
 
 static void free_buffers(UppeHandle* h) {
-    void* ptrs[] = {h->q, h->qi, h->qf, h->k1, h->E, h->J, h->scratch, h->op, h->ng, h->tw, h->w, h->nlfilt,
-                    h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red};
+    void* ptrs[] = {h->q,  h->qi,   h->qf,   h->k1,   h->E,     h->J,      h->scratch, h->opK,  h->opKi, h->kg2,
+                    h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -187,7 +187,9 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     ALLOC(h->E, fbytes);
     ALLOC(h->J, fbytes);
     if (c.cylindrical && c.n2 > 1) ALLOC(h->scratch, fbytes);
-    ALLOC(h->op, h->P * sizeof(float4));
+    ALLOC(h->opK, h->P * sizeof(float2));
+    ALLOC(h->opKi, h->P * sizeof(float));
+    ALLOC(h->kg2, (size_t)c.n0 * sizeof(float2));
     ALLOC(h->ng, (size_t)S * sizeof(float));
     ALLOC(h->tw, ((size_t)1 << h->twLog) * sizeof(float2));
     ALLOC(h->w, (size_t)c.n0 * sizeof(float));
@@ -295,11 +297,22 @@ extern "C" int uppe_set_material(UppeHandle* h, const double* w2n2, const double
         uppe_set_error(h, "uppe_set_material: null table");
         return UPPE_E_ARG;
     }
+    std::vector<float2> kg2(h->N0);
+    int cplx = 0;
+    for (int k = 0; k < h->N0; ++k) {
+        const float hi = (float)kg[k];
+        kg2[k] = make_float2(hi, (float)(kg[k] - (double)hi));
+        if (w2n2[2 * k + 1] != 0.0) cplx = 1;
+    }
     std::vector<float> ngf(h->S);
     for (int s = 0; s < h->S; ++s) ngf[s] = (float)ng[s];
     CUDA_TRY(h, cudaMemcpyAsync(h->w2n2_d, w2n2, 2 * h->N0 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->kg_d, kg, h->N0 * sizeof(double), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, cudaMemcpyAsync(h->ng, ngf.data(), h->S * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(h->kg2, kg2.data(), h->N0 * sizeof(float2), cudaMemcpyHostToDevice, h->stream));
+    h->complex_medium = cplx;
+    h->mat_version += 1;
+    h->E_valid = 0;
     PROF_TRY(h, UPPE_CLASS_OPERATOR, launch_build_operator(h));
     // exact max |Re kz + kg| and max Im kz of the new operator, for the range checks
     const float init[4] = {0.f, 0.f, 0.f, 0.f};
@@ -379,6 +392,100 @@ static int check_range(UppeHandle* h, double z) {
     return UPPE_OK;
 }
 
+static bool same_z(double a, double b) { return fabs(a - b) <= 1e-12 * fmax(1.0, fabs(b)); }
+
+// Adaptive estimate of dz from k1 (held in h->k1) and qi: one host read per step.
+static int estimate_dz(UppeHandle* h, double L, double z_sub, double dzmin, double* dz) {
+    const float init[4] = {0.f, INFINITY, 0.f, 0.f};
+    CUDA_TRY(h, cudaMemcpyAsync(h->red, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
+    PROF_TRY(h, UPPE_CLASS_STEP_SIZE, launch_absmax(h, h->qi));
+    PROF_TRY(h, UPPE_CLASS_STEP_SIZE, launch_step_size(h, h->qi, h->k1, L, 0.4, 1e-2));
+    float red[4];
+    CUDA_TRY(h, cudaMemcpyAsync(red, h->red, sizeof(red), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+    double d = (double)red[1];
+    if (d < dzmin) d = dzmin;
+    if (z_sub + d > L) d = L - z_sub;
+    *dz = d;
+    return UPPE_OK;
+}
+
+// Cartesian grids: every evaluation is the time pass plus one fused slice pass that finishes the
+// RK stage and already produces E for the next evaluation; the last stage leaves E for the first
+// evaluation of the next step, so a step is 8 kernels.
+static int rk4_step_cartesian(UppeHandle* h, double z_phase, double L, double z_sub, double dzmin, bool adaptive,
+                              double* dz_out) {
+    if (!(h->E_valid && h->E_mat == h->mat_version && same_z(h->E_z, z_phase))) {
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_INV, launch_real_cart(h, REAL_E, h->qi, nullptr, split_z(h, z_phase)));
+    }
+    h->E_valid = 0;
+    PROF_TRY(h, UPPE_CLASS_TIME, launch_time_pass(h, TIME_J, h->E, h->J, nullptr));
+    double dz;
+    if (adaptive) {
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
+                 launch_spec_cart(h, SPEC_STORE_K, h->J, h->k1, nullptr, nullptr, 0.f, 0.f, split_z(h, z_phase)));
+        int rc = estimate_dz(h, L, z_sub, dzmin, &dz);
+        if (rc) return rc;
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_INV,
+                 launch_apply1_cart(h, (float)(dz / 6), (float)(dz / 2), split_z(h, z_phase + 0.5 * dz)));
+    } else {
+        dz = L - z_sub;
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
+                 launch_fused_cart(h, SPEC_STAGE1, (float)(dz / 6), (float)(dz / 2), split_z(h, z_phase),
+                                   split_z(h, z_phase + 0.5 * dz)));
+    }
+    const StepArgs zh = split_z(h, z_phase + 0.5 * dz), ze = split_z(h, z_phase + dz);
+    PROF_TRY(h, UPPE_CLASS_TIME, launch_time_pass(h, TIME_J, h->E, h->J, nullptr));
+    PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, launch_fused_cart(h, SPEC_STAGE23, (float)(dz / 3), (float)(dz / 2), zh, zh));
+    PROF_TRY(h, UPPE_CLASS_TIME, launch_time_pass(h, TIME_J, h->E, h->J, nullptr));
+    PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, launch_fused_cart(h, SPEC_STAGE23, (float)(dz / 3), (float)dz, zh, ze));
+    PROF_TRY(h, UPPE_CLASS_TIME, launch_time_pass(h, TIME_J, h->E, h->J, nullptr));
+    PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, launch_fused_cart(h, SPEC_FINISH, (float)(dz / 6), 0.f, ze, ze));
+    h->E_valid = 1;
+    h->E_z = z_phase + dz;
+    h->E_mat = h->mat_version;
+    *dz_out = dz;
+    return UPPE_OK;
+}
+
+// Cylindrical grids: inverse transform, time pass and forward transform per evaluation.
+static int rk4_step_generic(UppeHandle* h, double z_phase, double L, double z_sub, double dzmin, bool adaptive,
+                            double* dz_out) {
+    double dz;
+    h->E_valid = 0;
+    if (adaptive) {
+        StepArgs z = split_z(h, z_phase);
+        CUDA_TRY(h, eval_to_J(h, h->qi, z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STORE_K, h->J, h->k1, nullptr, nullptr, 0.f, 0.f, z));
+        int rc = estimate_dz(h, L, z_sub, dzmin, &dz);
+        if (rc) return rc;
+        PROF_TRY(h, UPPE_CLASS_STEP_SIZE, launch_apply_stage1(h, (float)(dz / 6), (float)(dz / 2)));
+    } else {
+        dz = L - z_sub;
+        StepArgs z = split_z(h, z_phase);
+        CUDA_TRY(h, eval_to_J(h, h->qi, z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
+                 spec_pass(h, SPEC_STAGE1, h->J, h->q, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z));
+    }
+    {
+        StepArgs z = split_z(h, z_phase + 0.5 * dz);
+        CUDA_TRY(h, eval_to_J(h, h->q, z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
+                 spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), z));
+        CUDA_TRY(h, eval_to_J(h, h->q, z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
+                 spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)dz, z));
+    }
+    {
+        StepArgs z = split_z(h, z_phase + dz);
+        CUDA_TRY(h, eval_to_J(h, h->q, z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
+                 spec_pass(h, SPEC_FINISH, h->J, h->qi, h->qf, nullptr, (float)(dz / 6), 0.f, z));
+    }
+    *dz_out = dz;
+    return UPPE_OK;
+}
+
 extern "C" int uppe_rk4_step(UppeHandle* h, double z_phase, double L, double z_sub, double dzmin, double* dz_out) {
     if (!h) return UPPE_E_ARG;
     int rc = check_ready(h, true);
@@ -387,43 +494,13 @@ extern "C" int uppe_rk4_step(UppeHandle* h, double z_phase, double L, double z_s
         uppe_set_error(h, "subcycle length must be positive");
         return UPPE_E_ARG;
     }
-    double dz;
     const bool adaptive = !(dzmin >= L - z_sub);
     rc = check_range(h, z_phase + (L - z_sub));
     if (rc) return rc;
-    if (adaptive) {
-        StepArgs z = split_z(h, z_phase);
-        CUDA_TRY(h, eval_to_J(h, h->qi, z));
-        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STORE_K, h->J, h->k1, nullptr, nullptr, 0.f, 0.f, z));
-        const float init[4] = {0.f, INFINITY, 0.f, 0.f};
-        CUDA_TRY(h, cudaMemcpyAsync(h->red, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
-        PROF_TRY(h, UPPE_CLASS_STEP_SIZE, launch_absmax(h, h->qi));
-        PROF_TRY(h, UPPE_CLASS_STEP_SIZE, launch_step_size(h, h->qi, h->k1, L, 0.4, 1e-2));
-        float red[4];
-        CUDA_TRY(h, cudaMemcpyAsync(red, h->red, sizeof(red), cudaMemcpyDeviceToHost, h->stream));
-        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        dz = (double)red[1];
-        if (dz < dzmin) dz = dzmin;
-        if (z_sub + dz > L) dz = L - z_sub;
-        PROF_TRY(h, UPPE_CLASS_STEP_SIZE, launch_apply_stage1(h, (float)(dz / 6), (float)(dz / 2)));
-    } else {
-        dz = L - z_sub;
-        StepArgs z = split_z(h, z_phase);
-        CUDA_TRY(h, eval_to_J(h, h->qi, z));
-        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STAGE1, h->J, h->q, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z));
-    }
-    {
-        StepArgs z = split_z(h, z_phase + 0.5 * dz);
-        CUDA_TRY(h, eval_to_J(h, h->q, z));
-        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), z));
-        CUDA_TRY(h, eval_to_J(h, h->q, z));
-        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)dz, z));
-    }
-    {
-        StepArgs z = split_z(h, z_phase + dz);
-        CUDA_TRY(h, eval_to_J(h, h->q, z));
-        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_FINISH, h->J, h->qi, h->qf, nullptr, (float)(dz / 6), 0.f, z));
-    }
+    double dz = 0.0;
+    rc = h->cfg.cylindrical ? rk4_step_generic(h, z_phase, L, z_sub, dzmin, adaptive, &dz)
+                            : rk4_step_cartesian(h, z_phase, L, z_sub, dzmin, adaptive, &dz);
+    if (rc) return rc;
     if (dz_out) *dz_out = dz;
     return UPPE_OK;
 }
@@ -435,6 +512,7 @@ extern "C" int uppe_finish(UppeHandle* h, double z_phase, void* A, void* J, void
     rc = check_range(h, z_phase);
     if (rc) return rc;
     StepArgs z = split_z(h, z_phase);
+    h->E_valid = 0;
     PROF_TRY(h, UPPE_CLASS_OTHER, real_pass(h, REAL_FINISH, h->qi, (float2*)A, z));
     PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_pass(h, TIME_J, h->E, J ? (float2*)J : h->J, nullptr));
     if (chi_w || ne_w) PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_pass(h, TIME_CHI_NE, h->E, (float2*)chi_w, (float2*)ne_w));
@@ -448,6 +526,7 @@ extern "C" int uppe_eval_rhs(UppeHandle* h, const void* q_in, double z_phase, vo
     rc = check_range(h, z_phase);
     if (rc) return rc;
     StepArgs z = split_z(h, z_phase);
+    h->E_valid = 0;
     CUDA_TRY(h, eval_to_J(h, (const float2*)q_in, z));
     PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STORE_K, h->J, (float2*)S_out, nullptr, nullptr, 0.f, 0.f, z));
     return UPPE_OK;

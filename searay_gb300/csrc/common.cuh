@@ -77,25 +77,51 @@ UPPE_DEV float ff_phase(float Khi, float Klo, float zhi, float zlo) {
     return r + e;
 }
 
-// Per-point linear operator, built once per material update:
-//   x = high part of K = Re(kz) + kg,  y = low part of K,  z = Re(kz),  w = Im(kz)
-// The propagator factor exp(i (kz + kg) z) = exp(-Im(kz) z) * exp(i K z).
+// Per-point linear operator, built once per material update.  The propagator factor is
+//   exp(i (kz + kg) z) = exp(-Im(kz) z) * exp(i K z),   K = Re(kz) + kg(w),
+// so every point stores K as a float-float pair (8 bytes).  Re(kz) is recovered as K - kg(w) with
+// kg(w) = -w/v_window held per frequency (also float-float); Im(kz) is stored per point only for
+// absorbing media (complex chi), otherwise it is zero.
+struct OpView {
+    const float2* __restrict__ K;    // [P] {hi, lo}
+    const float* __restrict__ ki;    // [P] Im kz, or nullptr when the medium is real
+    const float2* __restrict__ kg;   // [N0] {hi, lo}
+};
+
+struct OpPoint {
+    float Khi, Klo, kzr, kzi;
+};
+
+UPPE_DEV OpPoint op_at(const OpView& v, size_t idx, float2 kgw) {
+    const float2 k = v.K[idx];
+    OpPoint o;
+    o.Khi = k.x;
+    o.Klo = k.y;
+    o.kzr = (k.x - kgw.x) + (k.y - kgw.y);
+    o.kzi = v.ki ? v.ki[idx] : 0.f;
+    return o;
+}
+
+// i kz
+UPPE_DEV float2 op_ikz(const OpPoint& o) { return make_float2(-o.kzi, o.kzr); }
+
 struct PhaseArgs {
     float zhi, zlo;  // z as float-float
     int plain;       // 1: plain FP32 phase K*z (no float-float), for the plain-FP32 form
 };
 
-UPPE_DEV float2 propagator_factor(float4 op, PhaseArgs pa, float sign) {
+UPPE_DEV float2 propagator_factor(const OpPoint& o, PhaseArgs pa, float sign) {
     float ph;
     if (pa.plain) {
-        ph = op.x * (pa.zhi + pa.zlo);
+        ph = o.Khi * (pa.zhi + pa.zlo);
     } else {
-        ph = ff_phase(op.x, op.y, pa.zhi, pa.zlo);
+        ph = ff_phase(o.Khi, o.Klo, pa.zhi, pa.zlo);
     }
     float s, c;
     sincosf(ph, &s, &c);
     // sign=+1: exp(i K z) exp(-Ki z);  sign=-1: exp(-i K z) exp(+Ki z)
-    float amp = expf(-sign * op.w * (pa.zhi + pa.zlo));
+    if (o.kzi == 0.f) return make_float2(c, sign * s);
+    const float amp = expf(-sign * o.kzi * (pa.zhi + pa.zlo));
     return make_float2(amp * c, sign * amp * s);
 }
 

@@ -60,13 +60,29 @@ UPPE_DEV void dft_small<8>(float2 (&u)[8], bool inv) {
     u[7] = csub(e[3], t3);
 }
 
+// Twiddle sources: a global table of 2^log entries tw[j] = exp(-2 pi i j / 2^log), or a shared
+// table holding the first half of such a table (the second half is its negative).
+struct TwGlobal {
+    const float2* __restrict__ p;
+    int log;
+    UPPE_DEV float2 get(int j) const { return __ldg(&p[j]); }
+};
+struct TwHalfShared {
+    const float2* p;
+    int log;
+    UPPE_DEV float2 get(int j) const {
+        const int half = 1 << (log - 1);
+        float2 v = p[j & (half - 1)];
+        return (j & half) ? make_float2(-v.x, -v.y) : v;
+    }
+};
+
 // One radix-R stage over all nb transforms; thread `tid` of `nthr` handles ITEMS butterflies.
 // batch_fast: consecutive threads take consecutive transforms (use when es != 1 so that the
 // accesses of a warp are contiguous in shared memory).
-template <int R, int ITEMS>
-UPPE_DEV void stockham_stage(float2* buf, int logN, int logp, int lognb, int bs, int es,
-                             const float2* __restrict__ tw, int twLog, bool inv, bool batch_fast,
-                             int tid, int nthr) {
+template <int R, int ITEMS, class TW>
+UPPE_DEV void stockham_stage(float2* buf, int logN, int logp, int lognb, int bs, int es, const TW& tw, bool inv,
+                             bool batch_fast, int tid, int nthr) {
     constexpr int LOGR = (R == 2) ? 1 : (R == 4) ? 2 : 3;
     const int logq = logN - LOGR;
     const int nq = 1 << logq;
@@ -89,10 +105,10 @@ UPPE_DEV void stockham_stage(float2* buf, int logN, int logp, int lognb, int bs,
 #pragma unroll
         for (int r = 0; r < R; ++r) u[it][r] = base[(i + r * nq) * es];
         if (logp > 0) {
-            const int sh = twLog - logp - LOGR;  // NT / (p R)
+            const int sh = tw.log - logp - LOGR;  // NT / (p R)
 #pragma unroll
             for (int r = 1; r < R; ++r) {
-                float2 w = __ldg(&tw[(r * k) << sh]);
+                float2 w = tw.get((r * k) << sh);
                 if (inv) w.y = -w.y;
                 u[it][r] = cmul(u[it][r], w);
             }
@@ -111,32 +127,40 @@ UPPE_DEV void stockham_stage(float2* buf, int logN, int logp, int lognb, int bs,
 
 // Full transform along one axis.  ET = elements per thread = nb*N/nthr (compile time); radix 8
 // stages first, then one radix-4 or radix-2 stage for the remainder.
-template <int ET>
-UPPE_DEV void fft_axis(float2* buf, int logN, int lognb, int bs, int es, const float2* __restrict__ tw,
-                       int twLog, bool inv, int tid, int nthr) {
-    const bool batch_fast = (es != 1);
+template <int ET, class TW>
+UPPE_DEV void fft_axis_tw(float2* buf, int logN, int lognb, int bs, int es, const TW& tw, bool inv, int tid,
+                          int nthr, int batch_fast_mode = -1) {
+    // batch_fast_mode: -1 = automatic (batch-fast when es != 1), 0 = element-fast, 1 = batch-fast
+    const bool batch_fast = (batch_fast_mode < 0) ? (es != 1) : (batch_fast_mode != 0);
     int logp = 0;
     while (logp < logN) {
         const int rem = logN - logp;
         if constexpr (ET >= 8) {
             if (rem >= 3) {
-                stockham_stage<8, ET / 8>(buf, logN, logp, lognb, bs, es, tw, twLog, inv, batch_fast, tid, nthr);
+                stockham_stage<8, ET / 8>(buf, logN, logp, lognb, bs, es, tw, inv, batch_fast, tid, nthr);
                 logp += 3;
                 continue;
             }
         }
         if constexpr (ET >= 4) {
             if (rem >= 2) {
-                stockham_stage<4, ET / 4>(buf, logN, logp, lognb, bs, es, tw, twLog, inv, batch_fast, tid, nthr);
+                stockham_stage<4, ET / 4>(buf, logN, logp, lognb, bs, es, tw, inv, batch_fast, tid, nthr);
                 logp += 2;
                 continue;
             }
         }
         if constexpr (ET >= 2) {
-            stockham_stage<2, ET / 2>(buf, logN, logp, lognb, bs, es, tw, twLog, inv, batch_fast, tid, nthr);
+            stockham_stage<2, ET / 2>(buf, logN, logp, lognb, bs, es, tw, inv, batch_fast, tid, nthr);
             logp += 1;
         } else {
             break;  // unreachable for valid launches (ET >= 2 whenever logN >= 1)
         }
     }
+}
+
+// Global-table form (twLog = log2 of the table size).
+template <int ET>
+UPPE_DEV void fft_axis(float2* buf, int logN, int lognb, int bs, int es, const float2* __restrict__ tw, int twLog,
+                       bool inv, int tid, int nthr) {
+    fft_axis_tw<ET>(buf, logN, lognb, bs, es, TwGlobal{tw, twLog}, inv, tid, nthr);
 }

@@ -21,7 +21,7 @@ enum { C_STORE = 0, C_FINISH1 = 1, C_SPEC = 2 };
 struct GemmArgs {
     const float2* A;  // operand source ([w][r|k][m] layout, row length N1, N2 azimuthal nodes)
     const float* B;   // [N2][NI][NK]
-    const float4* op;
+    OpView op;
     float2* C0;       // store target / q_out / A_out
     float2* C1;       // E (finish) / qf
     const float2* qi;
@@ -55,9 +55,9 @@ __global__ void __launch_bounds__(256) k_hankel_gemm(GemmArgs g) {
                 const size_t idx = ((size_t)w * g.N1 + k) * g.N2 + m;
                 v = g.A[idx];
                 if (AMODE != A_PLAIN) {
-                    float4 o = g.op[idx];
+                    const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
                     v = cmul(propagator_factor(o, pa, 1.f), v);
-                    if (AMODE == A_QPHASE_IKZ) v = cmul(make_float2(-o.w, o.z), v);
+                    if (AMODE == A_QPHASE_IKZ) v = cmul(op_ikz(o), v);
                 }
             }
             As[kk][ww] = v;
@@ -97,13 +97,13 @@ __global__ void __launch_bounds__(256) k_hankel_gemm(GemmArgs g) {
             if (CMODE == C_STORE) {
                 g.C0[idx] = v;
             } else if (CMODE == C_FINISH1) {
-                float4 o = g.op[idx];
+                const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
                 if (g.C0) g.C0[idx] = v;
-                g.C1[idx] = cmul(make_float2(-o.w, o.z), v);
+                g.C1[idx] = cmul(op_ikz(o), v);
             } else {
-                float4 o = g.op[idx];
+                const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
                 float2 f = propagator_factor(o, pa, -1.f);
-                float2 s = cscale(cmul_i(cmul(f, v)), 0.5f / o.z);
+                float2 s = cscale(cmul_i(cmul(f, v)), 0.5f / o.kzr);
                 switch (g.spec_mode) {
                     case SPEC_STORE_K:
                         g.C0[idx] = s;
@@ -170,7 +170,7 @@ static cudaError_t run_gemm(UppeHandle* h, GemmArgs& g) {
 
 static GemmArgs base_args(UppeHandle* h, StepArgs z) {
     GemmArgs g{};
-    g.op = h->op;
+    g.op = uppe_op_view(h);
     g.N0 = h->N0;
     g.N1 = h->N1;
     g.N2 = h->N2;

@@ -1,0 +1,266 @@
+// Time-axis pass of one UPPE right-hand-side evaluation: the part of SeaRay's update_current
+// (modules/uppe_kernel.py:139-186) that runs along t for every transverse point.
+//
+// One CTA takes C adjacent transverse points ("columns") and all N0 = M + 1 frequencies:
+//   1. irfft along w (fft.cl:257-280, 1/Nt normalised) as an M-point complex inverse FFT of the
+//      even/odd packing Z[k] = (X[k] + conj X[M-k]) + i e^{2 pi i k/Nt} (X[k] - conj X[M-k]),
+//      which leaves z[m] = Nt (E(2m) + i E(2m+1)),
+//   2. per time sample: Kerr chi = ng chi3/nref E^2 (uppe.cl:132-151), the ionization rate
+//      (ionization.cl:22-44 explicit / 71-97 series), the electron density by the reverse
+//      trapezoid sum with rate(Nt-1) = 0 and depletion ne = ng (1 - exp(-S)) (ionization.cl:127-155),
+//      SoftTimeWindow on ne (fft.cl:331-355), P = chi E and Jpl = ne E (uppe.cl:153-165,
+//      uppe_kernel.py:169); P and Jpl are written back packed as even/odd pairs, in place,
+//   3. two M-point forward FFTs (P, then Jpl), split into the real spectra and
+//      J = -i w P + Jpl / (0.1 - i w), times the NL filter (fft.cl:282-329, uppe_kernel.py:171-186).
+// The density sum is a two-pass blocked scan: every thread sums its own 32 consecutive samples,
+// then adds the totals of all later segments of its column (the sum runs from high to low t).
+// The sums are float-float in the mixed form.
+#include <math.h>
+
+#include "common.cuh"
+#include "fft_smem.cuh"
+#include "uppe_internal.h"
+
+struct TimeParams {
+    int Nt, logNt, M, logM, C, logC, S, spt;
+    float inv_nt, hdt, redchi3, damping;
+    int rate_form;
+    float fconv, cutoff;
+    float y0, ypow, yexp;  // explicit form: rate = 2^(y0 + ypow log2(Em) + yexp / Em)
+    float lrc2;            // series form: log2(rate_conv)
+    float c2[6];           // series form: log2(e) * c_i, polynomial in L = ln(Em)
+    int wcut, wwid, plain;
+};
+
+#define UPPE_LN2 0.69314718055994530942f
+
+// Ionization rate in simulation units from the field in simulation units.
+__device__ __forceinline__ float ion_rate(const TimeParams& tp, float e) {
+    const float em = fmaf(tp.fconv, fabsf(e), tp.cutoff);
+    const float l2 = __log2f(em);
+    if (tp.rate_form == UPPE_RATE_EXPLICIT) {
+        return exp2f(fmaf(tp.ypow, l2, fmaf(tp.yexp, __frcp_rn(em), tp.y0)));
+    }
+    const float L = l2 * UPPE_LN2;
+    float p = tp.c2[5];
+    p = fmaf(p, L, tp.c2[4]);
+    p = fmaf(p, L, tp.c2[3]);
+    p = fmaf(p, L, tp.c2[2]);
+    p = fmaf(p, L, tp.c2[1]);
+    p = fmaf(p, L, tp.c2[0]);
+    return exp2f(tp.lrc2 + p);
+}
+
+__device__ __forceinline__ float smooth5(float q) { return q * q * q * (10.f - 15.f * q + 6.f * q * q); }
+
+__device__ __forceinline__ float soft_window(int i, int Ni, int cut, int wid) {
+    float f = 1.f;
+    if (i < cut || i > Ni - cut - 1) f = 0.f;
+    if (i >= cut && i < cut + wid) f *= smooth5((float)(i - cut) / (float)wid);
+    if (i <= Ni - cut - 1 && i > Ni - cut - wid - 1) f *= smooth5((float)(Ni - cut - 1 - i) / (float)wid);
+    return f;
+}
+
+__device__ __forceinline__ void acc_add(ffloat& s, float p, int plain) {
+    if (plain)
+        s.hi += p;
+    else
+        s = ff_add_f(s, p);
+}
+
+// Real spectrum X[k], k in [0, M], of the real signal packed as z[m] = x(2m) + i x(2m+1) whose
+// M-point FFT is Zc: X[k] = (Za + Zb)/2 - (i/2) e^{-2 pi i k/Nt} (Za - Zb), Za = Zc[k mod M],
+// Zb = conj Zc[(M-k) mod M].
+__device__ __forceinline__ float2 real_spectrum(float2 Za, float2 Zb_raw, float2 twk) {
+    const float2 Zb = cconj(Zb_raw);
+    const float2 s = cadd(Za, Zb);
+    const float2 d = cmul(twk, csub(Za, Zb));
+    return cscale(csub(s, cmul_i(d)), 0.5f);
+}
+
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gsrc));
+}
+
+__global__ void __launch_bounds__(256, 3) k_time(int mode, const float2* __restrict__ E, float2* __restrict__ out0,
+                                                  float2* __restrict__ out1, const float* __restrict__ ng,
+                                                  const float* __restrict__ wv, const float* __restrict__ filt,
+                                                  const float2* __restrict__ tw, int twLog, TimeParams tp) {
+    // shared layout: Zp [M+1][C] (E pairs, then P pairs), Zj [M+1][C] (the raw half spectrum X
+    // while loading, then the rates (r(2m), r(2m+1)), then Jpl pairs), twiddles e^{-2 pi i j/Nt}
+    // for j < Nt/2, one float-float segment total per thread.  Rows of C float2 keep the
+    // column-batched FFT accesses of a warp on distinct banks.
+    extern __shared__ float2 Zp[];
+    const int C = tp.C, logC = tp.logC, Nt = tp.Nt, M = tp.M, S = tp.S;
+    float2* Zj = Zp + (size_t)(M + 1) * C;
+    float2* twl = Zj + (size_t)(M + 1) * C;
+    ffloat* tot = reinterpret_cast<ffloat*>(twl + (Nt >> 1));
+    const int tid = threadIdx.x, T = blockDim.x;
+    const size_t col0 = (size_t)blockIdx.x * C;
+    const bool ionize = tp.rate_form != UPPE_RATE_NONE;
+    const TwHalfShared tws{twl, tp.logNt};
+
+    // ---- 1. stage the half spectrum X[k][c], k in [0, M], with asynchronous copies ----
+    for (int it = tid; it < (M + 1) * C; it += T) {
+        const int c = it & (C - 1);
+        const int k = it >> logC;
+        cp_async8(&Zj[it], &E[(size_t)k * S + col0 + c]);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    for (int j = tid; j < (Nt >> 1); j += T) twl[j] = __ldg(&tw[j << (twLog - tp.logNt)]);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    __syncthreads();
+    // even/odd packing Z[k] = (X[k] + conj X[M-k]) + i e^{2 pi i k/Nt} (X[k] - conj X[M-k])
+    const int npairs = (M / 2 + 1) * C;
+    for (int it = tid; it < npairs; it += T) {
+        const int c = it & (C - 1);
+        const int k = it >> logC;
+        float2 Xa = Zj[k * C + c];
+        float2 Xm = Zj[(M - k) * C + c];
+        if (k == 0) {
+            Xa.y = 0.f;
+            Xm.y = 0.f;
+        }
+        const float2 t = cconj(tws.get(k));  // e^{+2 pi i k / Nt}
+        const float2 b = cconj(Xm);
+        Zp[k * C + c] = cadd(cadd(Xa, b), cmul_i(cmul(t, csub(Xa, b))));
+        if (k != 0 && 2 * k != M) {
+            const float2 t2 = make_float2(-t.x, t.y);  // e^{2 pi i (M-k)/Nt}
+            const float2 b2 = cconj(Xa);
+            Zp[(M - k) * C + c] = cadd(cadd(Xm, b2), cmul_i(cmul(t2, csub(Xm, b2))));
+        }
+    }
+    __syncthreads();
+    fft_axis_tw<16>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
+
+    // ---- 2. sources, in place ----
+    const int c = tid & (C - 1);
+    const int seg = tid >> logC;
+    const int mps = tp.spt >> 1;  // packed pairs per thread
+    const int m0 = seg * mps;
+    const int t1 = 2 * (m0 + mps);  // first sample of the next segment
+    const float ngc = ng[col0 + c];
+    const float kerr = ngc * tp.redchi3;
+    const float inv = tp.inv_nt;
+    float r_next = 0.f;
+    if (ionize) {
+        if (t1 <= Nt - 2) r_next = ion_rate(tp, Zp[(t1 >> 1) * C + c].x * inv);
+        ffloat part = {0.f, 0.f};
+        float rn = r_next;
+        for (int m = m0 + mps - 1; m >= m0; --m) {
+            const float2 zv = Zp[m * C + c];
+            const int t = 2 * m + 1;
+            const float r1 = (t == Nt - 1) ? 0.f : ion_rate(tp, zv.y * inv);
+            if (t <= Nt - 2) acc_add(part, tp.hdt * (r1 + rn), tp.plain);
+            const float r0 = ion_rate(tp, zv.x * inv);
+            acc_add(part, tp.hdt * (r0 + r1), tp.plain);
+            rn = r0;
+            Zj[m * C + c] = make_float2(r0, r1);  // this thread's own slot, reused below
+        }
+        tot[tid] = part;
+    }
+    __syncthreads();  // all segment totals written; from here each thread touches only its own pairs
+    ffloat Sacc = {0.f, 0.f};
+    if (ionize) {
+        const int nseg = T >> logC;
+        for (int s2 = seg + 1; s2 < nseg; ++s2) {
+            const ffloat v = tot[(s2 << logC) + c];
+            if (tp.plain)
+                Sacc.hi += v.hi;
+            else
+                Sacc = ff_add(Sacc, v);
+        }
+    }
+    {
+        float rn = r_next;
+        const int wlo = tp.wcut + tp.wwid, whi = Nt - tp.wcut - tp.wwid - 1;  // window is 1 on [wlo, whi]
+        for (int m = m0 + mps - 1; m >= m0; --m) {
+            const float2 zv = Zp[m * C + c];
+            const float e1 = zv.y * inv, e0 = zv.x * inv;
+            float ne1 = 0.f, ne0 = 0.f;
+            if (ionize) {
+                const float2 rr = Zj[m * C + c];
+                const int t = 2 * m + 1;
+                if (t <= Nt - 2) acc_add(Sacc, tp.hdt * (rr.y + rn), tp.plain);
+                ne1 = -ngc * expm1f(-ff_value(Sacc));
+                if (t < wlo || t > whi) ne1 *= soft_window(t, Nt, tp.wcut, tp.wwid);
+                acc_add(Sacc, tp.hdt * (rr.x + rr.y), tp.plain);
+                rn = rr.x;
+                ne0 = -ngc * expm1f(-ff_value(Sacc));
+                if (t - 1 < wlo || t - 1 > whi) ne0 *= soft_window(t - 1, Nt, tp.wcut, tp.wwid);
+            }
+            const float chi1 = kerr * e1 * e1, chi0 = kerr * e0 * e0;
+            if (mode == TIME_J) {
+                Zp[m * C + c] = make_float2(chi0 * e0, chi1 * e1);
+                Zj[m * C + c] = make_float2(ne0 * e0, ne1 * e1);
+            } else {
+                Zp[m * C + c] = make_float2(chi0, chi1);
+                Zj[m * C + c] = make_float2(ne0, ne1);
+            }
+        }
+    }
+    __syncthreads();
+
+    // ---- 3. forward FFTs (P, then Jpl) and the current ----
+    const bool two = ionize || mode == TIME_CHI_NE;
+    fft_axis_tw<16>(Zp, tp.logM, logC, 1, C, tws, false, tid, T);
+    if (two) fft_axis_tw<16>(Zj, tp.logM, logC, 1, C, tws, false, tid, T);
+    for (int it = tid; it < (M + 1) * C; it += T) {
+        const int cc = it & (C - 1);
+        const int k = it >> logC;
+        const int ka = k & (M - 1), kb = (M - k) & (M - 1);
+        const float2 twk = tws.get(k);  // e^{-2 pi i k / Nt}
+        const float2 P = real_spectrum(Zp[ka * C + cc], Zp[kb * C + cc], twk);
+        const float2 Q = two ? real_spectrum(Zj[ka * C + cc], Zj[kb * C + cc], twk) : make_float2(0.f, 0.f);
+        const size_t o = (size_t)k * S + col0 + cc;
+        if (mode == TIME_J) {
+            const float wk = wv[k];
+            float2 J = cmul_mi(cscale(P, wk));  // -i w P
+            if (ionize) J = cadd(J, cdiv(Q, make_float2(tp.damping, -wk)));
+            out0[o] = cscale(J, filt[k]);
+        } else {
+            if (out0) out0[o] = P;
+            if (out1) out1[o] = ionize ? Q : make_float2(0.f, 0.f);
+        }
+    }
+}
+
+cudaError_t uppe_configure_time_kernel(size_t smem_bytes) {
+    return cudaFuncSetAttribute(k_time, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+}
+
+cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1) {
+    const UppeConfig& c = h->cfg;
+    TimeParams tp;
+    tp.Nt = h->Nt;
+    tp.logNt = ilog2_exact(h->Nt);
+    tp.M = h->M;
+    tp.logM = ilog2_exact(h->M);
+    tp.C = h->time_cols;
+    tp.logC = ilog2_exact(h->time_cols);
+    tp.S = h->S;
+    const int T = h->Nt * h->time_cols / 32;
+    tp.spt = h->Nt * h->time_cols / T;
+    tp.inv_nt = (float)(1.0 / (double)h->Nt);
+    tp.hdt = (float)(0.5 * c.dt);
+    tp.redchi3 = (float)c.chi3_over_nref;
+    tp.damping = (float)c.damping;
+    tp.rate_form = c.rate_form;
+    tp.fconv = (float)c.field_conv;
+    tp.cutoff = (float)c.field_cutoff;
+    const double log2e = 1.4426950408889634;
+    tp.y0 = (c.rate_form == UPPE_RATE_EXPLICIT) ? (float)log2(c.rate_conv * c.c_pre) : 0.f;
+    tp.ypow = (float)c.c_pow;
+    tp.yexp = (float)(c.c_exp * log2e);
+    tp.lrc2 = (c.rate_conv > 0) ? (float)log2(c.rate_conv) : 0.f;
+    for (int i = 0; i < 6; ++i) tp.c2[i] = (float)(c.clog[i] * log2e);
+    tp.wcut = c.window_cutoff;
+    tp.wwid = c.window_width;
+    tp.plain = (c.precision == UPPE_PREC_FP32);
+    const size_t smem = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
+    h->launches++;
+    k_time<<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw, h->twLog,
+                                                         tp);
+    return cudaGetLastError();
+}

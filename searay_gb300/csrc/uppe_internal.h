@@ -20,6 +20,7 @@ enum UppeSpecMode {
 enum UppeRealMode {
     REAL_E = 0,       // E <- T^-1( i kz exp(i(kz+kg)z) q )
     REAL_FINISH = 1,  // A <- T^-1( exp(i(kz+kg)z) q ) and E <- i kz A   (uppe_kernel.py:250-253)
+    REAL_APPLY1 = 2,  // first RK stage from k1 (q <- qi + Ce k1, qf <- qi + Cs k1), then E from q
 };
 
 // Modes of the time-axis pass.
@@ -42,7 +43,10 @@ struct UppeHandle {
     cudaStream_t stream;
     // library-owned device buffers
     float2 *q, *qi, *qf, *k1, *E, *J, *scratch;
-    float4* op;
+    float2* opK;     // [P] K = Re kz + kg as float-float
+    float* opKi;     // [P] Im kz (read only when complex_medium)
+    float2* kg2;     // [N0] kg as float-float
+    int complex_medium;
     float* ng;
     float2* tw;
     float* w;        // omega per bin (FP32)
@@ -56,12 +60,19 @@ struct UppeHandle {
     int have_grid, have_material, have_field;
     double max_abs_K;   // max |Re kz + kg| of the current operator
     double max_Ki;      // max Im kz of the current operator
+    long long mat_version; // incremented by every uppe_set_material
+    int E_valid;           // E holds T^-1(i kz e^{..} qi) for (E_z, E_mat): reusable by the next step
+    double E_z;
+    long long E_mat;
     long long launches; // kernels launched by this handle
     void* prof;         // profiling state (capi.cu), NULL when off
     char err[512];
 };
 
 int uppe_set_error(UppeHandle* h, const char* fmt, ...);
+
+struct OpView;
+OpView uppe_op_view(const UppeHandle* h);
 
 // ---- kernel launch wrappers (uppe_kernels.cu) ----
 cudaError_t launch_build_operator(UppeHandle* h);
@@ -71,6 +82,11 @@ cudaError_t uppe_configure_time_kernel(size_t smem_bytes);
 cudaError_t launch_real_cart(UppeHandle* h, int mode, const float2* src, float2* A_out, StepArgs z);
 cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, float2* q_out, float2* qf_io,
                              const float2* qi, float Cs, float Ce, StepArgs z);
+// Cartesian fused pass: forward FFT of J, RHS, RK stage (SPEC_STAGE1/STAGE23/FINISH), then E at
+// z_next from the new stage estimate; writes qf / qi as the stage requires and E.
+cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next);
+// Cartesian first stage from k1 (adaptive step) fused with the inverse transform to E.
+cudaError_t launch_apply1_cart(UppeHandle* h, float Cs, float Ce, StepArgs z);
 cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1);
 cudaError_t launch_absmax(UppeHandle* h, const float2* q);
 cudaError_t launch_step_size(UppeHandle* h, const float2* q, const float2* k, double L, double dphi, double rel_amin);
