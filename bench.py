@@ -36,17 +36,39 @@ sys.path.insert(0, str(ROOT))
 
 METRIC = "UPPE grid-pt*steps/s (RK4 z-step)"
 UNIT = "grid-pt*steps/s"
-# algorithmic HBM bytes per grid point per launch of each kernel class on a Cartesian grid
-# (complex64 fields, 8-byte per-point operator K = Re kz + kg as float-float):
+# Algorithmic work per launch of each kernel class.  Complex64 fields, 8-byte per-point operator
+# K = Re kz + kg (float-float).
+# Cartesian grids (bytes per grid point):
 #   transverse_inverse: read q, K; write E
 #   time_pass: read E; write J
-#   transverse_forward_rk (fused slice pass): read J, K, qi and/or qf; write qf or qi; write E for the
-#   next evaluation -- 40 / 48 / 48 / 40 bytes for the four RK stages
-ALGO_BYTES = {
+#   transverse_forward_rk (fused slice pass): read J, K, qi and/or qf; write qf or qi; write E for
+#   the next evaluation -- 40 / 48 / 48 / 40 bytes for the four RK stages
+CART_BYTES = {
     "transverse_inverse": 8 + 8 + 8,
     "time_pass": 8 + 8,
     "transverse_forward_rk": (40 + 48 + 48 + 40) / 4.0,
 }
+# Cylindrical grids: the transverse classes are the Hankel GEMMs (complex x real, 4 flops per
+# multiply-add): inverse M=N0 rows, N=Nr, K=Nk; forward N=Nr, K=Nr.  Bytes per point as above with
+# the RK epilogue of the forward pass writing q and qf (40 / 48 / 48 / 32).
+CYL_BYTES = {
+    "transverse_inverse": 8 + 8 + 8,
+    "time_pass": 8 + 8,
+    "transverse_forward_rk": (40 + 48 + 48 + 32) / 4.0,
+}
+
+
+def class_models(vd):
+    """{class: {"bytes": B per launch, "flops": F per launch (transverse GEMMs only)}}"""
+    N = vd["wave grid"]
+    P = N[0] * N[1] * N[2]
+    if vd["wave coordinates"] == "cartesian":
+        return {k: {"bytes": b * P} for k, b in CART_BYTES.items()}
+    Nr, Nk = N[1], vd.get("radial modes", N[1])
+    m = {k: {"bytes": b * P} for k, b in CYL_BYTES.items()}
+    m["transverse_inverse"]["flops"] = 4.0 * N[0] * N[2] * Nr * Nk
+    m["transverse_forward_rk"]["flops"] = 4.0 * N[0] * N[2] * Nr * Nr
+    return m
 
 
 def dist_env():
@@ -100,11 +122,12 @@ class ClockSampler:
 
 
 def measured_peaks():
+    """(HBM GB/s, bf16 dense TFLOP/s burst, source)"""
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
         d = json.loads(p.read_text())
-        return d.get("hbm_gbs", 6800.0), "measured"
-    return 6800.0, "fallback"
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), "measured"
+    return 6800.0, 1900.0, "fallback"
 
 
 def ncu_traffic(workload):
@@ -113,6 +136,12 @@ def ncu_traffic(workload):
     if p.exists():
         return json.loads(p.read_text())
     return {}
+
+
+def working_set_mb(vd):
+    N = vd["wave grid"]
+    P = N[0] * N[1] * N[2]
+    return (6 * 8 + 8 + 4) * P / 1e6  # q, qi, qf, k1, E, J (complex64) + K (float2) + Im kz
 
 
 def build_device(vd, precision):
@@ -305,29 +334,42 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms = float(t.item())
     value = P * args.steps * ws / (ms / 1e3)
-    peak, peak_kind = measured_peaks()
+    peak, tpeak, peak_kind = measured_peaks()
+    models = class_models(vd)
+    tensor_path = vd["wave coordinates"] != "cartesian" and args.precision == "mixed"
     kernels = {}
     for name, (tms, cnt) in prof.items():
         if cnt == 0:
             continue
         entry = {"launch_regions": cnt, "total_ms": tms, "avg_us": 1e3 * tms / cnt}
-        if name in ALGO_BYTES:
-            gbs = ALGO_BYTES[name] * P / (tms / cnt / 1e3) / 1e9
-            entry.update({"algo_bytes_per_launch": ALGO_BYTES[name] * P, "achieved_GBs": gbs, "frac": gbs / peak})
+        if name in models:
+            sec = tms / cnt / 1e3
+            gbs = models[name]["bytes"] / sec / 1e9
+            entry.update({"algo_bytes_per_launch": models[name]["bytes"], "achieved_GBs": gbs, "frac": gbs / peak})
+            if "flops" in models[name]:
+                tf = models[name]["flops"] / sec / 1e12
+                entry.update({"algo_flops_per_launch": models[name]["flops"], "achieved_TFLOPs": tf,
+                              "tensor_frac": tf / tpeak if tensor_path else None})
         kernels[name] = entry
-    dom = max((k for k in kernels if k in ALGO_BYTES), key=lambda k: kernels[k]["total_ms"])
+    dom = max((k for k in kernels if k in models), key=lambda k: kernels[k]["total_ms"])
     traffic = ncu_traffic(args.workload).get(dom)
-    roof = {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["achieved_GBs"], "peak": peak, "unit": "GB/s",
-            "frac": kernels[dom]["frac"], "traffic": traffic, "peak_source": peak_kind,
-            "share": kernels[dom]["total_ms"] / sum(v["total_ms"] for v in kernels.values())}
+    share = kernels[dom]["total_ms"] / sum(v["total_ms"] for v in kernels.values())
+    if tensor_path and "achieved_TFLOPs" in kernels[dom]:
+        roof = {"bound": "tensor", "kernel": dom, "achieved": kernels[dom]["achieved_TFLOPs"], "peak": tpeak,
+                "unit": "TFLOP/s", "frac": kernels[dom]["tensor_frac"], "traffic": traffic, "peak_source": peak_kind,
+                "share": share, "hbm_frac": kernels[dom]["frac"],
+                "note": "algorithmic flops; the split-BF16x3 tensor path executes 3x as many"}
+    else:
+        roof = {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["achieved_GBs"], "peak": peak, "unit": "GB/s",
+                "frac": kernels[dom]["frac"], "traffic": traffic, "peak_source": peak_kind, "share": share}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (float-float phase and density scan)" if args.precision == "mixed" else "f32",
         "data": "synthetic",
-        "config": {"workload": args.workload, "grid": [513, 128, 128] if args.workload == "cart_filament_128" else list(vd["wave grid"][:3]),
+        "config": {"workload": args.workload, "grid": list(vd["wave grid"][:3]),
                    "precision": args.precision, "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "working set (q, qi, qf, op, E, J: ~470 MB) larger than the 129 MB L2"},
+                   "l2": f"working set ({working_set_mb(vd):.0f} MB of fields and operator) vs the 129 MB L2"},
         "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk, "finite": finite,
     }
     if rank == 0 and not args.no_e2e:

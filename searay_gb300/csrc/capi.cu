@@ -15,6 +15,8 @@
 #include "common.cuh"
 #include "uppe_internal.h"
 
+void uppe_split_matrix_tiles(const float* B, int N2, int NI, int NK, std::vector<uint8_t>& out);
+
 static char g_create_error[512] = "";
 
 int uppe_set_error(UppeHandle* h, const char* fmt, ...) {
@@ -108,7 +110,7 @@ static StepArgs split_z(const UppeHandle* h, double z) {
 
 static void free_buffers(UppeHandle* h) {
     void* ptrs[] = {h->q,  h->qi,   h->qf,   h->k1,   h->E,     h->J,      h->scratch, h->opK,  h->opKi, h->kg2,
-                    h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red};
+                    h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red, h->dev_err, h->Minv_tc, h->Mfwd_tc};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -175,6 +177,12 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (c.n2 > nt) nt = c.n2;
     h->twLog = ilog2_exact(nt);
     h->stream = 0;
+    {
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
+            h->num_sms = nsm;
+        if (h->num_sms <= 0) h->num_sms = 152;
+    }
 
     const size_t fbytes = h->P * sizeof(float2);
     cudaError_t e = cudaSuccess;
@@ -202,6 +210,7 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     ALLOC(h->w2n2_d, (size_t)2 * c.n0 * sizeof(double));
     ALLOC(h->kg_d, (size_t)c.n0 * sizeof(double));
     ALLOC(h->red, 4 * sizeof(float));
+    ALLOC(h->dev_err, sizeof(int));
 #undef ALLOC
     if (e != cudaSuccess) {
         uppe_set_error(nullptr, "device allocation failed: %s", cudaGetErrorString(e));
@@ -217,6 +226,7 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
         tw[j] = make_float2((float)cos(a), (float)sin(a));
     }
     e = cudaMemcpy(h->tw, tw.data(), NT * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(h->dev_err, 0, sizeof(int));
     // Allow the kernels that stage a whole slice / time tile in shared memory the full 227 KB; each
     // launch still requests only what its grid needs.
     if (e == cudaSuccess) e = uppe_configure_slice_kernels(227 * 1024);
@@ -282,6 +292,15 @@ extern "C" int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, 
                 }
         CUDA_TRY(h, cudaMemcpy(h->Minv, Minv.data(), Minv.size() * sizeof(float), cudaMemcpyHostToDevice));
         CUDA_TRY(h, cudaMemcpy(h->Mfwd, Mfwd.data(), Mfwd.size() * sizeof(float), cudaMemcpyHostToDevice));
+        if (c.precision == UPPE_PREC_MIXED) {
+            std::vector<uint8_t> t;
+            uppe_split_matrix_tiles(Minv.data(), Nm, Nr, Nk, t);
+            if (!h->Minv_tc) CUDA_TRY(h, cudaMalloc((void**)&h->Minv_tc, t.size()));
+            CUDA_TRY(h, cudaMemcpy(h->Minv_tc, t.data(), t.size(), cudaMemcpyHostToDevice));
+            uppe_split_matrix_tiles(Mfwd.data(), Nm, Nr, Nr, t);
+            if (!h->Mfwd_tc) CUDA_TRY(h, cudaMalloc((void**)&h->Mfwd_tc, t.size()));
+            CUDA_TRY(h, cudaMemcpy(h->Mfwd_tc, t.data(), t.size(), cudaMemcpyHostToDevice));
+        }
     }
     h->have_grid = 1;
     return UPPE_OK;
@@ -548,9 +567,15 @@ extern "C" int uppe_check_finite(UppeHandle* h, int* nonfinite) {
     CUDA_TRY(h, cudaMemcpyAsync(h->red, init, sizeof(init), cudaMemcpyHostToDevice, h->stream));
     CUDA_TRY(h, launch_absmax(h, h->qi));
     float red[4];
+    int derr = 0;
     CUDA_TRY(h, cudaMemcpyAsync(red, h->red, sizeof(red), cudaMemcpyDeviceToHost, h->stream));
+    CUDA_TRY(h, cudaMemcpyAsync(&derr, h->dev_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
     CUDA_TRY(h, cudaStreamSynchronize(h->stream));
     *nonfinite = (red[2] != 0.f) ? 1 : 0;
+    if (derr) {
+        uppe_set_error(h, "a tensor-core kernel's bounded wait expired; results of this handle are invalid");
+        return UPPE_E_CUDA;
+    }
     return UPPE_OK;
 }
 

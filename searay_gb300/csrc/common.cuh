@@ -111,14 +111,15 @@ struct PhaseArgs {
 };
 
 UPPE_DEV float2 propagator_factor(const OpPoint& o, PhaseArgs pa, float sign) {
-    float ph;
-    if (pa.plain) {
-        ph = o.Khi * (pa.zhi + pa.zlo);
-    } else {
-        ph = ff_phase(o.Khi, o.Klo, pa.zhi, pa.zlo);
-    }
     float s, c;
-    sincosf(ph, &s, &c);
+    if (pa.plain) {
+        // plain FP32 form: the phase K z in FP32, full-range sincos
+        sincosf(o.Khi * (pa.zhi + pa.zlo), &s, &c);
+    } else {
+        // float-float phase already reduced to about [-pi, pi]: the hardware sin/cos is accurate to
+        // a few 1e-7 absolute on that range
+        __sincosf(ff_phase(o.Khi, o.Klo, pa.zhi, pa.zlo), &s, &c);
+    }
     // sign=+1: exp(i K z) exp(-Ki z);  sign=-1: exp(-i K z) exp(+Ki z)
     if (o.kzi == 0.f) return make_float2(c, sign * s);
     const float amp = expf(-sign * o.kzi * (pa.zhi + pa.zlo));

@@ -106,11 +106,29 @@ UPPE_DEV void stockham_stage(float2* buf, int logN, int logp, int lognb, int bs,
         for (int r = 0; r < R; ++r) u[it][r] = base[(i + r * nq) * es];
         if (logp > 0) {
             const int sh = tw.log - logp - LOGR;  // NT / (p R)
+            if constexpr (R == 8) {
+                // W^k, W^2k, W^4k from the table; the other powers as products of at most two of them
+                float2 w1 = tw.get(k << sh), w2 = tw.get((2 * k) << sh), w4 = tw.get((4 * k) << sh);
+                if (inv) {
+                    w1.y = -w1.y;
+                    w2.y = -w2.y;
+                    w4.y = -w4.y;
+                }
+                const float2 w3 = cmul(w1, w2);
+                u[it][1] = cmul(u[it][1], w1);
+                u[it][2] = cmul(u[it][2], w2);
+                u[it][3] = cmul(u[it][3], w3);
+                u[it][4] = cmul(u[it][4], w4);
+                u[it][5] = cmul(u[it][5], cmul(w4, w1));
+                u[it][6] = cmul(u[it][6], cmul(w4, w2));
+                u[it][7] = cmul(u[it][7], cmul(w4, w3));
+            } else {
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 w = tw.get((r * k) << sh);
-                if (inv) w.y = -w.y;
-                u[it][r] = cmul(u[it][r], w);
+                for (int r = 1; r < R; ++r) {
+                    float2 w = tw.get((r * k) << sh);
+                    if (inv) w.y = -w.y;
+                    u[it][r] = cmul(u[it][r], w);
+                }
             }
         }
         dft_small<R>(u[it], inv);

@@ -160,8 +160,16 @@ static cudaError_t launch_azimuth(UppeHandle* h, const float2* in, float2* out, 
     return cudaGetLastError();
 }
 
+cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* A, int inverse, float2* C0,
+                             float2* C1, const float2* qi, int NI, int NK, int spec_mode, float Cs, float Ce,
+                             StepArgs z);
+
+// Mixed-precision form: tensor-core GEMM (hankel_tc.cu); plain FP32 form: the FP32 SIMT GEMM below.
 template <int AMODE, int CMODE>
 static cudaError_t run_gemm(UppeHandle* h, GemmArgs& g) {
+    if (h->cfg.precision == UPPE_PREC_MIXED)
+        return launch_hankel_tc(h, AMODE, CMODE, g.A, g.B == h->Minv ? 1 : 0, g.C0, g.C1, g.qi, g.NI, g.NK,
+                                g.spec_mode, g.Cs, g.Ce, g.z);
     dim3 grid((g.NI + GBN - 1) / GBN, (g.N0 + GBM - 1) / GBM, g.N2);
     h->launches++;
     k_hankel_gemm<AMODE, CMODE><<<grid, 256, 0, h->stream>>>(g);

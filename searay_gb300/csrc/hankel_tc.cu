@@ -1,0 +1,383 @@
+// Radial Hankel transform on the 5th-generation tensor cores (tcgen05), split-BF16x3.
+//
+// Same contraction as hankel.cu, C[w][i] = sum_k A(w,k) B[i][k] with complex A and real B (the
+// folded Hankel matrices of modules/grid_tools.py:252-325), but as a real GEMM on the tensor core:
+//   * a tile of 64 frequencies becomes 128 MMA rows, row 2j = Re A(w0+j, .), row 2j+1 = Im A(w0+j, .);
+//   * every FP32 operand x is split into bf16 x_hi + x_lo and the product is accumulated as
+//     A_hi B_hi + A_hi B_lo + A_lo B_hi in FP32 (the dropped A_lo B_lo is ~2^-18 of the product);
+//   * one elected thread issues tcgen05.mma (M=128, N=128, K=16) from shared-memory operands in the
+//     no-swizzle K-major core-matrix layout; the accumulator lives in tensor memory (TMEM) and is
+//     read back with tcgen05.ld for the fused epilogue (store, finish, or ODE RHS + RK stage).
+// Every wait on an mbarrier is bounded; on expiry the kernel records an error flag and skips ahead.
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <vector>
+
+#include "common.cuh"
+#include "uppe_internal.h"
+
+#define TC_ROWS 128  // MMA rows per tile (64 frequencies x re/im)
+#define TC_W 64      // frequencies per tile
+#define TC_N 128     // output columns per tile
+#define TC_K 64      // reduction elements per shared tile (four K=16 MMAs)
+#define TC_TILE_BYTES (TC_ROWS * TC_K * 2)  // 16 KB per bf16 operand tile
+#define TC_STAGE_LD (TC_N + 1)              // padded row of the epilogue staging tile (float2)
+#define TC_WAIT_LIMIT (1 << 24)
+
+enum { TA_PLAIN = 0, TA_QPHASE_IKZ = 1, TA_QPHASE = 2 };
+enum { TC_STORE = 0, TC_FINISH1 = 1, TC_SPEC = 2 };
+
+struct TcArgs {
+    const float2* A;
+    const uint8_t* Btc;  // split matrix tiles [N2][nit][nkt][hi 16 KB | lo 16 KB]
+    int nit, nkt;
+    OpView op;
+    float2* C0;
+    float2* C1;
+    const float2* qi;
+    int N0, N1, N2, NI, NK;
+    int spec_mode;
+    float Cs, Ce;
+    StepArgs z;
+    int* err;
+};
+
+// Byte offset of element (row, k) of a 128 x 64 bf16 tile in the K-major, no-swizzle canonical
+// layout: 8x8 core matrices of 128 contiguous bytes (8 rows of 16 bytes); core matrices adjacent in
+// K are 128 bytes apart (leading byte offset), adjacent in M/N 1024 bytes apart (stride byte offset).
+__device__ __forceinline__ uint32_t core_off(int row, int k) {
+    return (uint32_t)((row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
+}
+
+// Shared-memory matrix descriptor of tcgen05 (start address, LBO, SBO in 16-byte units; version 1;
+// no swizzle).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)(128u >> 4) << 16;
+    d |= (uint64_t)(1024u >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, N = 128, M = 128.
+__device__ __forceinline__ uint32_t instr_desc() {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_ROWS >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, int* err) {
+    for (int i = 0; i < TC_WAIT_LIMIT; ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(ok)
+            : "r"(mbar), "r"(phase)
+            : "memory");
+        if (ok) return true;
+    }
+    if (err) atomicExch(err, 1);
+    return false;
+}
+
+__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
+    hi = __float2bfloat16_rn(x);
+    lo = __float2bfloat16_rn(x - __bfloat162float(hi));
+}
+
+#define TC_THREADS 256
+#define TC_STAGE_BYTES (4 * TC_TILE_BYTES)  // A_hi | A_lo | B_hi | B_lo
+
+__device__ __forceinline__ void cp_async16(uint32_t smem_addr, const void* g) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr), "l"(g));
+}
+
+// One K tile into a pipeline stage: the B tile (already split and laid out in global memory) by
+// asynchronous 16-byte copies, the A tile computed from the fields (phase, i kz) and split in place.
+template <int AMODE>
+__device__ __forceinline__ void tc_load_tile(const TcArgs& g, uint8_t* st, uint32_t st_a, const uint8_t* Btile,
+                                             int w0, int k0, int m, const PhaseArgs& pa, int tid) {
+    for (int c = tid; c < 2 * TC_TILE_BYTES / 16; c += TC_THREADS)
+        cp_async16(st_a + 2 * TC_TILE_BYTES + 16 * c, Btile + 16 * c);
+    asm volatile("cp.async.commit_group;\n" ::);
+#pragma unroll 4
+    for (int e = tid; e < TC_W * TC_K; e += TC_THREADS) {
+        const int kk = e & (TC_K - 1), wl = e >> 6;
+        const int w = w0 + wl, k = k0 + kk;
+        float2 v = make_float2(0.f, 0.f);
+        if (w < g.N0 && k < g.NK) {
+            const size_t idx = ((size_t)w * g.N1 + k) * g.N2 + m;
+            v = g.A[idx];
+            if (AMODE != TA_PLAIN) {
+                const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
+                v = cmul(propagator_factor(o, pa, 1.f), v);
+                if (AMODE == TA_QPHASE_IKZ) v = cmul(op_ikz(o), v);
+            }
+        }
+        __nv_bfloat16 rh, rl, ih, il;
+        split_bf16(v.x, rh, rl);
+        split_bf16(v.y, ih, il);
+        const uint32_t ore = core_off(2 * wl, kk), oim = core_off(2 * wl + 1, kk);
+        *reinterpret_cast<__nv_bfloat16*>(st + ore) = rh;
+        *reinterpret_cast<__nv_bfloat16*>(st + oim) = ih;
+        *reinterpret_cast<__nv_bfloat16*>(st + TC_TILE_BYTES + ore) = rl;
+        *reinterpret_cast<__nv_bfloat16*>(st + TC_TILE_BYTES + oim) = il;
+    }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    // make the generic-proxy and cp.async writes visible to the tensor core (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_issue(uint32_t tmem_d, uint32_t st_a, uint32_t idesc, bool first, uint32_t mbar) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+#pragma unroll
+    for (int ks = 0; ks < TC_K / 16; ++ks) {
+        const uint32_t koff = (uint32_t)ks * 256u;  // two core matrices along K per K=16 step
+        const uint64_t ahi = smem_desc(st_a + koff);
+        const uint64_t alo = smem_desc(st_a + TC_TILE_BYTES + koff);
+        const uint64_t bhi = smem_desc(st_a + 2 * TC_TILE_BYTES + koff);
+        const uint64_t blo = smem_desc(st_a + 3 * TC_TILE_BYTES + koff);
+        const uint32_t acc0 = (!first || ks > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(ahi), "l"(bhi), "r"(idesc), "r"(acc0));
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(ahi), "l"(blo), "r"(idesc), "r"(1u));
+        asm volatile(
+            "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+            "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+            "l"(alo), "l"(bhi), "r"(idesc), "r"(1u));
+    }
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+                 : "memory");
+}
+
+template <int AMODE, int CMODE>
+__global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
+    extern __shared__ __align__(1024) uint8_t smem_raw[];
+    // two pipeline stages of [A_hi | A_lo | B_hi | B_lo] (1024-byte aligned), reused afterwards as
+    // the epilogue staging tile
+    const uint32_t raw_a = (uint32_t)__cvta_generic_to_shared(smem_raw);
+    uint8_t* tiles = smem_raw + (((raw_a + 1023u) & ~1023u) - raw_a);
+    float2* stage = reinterpret_cast<float2*>(tiles);
+    __shared__ uint64_t mbar[2];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int aborted;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int m = blockIdx.z;
+    const int w0 = blockIdx.y * TC_W;
+    const int it = blockIdx.x;
+    const int i0 = it * TC_N;
+    const PhaseArgs pa{g.z.zhi, g.z.zlo, g.z.plain};
+    const uint32_t tiles_a = smem_u32(tiles);
+    const uint32_t mb0 = smem_u32(&mbar[0]);  // mbarrier of stage s at mb0 + 8 s
+
+    if (tid == 0) {
+        aborted = 0;
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb0));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb0 + 8u));
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
+                     "r"(TC_N));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    const uint32_t tmem_d = tmem_slot;
+    const int nkt = g.nkt;
+    const uint32_t idesc = instr_desc();
+    const uint8_t* Bbase = g.Btc + ((size_t)(m * g.nit + it) * nkt) * (2 * TC_TILE_BYTES);
+
+    tc_load_tile<AMODE>(g, tiles, tiles_a, Bbase, w0, 0, m, pa, tid);
+    __syncthreads();
+    for (int kt = 0; kt < nkt; ++kt) {
+        const int s = kt & 1;
+        if (tid == 0 && !aborted) tc_issue(tmem_d, tiles_a + s * TC_STAGE_BYTES, idesc, kt == 0, mb0 + 8u * s);
+        if (kt + 1 < nkt) {
+            // the other stage was read by the MMAs of tile kt-1: wait for them before refilling it
+            if (kt >= 1 && !mbar_wait(mb0 + 8u * (s ^ 1), (uint32_t)(((kt - 1) >> 1) & 1), g.err)) aborted = 1;
+            tc_load_tile<AMODE>(g, tiles + (s ^ 1) * TC_STAGE_BYTES, tiles_a + (s ^ 1) * TC_STAGE_BYTES,
+                                Bbase + (size_t)(kt + 1) * (2 * TC_TILE_BYTES), w0, (kt + 1) * TC_K, m, pa, tid);
+        }
+        __syncthreads();
+        if (aborted) break;
+    }
+    // all MMAs are complete once the last commit has arrived (commits track all earlier MMAs)
+    if (!aborted) {
+        const int kl = nkt - 1;
+        if (!mbar_wait(mb0 + 8u * (kl & 1), (uint32_t)((kl >> 1) & 1), g.err)) aborted = 1;
+    } else {
+        mbar_wait(mb0 + 8u * ((nkt - 1) & 1), (uint32_t)(((nkt - 1) >> 1) & 1), nullptr);
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;\n");
+    __syncthreads();
+
+    // ---- epilogue: TMEM -> registers -> padded staging tile [64][129] complex ----
+    // warps w and w+4 read the same 32 accumulator lanes (lane quarter w % 4), different columns
+    const int quarter = warp & 3;
+    const int row = quarter * 32 + lane;  // accumulator lane = MMA row
+    const int wl = row >> 1;
+    const int part = row & 1;
+#pragma unroll 1
+    for (int c0 = (warp >> 2) * 32; c0 < TC_N; c0 += 64) {
+        uint32_t r[32];
+        const uint32_t taddr = tmem_d + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+            "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+              "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+              "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+              "=r"(r[30]), "=r"(r[31])
+            : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+        float* st = reinterpret_cast<float*>(stage + wl * TC_STAGE_LD + c0) + part;
+#pragma unroll
+        for (int j = 0; j < 32; ++j) st[2 * j] = __uint_as_float(r[j]);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;\n");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_d), "r"(TC_N));
+    if (aborted) return;
+
+    // ---- fused epilogue, coalesced along the output columns ----
+    for (int e = tid; e < TC_W * TC_N; e += TC_THREADS) {
+        const int col = e & (TC_N - 1), wle = e >> 7;
+        const int w = w0 + wle, i = i0 + col;
+        if (w >= g.N0 || i >= g.NI) continue;
+        const float2 v = stage[wle * TC_STAGE_LD + col];
+        const size_t idx = ((size_t)w * g.N1 + i) * g.N2 + m;
+        if (CMODE == TC_STORE) {
+            g.C0[idx] = v;
+        } else if (CMODE == TC_FINISH1) {
+            const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
+            if (g.C0) g.C0[idx] = v;
+            g.C1[idx] = cmul(op_ikz(o), v);
+        } else {
+            const float cond = (w < 4) ? 0.f : 1.f;
+            const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
+            const float2 f = propagator_factor(o, pa, -1.f);
+            const float2 s = cscale(cmul_i(cmul(f, v)), 0.5f / o.kzr);
+            switch (g.spec_mode) {
+                case SPEC_STORE_K:
+                    g.C0[idx] = s;
+                    break;
+                case SPEC_STAGE1: {
+                    const float2 a = g.qi[idx];
+                    g.C1[idx] = cadd(a, cscale(s, g.Cs));
+                    g.C0[idx] = cscale(cadd(a, cscale(s, g.Ce)), cond);
+                } break;
+                case SPEC_STAGE23: {
+                    const float2 a = g.qi[idx];
+                    const float2 b = g.C1[idx];
+                    g.C1[idx] = cadd(b, cscale(s, g.Cs));
+                    g.C0[idx] = cscale(cadd(a, cscale(s, g.Ce)), cond);
+                } break;
+                default: {
+                    const float2 b = g.C1[idx];
+                    g.C0[idx] = cscale(cadd(b, cscale(s, g.Cs)), cond);
+                } break;
+            }
+        }
+    }
+}
+
+static size_t tc_smem_bytes() {
+    const size_t ops = 2 * (size_t)TC_STAGE_BYTES;
+    const size_t stage = (size_t)TC_W * TC_STAGE_LD * sizeof(float2);
+    return (ops > stage ? ops : stage) + 1024;  // + alignment slack
+}
+
+template <int AMODE, int CMODE>
+static cudaError_t run_tc(UppeHandle* h, TcArgs& a) {
+    static bool configured = false;
+    const size_t smem = tc_smem_bytes();
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_hankel_tc<AMODE, CMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    dim3 grid((a.NI + TC_N - 1) / TC_N, (a.N0 + TC_W - 1) / TC_W, a.N2);
+    h->launches++;
+    k_hankel_tc<AMODE, CMODE><<<grid, TC_THREADS, smem, h->stream>>>(a);
+    return cudaGetLastError();
+}
+
+// Entry used by hankel.cu in the mixed-precision form.  amode/cmode follow hankel.cu's A_*/C_* codes;
+// `inverse` selects the split tiles of Minv (else Mfwd).
+cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* A, int inverse, float2* C0,
+                             float2* C1, const float2* qi, int NI, int NK, int spec_mode, float Cs, float Ce,
+                             StepArgs z) {
+    TcArgs a{};
+    a.A = A;
+    a.Btc = inverse ? h->Minv_tc : h->Mfwd_tc;
+    a.nit = (NI + TC_N - 1) / TC_N;
+    a.nkt = (NK + TC_K - 1) / TC_K;
+    a.op = uppe_op_view(h);
+    a.C0 = C0;
+    a.C1 = C1;
+    a.qi = qi;
+    a.N0 = h->N0;
+    a.N1 = h->N1;
+    a.N2 = h->N2;
+    a.NI = NI;
+    a.NK = NK;
+    a.spec_mode = spec_mode;
+    a.Cs = Cs;
+    a.Ce = Ce;
+    a.z = z;
+    a.err = h->dev_err;
+    if (amode == TA_PLAIN && cmode == TC_STORE) return run_tc<TA_PLAIN, TC_STORE>(h, a);
+    if (amode == TA_PLAIN && cmode == TC_SPEC) return run_tc<TA_PLAIN, TC_SPEC>(h, a);
+    if (amode == TA_QPHASE_IKZ && cmode == TC_STORE) return run_tc<TA_QPHASE_IKZ, TC_STORE>(h, a);
+    if (amode == TA_QPHASE && cmode == TC_STORE) return run_tc<TA_QPHASE, TC_STORE>(h, a);
+    if (amode == TA_QPHASE && cmode == TC_FINISH1) return run_tc<TA_QPHASE, TC_FINISH1>(h, a);
+    return cudaErrorInvalidValue;
+}
+
+// Host: round to the nearest bf16 (ties to even) and back, for the split of the matrices.
+static inline uint16_t host_bf16_bits(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) == 0x7f800000u) return (uint16_t)(u >> 16);  // inf / nan
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+static inline float host_bf16_value(uint16_t b) {
+    uint32_t u = (uint32_t)b << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+}
+
+// Split an FP32 matrix B[N2][NI][NK] into bf16 hi/lo tiles in the core-matrix order of the kernel.
+void uppe_split_matrix_tiles(const float* B, int N2, int NI, int NK, std::vector<uint8_t>& out) {
+    const int nit = (NI + TC_N - 1) / TC_N, nkt = (NK + TC_K - 1) / TC_K;
+    out.assign((size_t)N2 * nit * nkt * 2 * TC_TILE_BYTES, 0);
+    for (int m = 0; m < N2; ++m)
+        for (int it = 0; it < nit; ++it)
+            for (int kt = 0; kt < nkt; ++kt) {
+                uint8_t* tile = out.data() + ((size_t)(m * nit + it) * nkt + kt) * 2 * TC_TILE_BYTES;
+                for (int r = 0; r < TC_N; ++r)
+                    for (int kk = 0; kk < TC_K; ++kk) {
+                        const int i = it * TC_N + r, k = kt * TC_K + kk;
+                        const float b = (i < NI && k < NK) ? B[((size_t)m * NI + i) * NK + k] : 0.f;
+                        const uint16_t hb = host_bf16_bits(b);
+                        const uint16_t lb = host_bf16_bits(b - host_bf16_value(hb));
+                        const uint32_t o = (uint32_t)((r >> 3) * 1024 + (kk >> 3) * 128 + (r & 7) * 16 + (kk & 7) * 2);
+                        memcpy(tile + o, &hb, 2);
+                        memcpy(tile + TC_TILE_BYTES + o, &lb, 2);
+                    }
+            }
+}

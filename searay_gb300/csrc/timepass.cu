@@ -61,6 +61,25 @@ __device__ __forceinline__ float soft_window(int i, int Ni, int cut, int wid) {
     return f;
 }
 
+// 1 - exp(-S) for S >= 0: the Taylor series of -expm1(-S) through S^8 (truncation below 1e-11
+// relative) for S < 1/4, where 1 - exp(-S) would cancel, and 1 - expf(-S) above.
+__device__ __forceinline__ float one_minus_exp_neg(float S) {
+    if (S == 0.f) return 0.f;
+    if (S < 0.25f) {
+        const float x = -S;
+        float p = 1.f / 40320.f;
+        p = fmaf(p, x, 1.f / 5040.f);
+        p = fmaf(p, x, 1.f / 720.f);
+        p = fmaf(p, x, 1.f / 120.f);
+        p = fmaf(p, x, 1.f / 24.f);
+        p = fmaf(p, x, 1.f / 6.f);
+        p = fmaf(p, x, 0.5f);
+        p = fmaf(p, x, 1.f);
+        return -x * p;
+    }
+    return 1.f - expf(-S);
+}
+
 __device__ __forceinline__ void acc_add(ffloat& s, float p, int plain) {
     if (plain)
         s.hi += p;
@@ -183,11 +202,11 @@ __global__ void __launch_bounds__(256, 3) k_time(int mode, const float2* __restr
                 const float2 rr = Zj[m * C + c];
                 const int t = 2 * m + 1;
                 if (t <= Nt - 2) acc_add(Sacc, tp.hdt * (rr.y + rn), tp.plain);
-                ne1 = -ngc * expm1f(-ff_value(Sacc));
+                ne1 = ngc * one_minus_exp_neg(ff_value(Sacc));
                 if (t < wlo || t > whi) ne1 *= soft_window(t, Nt, tp.wcut, tp.wwid);
                 acc_add(Sacc, tp.hdt * (rr.x + rr.y), tp.plain);
                 rn = rr.x;
-                ne0 = -ngc * expm1f(-ff_value(Sacc));
+                ne0 = ngc * one_minus_exp_neg(ff_value(Sacc));
                 if (t - 1 < wlo || t - 1 > whi) ne0 *= soft_window(t - 1, Nt, tp.wcut, tp.wwid);
             }
             const float chi1 = kerr * e1 * e1, chi0 = kerr * e0 * e0;
@@ -217,7 +236,10 @@ __global__ void __launch_bounds__(256, 3) k_time(int mode, const float2* __restr
         if (mode == TIME_J) {
             const float wk = wv[k];
             float2 J = cmul_mi(cscale(P, wk));  // -i w P
-            if (ionize) J = cadd(J, cdiv(Q, make_float2(tp.damping, -wk)));
+            if (ionize) {  // Jpl / (damping - i w) = Jpl (damping + i w) / (damping^2 + w^2)
+                const float rden = __frcp_rn(fmaf(wk, wk, tp.damping * tp.damping));
+                J = cadd(J, cscale(cmul(Q, make_float2(tp.damping, wk)), rden));
+            }
             out0[o] = cscale(J, filt[k]);
         } else {
             if (out0) out0[o] = P;

@@ -40,6 +40,7 @@ struct UppeHandle {
     size_t P;                      // N0*N1*N2
     int twLog;                     // twiddle table size 2^twLog
     int time_cols;                 // transverse points per CTA in the time pass
+    int num_sms;                   // multiprocessors of the device
     cudaStream_t stream;
     // library-owned device buffers
     float2 *q, *qi, *qf, *k1, *E, *J, *scratch;
@@ -53,10 +54,13 @@ struct UppeHandle {
     float* nlfilt;   // NL filter per bin
     float* Minv;     // cylindrical: [N2][Nr][Nk]
     float* Mfwd;     // cylindrical: [N2][Nr][Nr] (rows >= Nk zero)
+    uint8_t* Minv_tc; // the same, split into bf16 hi/lo tensor-core tiles (mixed form)
+    uint8_t* Mfwd_tc;
     double* kr2_d;   // [S] transverse eigenvalues (FP64)
     double* w2n2_d;  // [N0] complex w^2 (1 + chi0) interleaved
     double* kg_d;    // [N0]
     float* red;      // reduction scalars: [0] max|q|, [1] min dz, [2] nonfinite flag
+    int* dev_err;    // set by a kernel whose bounded wait expired
     int have_grid, have_material, have_field;
     double max_abs_K;   // max |Re kz + kg| of the current operator
     double max_Ki;      // max Im kz of the current operator

@@ -115,6 +115,15 @@ __device__ __forceinline__ void cp_async8_slice(void* smem_dst, const void* gsrc
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gsrc));
 }
 
+// Ask the memory system to bring `bytes` (a multiple of 16, 16-byte aligned) into L2 ahead of use.
+__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
+    const char* c = (const char*)p;
+    for (size_t off = 0; off < bytes; off += 32768) {
+        const unsigned n = (unsigned)((bytes - off) < 32768 ? (bytes - off) : 32768);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(c + off), "r"(n) : "memory");
+    }
+}
+
 __device__ __forceinline__ void slice_load_async(float2* sm, const float2* __restrict__ src, int S, int logN2, int tid,
                                                  int nthr) {
     for (int e = tid; e < S; e += nthr) cp_async8_slice(&sm[slice_pad(e, logN2)], &src[e]);
@@ -254,12 +263,21 @@ __global__ void __launch_bounds__(1024) k_fused_cart(int mode, const float2* __r
                                                      float2* __restrict__ qi_out, float2* __restrict__ qf,
                                                      const float2* __restrict__ qi, float2* __restrict__ E, float Cs,
                                                      float Ce, int logN1, int logN2, const float2* __restrict__ tw,
-                                                     int twLog, StepArgs z_rhs, StepArgs z_next) {
+                                                     int twLog, StepArgs z_rhs, StepArgs z_next, int next_wave) {
     extern __shared__ float2 sm[];
     const int S = 1 << (logN1 + logN2);
     const int iw = blockIdx.x;
     const size_t base = (size_t)iw * S;
     const int tid = threadIdx.x, nthr = blockDim.x;
+    if (tid == 0) {
+        // operator and RK state of this slice are read after the forward FFT: fetch them into L2 now;
+        // also the current of the slice a CTA of the next wave will take
+        const size_t fb = (size_t)S * sizeof(float2);
+        prefetch_l2(opv.K + base, fb);
+        if (mode != SPEC_FINISH) prefetch_l2(qi + base, fb);
+        if (mode != SPEC_STAGE1) prefetch_l2(qf + base, fb);
+        if ((int)(iw + next_wave) < (int)gridDim.x) prefetch_l2(J + base + (size_t)next_wave * S, fb);
+    }
     slice_load_async(sm, J + base, S, logN2, tid, nthr);
     slice_forward(sm, logN1, logN2, tw, twLog, tid, nthr);
     const PhaseArgs pr{z_rhs.zhi, z_rhs.zlo, z_rhs.plain};
@@ -327,7 +345,7 @@ cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepA
     h->launches++;
     k_fused_cart<<<h->N0, slice_threads(h), slice_smem(h), h->stream>>>(mode, h->J, uppe_op_view(h), h->qi, h->qf,
                                                                          h->qi, h->E, Cs, Ce, logN1, logN2, h->tw,
-                                                                         h->twLog, z_rhs, z_next);
+                                                                         h->twLog, z_rhs, z_next, h->num_sms);
     return cudaGetLastError();
 }
 
