@@ -114,6 +114,30 @@ int uppe_get_field(UppeHandle* h, void* q_out);
 /* Set *nonfinite to 1 if the current q holds NaN or Inf (the '!' check of uppe_kernel.py:219-220). */
 int uppe_check_finite(UppeHandle* h, int* nonfinite);
 
+/* ---- adjoint (vector-Jacobian products), for gradients through torch.autograd ----
+ * The reference has no adjoint; these entry points give the transposed linearisation of the maps
+ * above so that gradients of a loss on the outputs reach the incoming field and chi3 (n2).
+ * Cotangents are complex64 device arrays [N0][N1][N2] in the real-pair convention
+ * g = dL/dRe + i dL/dIm.  Cylindrical grids need one azimuthal node. */
+
+/* Replace chi3 / density reference (the Kerr coefficient, uppe_kernel.py:52) used from now on. */
+int uppe_set_chi3(UppeHandle* h, double chi3_over_nref);
+
+/* Set the spectral amplitude q directly (a checkpoint restart), device complex64 [N0][N1][N2]. */
+int uppe_set_field(UppeHandle* h, const void* q);
+
+/* VJP of one fixed RK4 step q0 -> q1 at z_phase with step dz (the body of uppe_kernel.py:305-325
+ * with dz fixed): lam_in = (dq1/dq0)^H lam_out.  Recomputes the stage estimates from q0.  Adds
+ * d(loss)/d(chi3/nref) of this step to *dred (may be NULL).  Overwrites the handle's q. */
+int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0, const void* lam_out, void* lam_in, double z_phase,
+                          double dz, double* dred);
+
+/* VJP of uppe_load_field (q = T a): lam_a = T^H lam_q. */
+int uppe_adjoint_load(UppeHandle* h, const void* lam_q, void* lam_a);
+
+/* VJP of the field output of uppe_finish (A = T^-1 exp(i(kz+kg)z) q): lam_q from lam_A. */
+int uppe_adjoint_finish(UppeHandle* h, double z_phase, const void* lam_A, void* lam_q);
+
 /* Timing classes of the kernels, for uppe_profile_read. */
 #define UPPE_NCLASS 6
 #define UPPE_CLASS_OPERATOR 0   /* kz build (UpdateMaterial) */

@@ -110,7 +110,9 @@ static StepArgs split_z(const UppeHandle* h, double z) {
 
 static void free_buffers(UppeHandle* h) {
     void* ptrs[] = {h->q,  h->qi,   h->qf,   h->k1,   h->E,     h->J,      h->scratch, h->opK,  h->opKi, h->kg2,
-                    h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red, h->dev_err, h->Minv_tc, h->Mfwd_tc};
+                    h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red, h->dev_err, h->Minv_tc, h->Mfwd_tc,
+                    h->adj_q1, h->adj_q2, h->adj_q3, h->adj_lf, h->adj_acc, h->adj_lk, h->adj_mu, h->MfwdT, h->MinvT,
+                    h->dred_d};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -172,6 +174,7 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (tc > 16) tc = 16;
     if (tc > h->S) tc = h->S;
     h->time_cols = tc;
+    h->redchi3 = c.chi3_over_nref;
     int nt = Nt;
     if (c.n1 > nt) nt = c.n1;
     if (c.n2 > nt) nt = c.n2;
@@ -231,6 +234,7 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     // launch still requests only what its grid needs.
     if (e == cudaSuccess) e = uppe_configure_slice_kernels(227 * 1024);
     if (e == cudaSuccess) e = uppe_configure_time_kernel(227 * 1024);
+    if (e == cudaSuccess) e = uppe_configure_time_adj_kernel(224 * 1024);  // leaves room for its static shared memory
     if (e != cudaSuccess) {
         uppe_set_error(nullptr, "device set-up failed: %s", cudaGetErrorString(e));
         free_buffers(h);
@@ -292,6 +296,19 @@ extern "C" int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, 
                 }
         CUDA_TRY(h, cudaMemcpy(h->Minv, Minv.data(), Minv.size() * sizeof(float), cudaMemcpyHostToDevice));
         CUDA_TRY(h, cudaMemcpy(h->Mfwd, Mfwd.data(), Mfwd.size() * sizeof(float), cudaMemcpyHostToDevice));
+        // transposed matrices for the adjoint transforms (one azimuthal node)
+        if (Nm == 1) {
+            std::vector<float> MfT((size_t)Nr * Nr, 0.f), MiT((size_t)Nr * Nr, 0.f);
+            for (int r = 0; r < Nr; ++r)
+                for (int k = 0; k < Nr; ++k) {
+                    MfT[(size_t)r * Nr + k] = Mfwd[(size_t)k * Nr + r];
+                    if (k < Nk) MiT[(size_t)k * Nr + r] = Minv[(size_t)r * Nk + k];
+                }
+            if (!h->MfwdT) CUDA_TRY(h, cudaMalloc((void**)&h->MfwdT, MfT.size() * sizeof(float)));
+            if (!h->MinvT) CUDA_TRY(h, cudaMalloc((void**)&h->MinvT, MiT.size() * sizeof(float)));
+            CUDA_TRY(h, cudaMemcpy(h->MfwdT, MfT.data(), MfT.size() * sizeof(float), cudaMemcpyHostToDevice));
+            CUDA_TRY(h, cudaMemcpy(h->MinvT, MiT.data(), MiT.size() * sizeof(float), cudaMemcpyHostToDevice));
+        }
         if (c.precision == UPPE_PREC_MIXED) {
             std::vector<uint8_t> t;
             uppe_split_matrix_tiles(Minv.data(), Nm, Nr, Nk, t);
@@ -576,6 +593,120 @@ extern "C" int uppe_check_finite(UppeHandle* h, int* nonfinite) {
         uppe_set_error(h, "a tensor-core kernel's bounded wait expired; results of this handle are invalid");
         return UPPE_E_CUDA;
     }
+    return UPPE_OK;
+}
+
+// =============================================================================================
+// Adjoint: vector-Jacobian products of the fixed-step RK4 map, of the load transform and of the
+// finish transform, for gradients through torch.autograd.
+// =============================================================================================
+extern "C" int uppe_set_chi3(UppeHandle* h, double chi3_over_nref) {
+    if (!h) return UPPE_E_ARG;
+    h->redchi3 = chi3_over_nref;
+    return UPPE_OK;
+}
+
+extern "C" int uppe_set_field(UppeHandle* h, const void* q) {
+    if (!h || !q) return UPPE_E_ARG;
+    if (!h->have_grid) {
+        uppe_set_error(h, "uppe_set_field before uppe_set_grid");
+        return UPPE_E_ARG;
+    }
+    CUDA_TRY(h, cudaMemcpyAsync(h->qi, q, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
+    h->have_field = 1;
+    h->E_valid = 0;
+    return UPPE_OK;
+}
+
+static int ensure_adjoint(UppeHandle* h) {
+    if (h->cfg.cylindrical && h->N2 != 1) {
+        uppe_set_error(h, "the adjoint supports cylindrical grids with one azimuthal node only");
+        return UPPE_E_ARG;
+    }
+    if (h->adj_mu) return UPPE_OK;
+    const size_t fb = h->P * sizeof(float2);
+    float2** bufs[] = {&h->adj_q1, &h->adj_q2, &h->adj_q3, &h->adj_lf, &h->adj_acc, &h->adj_lk, &h->adj_mu};
+    for (float2** b : bufs) CUDA_TRY(h, cudaMalloc((void**)b, fb));
+    CUDA_TRY(h, cudaMalloc((void**)&h->dred_d, sizeof(double)));
+    return UPPE_OK;
+}
+
+static cudaError_t adj_pass(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z) {
+    return h->cfg.cylindrical ? launch_adj_cyl(h, mode, in, out, z) : launch_adj_cart(h, mode, in, out, z);
+}
+
+// mu = S'(qs)^H lamk at z = zs (the right-hand side of load_source, uppe_kernel.py:188-216)
+static int vjp_rhs(UppeHandle* h, const float2* qs, double zs, const float2* lamk, float2* mu) {
+    const StepArgs z = split_z(h, zs);
+    h->E_valid = 0;
+    PROF_TRY(h, UPPE_CLASS_OTHER, real_pass(h, REAL_E, qs, nullptr, z));
+    PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_S, lamk, h->J, z));
+    PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_adjoint(h, h->E, h->J, h->k1, h->dred_d));
+    PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_E, h->k1, mu, z));
+    return UPPE_OK;
+}
+
+extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void* lam_out, void* lam_in, double z_phase,
+                                     double dz, double* dred_out) {
+    if (!h || !q0v || !lam_out || !lam_in) return UPPE_E_ARG;
+    int rc = check_ready(h, false);
+    if (rc) return rc;
+    rc = ensure_adjoint(h);
+    if (rc) return rc;
+    rc = check_range(h, z_phase + dz);
+    if (rc) return rc;
+    const float2* q0 = (const float2*)q0v;
+    CUDA_TRY(h, cudaMemsetAsync(h->dred_d, 0, sizeof(double), h->stream));
+    // recompute the stage estimates q1', q2', q3' of the forward step (uppe_kernel.py:305-322)
+    CUDA_TRY(h, cudaMemcpyAsync(h->qi, q0, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
+    h->E_valid = 0;
+    {
+        const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz);
+        CUDA_TRY(h, eval_to_J(h, h->qi, z0));
+        PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE1, h->J, h->q, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z0));
+        CUDA_TRY(h, cudaMemcpyAsync(h->adj_q1, h->q, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
+        CUDA_TRY(h, eval_to_J(h, h->q, zh));
+        PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), zh));
+        CUDA_TRY(h, cudaMemcpyAsync(h->adj_q2, h->q, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
+        CUDA_TRY(h, eval_to_J(h, h->q, zh));
+        PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)dz, zh));
+        CUDA_TRY(h, cudaMemcpyAsync(h->adj_q3, h->q, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
+    }
+    // reverse sweep through the four stages
+    CUDA_TRY(h, launch_adj_rk(h, 0, (const float2*)lam_out, nullptr, (float)(dz / 6), 0.f));
+    if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu))) return rc;
+    CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)dz));
+    if ((rc = vjp_rhs(h, h->adj_q2, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu))) return rc;
+    CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)(dz / 2)));
+    if ((rc = vjp_rhs(h, h->adj_q1, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu))) return rc;
+    CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 6), (float)(dz / 2)));
+    if ((rc = vjp_rhs(h, q0, z_phase, h->adj_lk, h->adj_mu))) return rc;
+    CUDA_TRY(h, launch_adj_rk(h, 2, nullptr, (float2*)lam_in, 0.f, 0.f));
+    if (dred_out) {
+        double d = 0.0;
+        CUDA_TRY(h, cudaMemcpyAsync(&d, h->dred_d, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        *dred_out += d;
+    }
+    return UPPE_OK;
+}
+
+extern "C" int uppe_adjoint_load(UppeHandle* h, const void* lam_q, void* lam_a) {
+    if (!h || !lam_q || !lam_a) return UPPE_E_ARG;
+    if (!h->have_grid) return UPPE_E_ARG;
+    int rc = ensure_adjoint(h);
+    if (rc) return rc;
+    CUDA_TRY(h, adj_pass(h, ADJ_LOAD, (const float2*)lam_q, (float2*)lam_a, split_z(h, 0.0)));
+    return UPPE_OK;
+}
+
+extern "C" int uppe_adjoint_finish(UppeHandle* h, double z_phase, const void* lam_A, void* lam_q) {
+    if (!h || !lam_A || !lam_q) return UPPE_E_ARG;
+    int rc = check_ready(h, false);
+    if (rc) return rc;
+    rc = ensure_adjoint(h);
+    if (rc) return rc;
+    CUDA_TRY(h, adj_pass(h, ADJ_FIN, (const float2*)lam_A, (float2*)lam_q, split_z(h, z_phase)));
     return UPPE_OK;
 }
 

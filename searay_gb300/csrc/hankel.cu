@@ -15,8 +15,8 @@
 #define GBN 64
 #define GBK 16
 
-enum { A_PLAIN = 0, A_QPHASE_IKZ = 1, A_QPHASE = 2 };
-enum { C_STORE = 0, C_FINISH1 = 1, C_SPEC = 2 };
+enum { A_PLAIN = 0, A_QPHASE_IKZ = 1, A_QPHASE = 2, A_SADJ = 3 };
+enum { C_STORE = 0, C_FINISH1 = 1, C_SPEC = 2, C_QADJ = 3, C_FADJ = 4 };
 
 struct GemmArgs {
     const float2* A;  // operand source ([w][r|k][m] layout, row length N1, N2 azimuthal nodes)
@@ -54,7 +54,12 @@ __global__ void __launch_bounds__(256) k_hankel_gemm(GemmArgs g) {
             if (w < g.N0 && k < g.NK) {
                 const size_t idx = ((size_t)w * g.N1 + k) * g.N2 + m;
                 v = g.A[idx];
-                if (AMODE != A_PLAIN) {
+                if (AMODE == A_SADJ) {
+                    // conj(D2) v, D2 = (i/2) exp(-i(kz+kg)z) / Re kz
+                    const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
+                    const float2 f = cconj(propagator_factor(o, pa, -1.f));
+                    v = cscale(cmul_mi(cmul(f, v)), 0.5f / o.kzr);
+                } else if (AMODE != A_PLAIN) {
                     const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
                     v = cmul(propagator_factor(o, pa, 1.f), v);
                     if (AMODE == A_QPHASE_IKZ) v = cmul(op_ikz(o), v);
@@ -96,6 +101,11 @@ __global__ void __launch_bounds__(256) k_hankel_gemm(GemmArgs g) {
             const float2 v = acc[r][j];
             if (CMODE == C_STORE) {
                 g.C0[idx] = v;
+            } else if (CMODE == C_QADJ || CMODE == C_FADJ) {
+                const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
+                float2 r = cmul(cconj(propagator_factor(o, pa, 1.f)), v);
+                if (CMODE == C_QADJ) r = cmul(cconj(op_ikz(o)), r);
+                g.C0[idx] = r;
             } else if (CMODE == C_FINISH1) {
                 const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
                 if (g.C0) g.C0[idx] = v;
@@ -240,4 +250,36 @@ cudaError_t launch_spec_cyl(UppeHandle* h, int mode, const float2* src_real, flo
     g.spec_mode = mode;
     if (mode == SPEC_LOAD) return run_gemm<A_PLAIN, C_STORE>(h, g);
     return run_gemm<A_PLAIN, C_SPEC>(h, g);
+}
+
+// Adjoint transverse transforms on cylindrical grids (one azimuthal node), FP32 SIMT GEMMs with the
+// transposed folded matrices: ADJ_S / ADJ_LOAD apply Mfwd^T, ADJ_E / ADJ_FIN apply Minv^T.
+template <int AMODE, int CMODE>
+static cudaError_t run_gemm_simt(UppeHandle* h, GemmArgs& g) {
+    dim3 grid((g.NI + GBN - 1) / GBN, (g.N0 + GBM - 1) / GBM, g.N2);
+    h->launches++;
+    k_hankel_gemm<AMODE, CMODE><<<grid, 256, 0, h->stream>>>(g);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adj_cyl(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z) {
+    GemmArgs g = base_args(h, z);
+    g.A = in;
+    g.C0 = out;
+    g.NI = h->N1;
+    g.NK = h->N1;
+    switch (mode) {
+        case ADJ_S:
+            g.B = h->MfwdT;
+            return run_gemm_simt<A_SADJ, C_STORE>(h, g);
+        case ADJ_LOAD:
+            g.B = h->MfwdT;
+            return run_gemm_simt<A_PLAIN, C_STORE>(h, g);
+        case ADJ_E:
+            g.B = h->MinvT;
+            return run_gemm_simt<A_PLAIN, C_QADJ>(h, g);
+        default:
+            g.B = h->MinvT;
+            return run_gemm_simt<A_PLAIN, C_FADJ>(h, g);
+    }
 }

@@ -252,7 +252,7 @@ cudaError_t uppe_configure_time_kernel(size_t smem_bytes) {
     return cudaFuncSetAttribute(k_time, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
 }
 
-cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1) {
+static TimeParams make_time_params(const UppeHandle* h) {
     const UppeConfig& c = h->cfg;
     TimeParams tp;
     tp.Nt = h->Nt;
@@ -266,7 +266,7 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
     tp.spt = h->Nt * h->time_cols / T;
     tp.inv_nt = (float)(1.0 / (double)h->Nt);
     tp.hdt = (float)(0.5 * c.dt);
-    tp.redchi3 = (float)c.chi3_over_nref;
+    tp.redchi3 = (float)h->redchi3;
     tp.damping = (float)c.damping;
     tp.rate_form = c.rate_form;
     tp.fconv = (float)c.field_conv;
@@ -280,9 +280,255 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
     tp.wcut = c.window_cutoff;
     tp.wwid = c.window_width;
     tp.plain = (c.precision == UPPE_PREC_FP32);
+    return tp;
+}
+
+cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1) {
+    const TimeParams tp = make_time_params(h);
+    const int T = h->Nt * h->time_cols / 32;
     const size_t smem = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
     h->launches++;
     k_time<<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw, h->twLog,
                                                          tp);
+    return cudaGetLastError();
+}
+
+// =============================================================================================
+// Adjoint of the time pass (vector-Jacobian product of J(E) for one evaluation).
+//
+// Given the forward input E(w) and the cotangent G(w) of the current J(w) (after the transposed
+// forward transverse transform and conj of the RHS factor), writes the cotangent gE(w) of E(w):
+//   P(w)   = rfft(p),  p = kappa e^3         J = filt (-i w P + Ppl / (0.1 - i w)),  Ppl = rfft(ne e)
+//   gp(t)  = Re sum_k Gp_k e^{2 pi i k t/Nt},  Gp = conj(filt (-i w)) G   (transpose of rfft)
+//   gpl(t) = Re sum_k Gl_k e^{2 pi i k t/Nt},  Gl = conj(filt / (0.1 - i w)) G
+//   ge(t)  = 3 kappa e^2 gp + ne gpl + dr/de(t) hdt (Pfx(t) + Pfx(t-1)),
+//            Pfx(j) = sum_{t <= j} gpl(t) e(t) ng w(t) exp(-S(t))   (transpose of the reverse scan)
+//   gE(w)  = (1/Nt) W2 rfft(ge),  W2 = 1 at w = 0 and the last bin, 2 elsewhere   (transpose of irfft)
+// and adds sum gp ng e^3 (the derivative with respect to chi3/nref) to *dred.
+// =============================================================================================
+__device__ __forceinline__ float ion_rate_deriv(const TimeParams& tp, float e, float r) {
+    // d rate / d e = rate * d(log rate)/d(Em) * fconv * sign(e)
+    const float em = fmaf(tp.fconv, fabsf(e), tp.cutoff);
+    const float inv = __frcp_rn(em);
+    float dl;
+    if (tp.rate_form == UPPE_RATE_EXPLICIT) {
+        // d/dEm [C_pow ln Em + C_exp / Em] = (C_pow - C_exp / Em) / Em, C_exp = ln2 * yexp
+        dl = (tp.ypow - UPPE_LN2 * tp.yexp * inv) * inv;
+    } else {
+        const float L = __log2f(em) * UPPE_LN2;
+        float dp = 5.f * tp.c2[5];
+        dp = fmaf(dp, L, 4.f * tp.c2[4]);
+        dp = fmaf(dp, L, 3.f * tp.c2[3]);
+        dp = fmaf(dp, L, 2.f * tp.c2[2]);
+        dp = fmaf(dp, L, tp.c2[1]);
+        dl = dp * UPPE_LN2 * inv;
+    }
+    const float sg = (e > 0.f) ? 1.f : ((e < 0.f) ? -1.f : 0.f);
+    return r * dl * tp.fconv * sg;
+}
+
+// even/odd packing of a half spectrum X(k) = f(k) into z for the M-point inverse FFT
+template <class F>
+__device__ __forceinline__ void pack_half_spectrum(float2* Z, int C, int logC, int M, const TwHalfShared& tws, F X,
+                                                   int tid, int T) {
+    const int npairs = (M / 2 + 1) * C;
+    for (int it = tid; it < npairs; it += T) {
+        const int c = it & (C - 1);
+        const int k = it >> logC;
+        float2 Xa = X(k, c), Xm = X(M - k, c);
+        if (k == 0) {
+            Xa.y = 0.f;
+            Xm.y = 0.f;
+        }
+        const float2 t = cconj(tws.get(k));
+        const float2 b = cconj(Xm);
+        Z[k * C + c] = cadd(cadd(Xa, b), cmul_i(cmul(t, csub(Xa, b))));
+        if (k != 0 && 2 * k != M) {
+            const float2 t2 = make_float2(-t.x, t.y);
+            const float2 b2 = cconj(Xa);
+            Z[(M - k) * C + c] = cadd(cadd(Xm, b2), cmul_i(cmul(t2, csub(Xm, b2))));
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_time_adj(const float2* __restrict__ E, const float2* __restrict__ G,
+                                                  float2* __restrict__ gE, const float* __restrict__ ng,
+                                                  const float* __restrict__ wv, const float* __restrict__ filt,
+                                                  const float2* __restrict__ tw, int twLog, TimeParams tp,
+                                                  double* dred) {
+    extern __shared__ float2 sa[];
+    const int C = tp.C, logC = tp.logC, Nt = tp.Nt, M = tp.M, S = tp.S;
+    const int R = (M + 1) * C;
+    float2* Ze = sa;           // e pairs, then ge pairs
+    float2* Zn = sa + R;       // raw E / rates / ne pairs
+    float2* Za = sa + 2 * R;   // raw G / ng w exp(-S) pairs
+    float2* Zp = sa + 3 * R;   // gp pairs
+    float2* Zl = sa + 4 * R;   // gpl pairs
+    float2* twl = sa + 5 * R;
+    ffloat* tot = reinterpret_cast<ffloat*>(twl + (Nt >> 1));
+    __shared__ double red_sh[8];
+    const int tid = threadIdx.x, T = blockDim.x;
+    const size_t col0 = (size_t)blockIdx.x * C;
+    const bool ionize = tp.rate_form != UPPE_RATE_NONE;
+    const TwHalfShared tws{twl, tp.logNt};
+
+    // ---- 1. stage E and G, recompute e(t), form the transposed-rfft inputs ----
+    for (int it = tid; it < R; it += T) {
+        const int c = it & (C - 1);
+        const int k = it >> logC;
+        cp_async8(&Zn[it], &E[(size_t)k * S + col0 + c]);
+        cp_async8(&Za[it], &G[(size_t)k * S + col0 + c]);
+    }
+    asm volatile("cp.async.commit_group;\n" ::);
+    for (int j = tid; j < (Nt >> 1); j += T) twl[j] = __ldg(&tw[j << (twLog - tp.logNt)]);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+    __syncthreads();
+    pack_half_spectrum(Ze, C, logC, M, tws, [&](int k, int c) { return Zn[k * C + c]; }, tid, T);
+    // Gp_k = W_k filt_k (i w_k) G_k ; Gl_k = W_k filt_k G_k / (0.1 + i w_k), W = 1/2 inside the band
+    pack_half_spectrum(Zp, C, logC, M, tws, [&](int k, int c) {
+        const float wk = wv[k];
+        const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
+        return cscale(cmul_i(Za[k * C + c]), wk * wt * filt[k]);
+    }, tid, T);
+    if (ionize)
+        pack_half_spectrum(Zl, C, logC, M, tws, [&](int k, int c) {
+            const float wk = wv[k];
+            const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
+            const float rden = __frcp_rn(fmaf(wk, wk, tp.damping * tp.damping));
+            return cscale(cmul(Za[k * C + c], make_float2(tp.damping, -wk)), rden * wt * filt[k]);
+        }, tid, T);
+    __syncthreads();
+    fft_axis_tw<16>(Ze, tp.logM, logC, 1, C, tws, true, tid, T);
+    fft_axis_tw<16>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
+    if (ionize) fft_axis_tw<16>(Zl, tp.logM, logC, 1, C, tws, true, tid, T);
+
+    // ---- 2. forward sources along t (ne and ng w exp(-S)), as in k_time ----
+    const int c = tid & (C - 1);
+    const int seg = tid >> logC;
+    const int mps = tp.spt >> 1;
+    const int m0 = seg * mps;
+    const int t1 = 2 * (m0 + mps);
+    const float ngc = ng[col0 + c];
+    const float kerr = ngc * tp.redchi3;
+    const float inv = tp.inv_nt;
+    const int nseg = T >> logC;
+    if (ionize) {
+        float r_next = 0.f;
+        if (t1 <= Nt - 2) r_next = ion_rate(tp, Ze[(t1 >> 1) * C + c].x * inv);
+        ffloat part = {0.f, 0.f};
+        float rn = r_next;
+        for (int m = m0 + mps - 1; m >= m0; --m) {
+            const float2 zv = Ze[m * C + c];
+            const int t = 2 * m + 1;
+            const float r1 = (t == Nt - 1) ? 0.f : ion_rate(tp, zv.y * inv);
+            if (t <= Nt - 2) acc_add(part, tp.hdt * (r1 + rn), tp.plain);
+            const float r0 = ion_rate(tp, zv.x * inv);
+            acc_add(part, tp.hdt * (r0 + r1), tp.plain);
+            rn = r0;
+            Zn[m * C + c] = make_float2(r0, r1);
+        }
+        tot[tid] = part;
+        __syncthreads();
+        ffloat Sacc = {0.f, 0.f};
+        for (int s2 = seg + 1; s2 < nseg; ++s2) Sacc = ff_add(Sacc, tot[(s2 << logC) + c]);
+        rn = r_next;
+        for (int m = m0 + mps - 1; m >= m0; --m) {
+            const float2 rr = Zn[m * C + c];
+            const int t = 2 * m + 1;
+            if (t <= Nt - 2) acc_add(Sacc, tp.hdt * (rr.y + rn), tp.plain);
+            const float w1 = soft_window(t, Nt, tp.wcut, tp.wwid);
+            const float S1 = ff_value(Sacc);
+            acc_add(Sacc, tp.hdt * (rr.x + rr.y), tp.plain);
+            rn = rr.x;
+            const float w0 = soft_window(t - 1, Nt, tp.wcut, tp.wwid);
+            const float S0 = ff_value(Sacc);
+            Zn[m * C + c] = make_float2(ngc * one_minus_exp_neg(S0) * w0, ngc * one_minus_exp_neg(S1) * w1);
+            Za[m * C + c] = make_float2(ngc * w0 * expf(-S0), ngc * w1 * expf(-S1));
+        }
+        __syncthreads();  // segment totals are reused below
+    }
+
+    // ---- 3. transposed scan: Pfx(j) = sum_{t <= j} gpl e a, two passes in increasing t ----
+    ffloat carry = {0.f, 0.f};
+    if (ionize) {
+        ffloat part = {0.f, 0.f};
+        for (int m = m0; m < m0 + mps; ++m) {
+            const float2 e2 = Ze[m * C + c], l2 = Zl[m * C + c], a2 = Za[m * C + c];
+            acc_add(part, l2.x * e2.x * inv * a2.x, tp.plain);
+            acc_add(part, l2.y * e2.y * inv * a2.y, tp.plain);
+        }
+        tot[tid] = part;
+        __syncthreads();
+        for (int s2 = 0; s2 < seg; ++s2) carry = ff_add(carry, tot[(s2 << logC) + c]);
+    }
+    // ---- 4. pointwise cotangent of e(t), written over the e pairs ----
+    float dred_part = 0.f;
+    {
+        ffloat Pprev = carry;  // Pfx(t - 1)
+        for (int m = m0; m < m0 + mps; ++m) {
+            const float2 e2 = Ze[m * C + c];
+            const float2 p2 = Zp[m * C + c];
+            float ge[2];
+            const float ev[2] = {e2.x * inv, e2.y * inv};
+            const float gp[2] = {p2.x, p2.y};
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int t = 2 * m + h;
+                const float e = ev[h];
+                float g = 3.f * kerr * e * e * gp[h];
+                dred_part = fmaf(gp[h] * ngc * e * e, e, dred_part);
+                if (ionize) {
+                    const float2 l2 = Zl[m * C + c], n2 = Zn[m * C + c], a2 = Za[m * C + c];
+                    const float gl = h ? l2.y : l2.x;
+                    const float ne = h ? n2.y : n2.x;
+                    const float a = h ? a2.y : a2.x;
+                    g = fmaf(ne, gl, g);
+                    ffloat P = Pprev;
+                    acc_add(P, gl * e * a, tp.plain);
+                    if (t <= Nt - 2) {
+                        const float r = ion_rate(tp, e);
+                        const float gr = tp.hdt * (ff_value(P) + ff_value(Pprev));
+                        g = fmaf(gr, ion_rate_deriv(tp, e, r), g);
+                    }
+                    Pprev = P;
+                }
+                ge[h] = g;
+            }
+            Ze[m * C + c] = make_float2(ge[0], ge[1]);
+        }
+    }
+    // block reduction of the chi3 derivative
+    double dsum = (double)dred_part;
+    for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+    if ((tid & 31) == 0) red_sh[tid >> 5] = dsum;
+    __syncthreads();
+    if (tid == 0) {
+        double b = 0.0;
+        for (int i = 0; i < (T >> 5); ++i) b += red_sh[i];
+        atomicAdd(dred, b);
+    }
+
+    // ---- 5. transpose of irfft: gE = (1/Nt) W2 rfft(ge) ----
+    fft_axis_tw<16>(Ze, tp.logM, logC, 1, C, tws, false, tid, T);
+    for (int it = tid; it < (M + 1) * C; it += T) {
+        const int cc = it & (C - 1);
+        const int k = it >> logC;
+        const int ka = k & (M - 1), kb = (M - k) & (M - 1);
+        const float2 X = real_spectrum(Ze[ka * C + cc], Ze[kb * C + cc], tws.get(k));
+        const float wt = (k == 0 || k == M) ? inv : 2.f * inv;
+        gE[(size_t)k * S + col0 + cc] = cscale(X, wt);
+    }
+}
+
+cudaError_t uppe_configure_time_adj_kernel(size_t smem_bytes) {
+    return cudaFuncSetAttribute(k_time_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+}
+
+cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G, float2* gE, double* dred) {
+    const TimeParams tp = make_time_params(h);
+    const int T = h->Nt * h->time_cols / 32;
+    const size_t smem = ((size_t)(h->M + 1) * 5 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
+    h->launches++;
+    k_time_adj<<<h->S / h->time_cols, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred);
     return cudaGetLastError();
 }

@@ -24,6 +24,13 @@ enum UppeRealMode {
 };
 
 // Modes of the time-axis pass.
+enum UppeAdjMode {
+    ADJ_S = 0,     // cotangent of S -> cotangent of J (before the forward transverse transform)
+    ADJ_LOAD = 1,  // transpose of the load transform
+    ADJ_E = 2,     // cotangent of E -> cotangent of q
+    ADJ_FIN = 3,   // cotangent of the finish A -> cotangent of q
+};
+
 enum UppeTimeMode {
     TIME_J = 0,       // J(w) from E(w): Kerr + plasma current, NL filter
     TIME_CHI_NE = 1,  // rfft of chi(t) and ne(t) (diagnostic outputs of finish)
@@ -64,6 +71,12 @@ struct UppeHandle {
     int have_grid, have_material, have_field;
     double max_abs_K;   // max |Re kz + kg| of the current operator
     double max_Ki;      // max Im kz of the current operator
+    double redchi3;        // chi3 / density reference in use (uppe_set_chi3)
+    // adjoint work buffers (allocated by the first adjoint call)
+    float2 *adj_q1, *adj_q2, *adj_q3, *adj_lf, *adj_acc, *adj_lk, *adj_mu;
+    float* MfwdT;          // cylindrical adjoint: [Nr][Nr], MfwdT[r][k] = Mfwd[k][r]
+    float* MinvT;          // [Nr][Nr], MinvT[k][r] = Minv[r][k] for k < Nk, 0 beyond
+    double* dred_d;        // device accumulator of d(loss)/d(chi3/nref)
     long long mat_version; // incremented by every uppe_set_material
     int E_valid;           // E holds T^-1(i kz e^{..} qi) for (E_z, E_mat): reusable by the next step
     double E_z;
@@ -96,6 +109,12 @@ cudaError_t launch_absmax(UppeHandle* h, const float2* q);
 cudaError_t launch_step_size(UppeHandle* h, const float2* q, const float2* k, double L, double dphi, double rel_amin);
 cudaError_t launch_apply_stage1(UppeHandle* h, float Cs, float Ce);
 cudaError_t launch_ikz(UppeHandle* h, const float2* A, float2* E);
+
+cudaError_t launch_adj_cart(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z);
+cudaError_t launch_adj_rk(UppeHandle* h, int mode, const float2* lam_out, float2* lam_in, float a_f, float a_mu);
+cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G, float2* gE, double* dred);
+cudaError_t uppe_configure_time_adj_kernel(size_t smem_bytes);
+cudaError_t launch_adj_cyl(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z);
 
 // ---- cylindrical transverse transform (hankel.cu) ----
 cudaError_t launch_real_cyl(UppeHandle* h, int mode, const float2* src, float2* A_out, StepArgs z);

@@ -91,6 +91,11 @@ cudaError_t launch_operator_bounds(UppeHandle* h) {
     return cudaGetLastError();
 }
 
+static unsigned reduce_blocks_host(size_t n) {
+    size_t b = (n + 255) / 256;
+    return (unsigned)(b < 152 * 8 ? b : 152 * 8);
+}
+
 OpView uppe_op_view(const UppeHandle* h) {
     OpView v;
     v.K = h->opK;
@@ -300,6 +305,87 @@ __global__ void __launch_bounds__(1024) k_fused_cart(int mode, const float2* __r
     for (int e = tid; e < S; e += nthr) E[base + e] = cscale(sm[slice_pad(e, logN2)], scale);
 }
 
+// ---- adjoint (vector-Jacobian products) of the Cartesian slice passes ----
+// ADJ_S:    out = F^H( conj(D2) in ),  D2 = (i/2) exp(-i(kz+kg)z) / Re kz   (cotangent of the RHS
+//           S -> cotangent of the current J before the forward transform; F^H = unnormalised inverse FFT)
+// ADJ_LOAD: out = F^H in                                                     (transpose of the load kspacex)
+// ADJ_E:    out = conj(D0) (1/N) F in,  D0 = i kz exp(i(kz+kg)z)           (cotangent of E -> of q)
+// ADJ_FIN:  out = conj(exp(i(kz+kg)z)) (1/N) F in                           (cotangent of the finish A -> of q)
+__global__ void __launch_bounds__(1024) k_adj_cart(int mode, const float2* __restrict__ in, OpView opv,
+                                                   float2* __restrict__ out, int logN1, int logN2,
+                                                   const float2* __restrict__ tw, int twLog, StepArgs z) {
+    extern __shared__ float2 sm[];
+    const int S = 1 << (logN1 + logN2);
+    const int iw = blockIdx.x;
+    const size_t base = (size_t)iw * S;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const PhaseArgs pa{z.zhi, z.zlo, z.plain};
+    const float2 kgw = opv.kg[iw];
+    slice_load_async(sm, in + base, S, logN2, tid, nthr);
+    if (mode == ADJ_S || mode == ADJ_LOAD) {
+        if (mode == ADJ_S) {
+            for (int e = tid; e < S; e += nthr) {
+                const OpPoint o = op_at(opv, base + e, kgw);
+                const int pe = slice_pad(e, logN2);
+                // conj(D2) = (-i/2) conj(exp(-iKz) exp(Ki z)) / Re kz
+                const float2 f = cconj(propagator_factor(o, pa, -1.f));
+                sm[pe] = cscale(cmul_mi(cmul(f, sm[pe])), 0.5f / o.kzr);
+            }
+            __syncthreads();
+        }
+        slice_inverse(sm, logN1, logN2, tw, twLog, tid, nthr);
+        for (int e = tid; e < S; e += nthr) out[base + e] = sm[slice_pad(e, logN2)];
+    } else {
+        slice_forward(sm, logN1, logN2, tw, twLog, tid, nthr);
+        const float scale = 1.0f / (float)S;
+        for (int e = tid; e < S; e += nthr) {
+            const OpPoint o = op_at(opv, base + e, kgw);
+            float2 v = cmul(cconj(propagator_factor(o, pa, 1.f)), cscale(sm[slice_pad(e, logN2)], scale));
+            if (mode == ADJ_E) v = cmul(cconj(op_ikz(o)), v);
+            out[base + e] = v;
+        }
+    }
+}
+
+cudaError_t launch_adj_cart(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z) {
+    int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
+    h->launches++;
+    k_adj_cart<<<h->N0, h->S / SLICE_ET, (size_t)(h->S + h->N1) * sizeof(float2), h->stream>>>(
+        mode, in, uppe_op_view(h), out, logN1, logN2, h->tw, h->twLog, z);
+    return cudaGetLastError();
+}
+
+// RK4 adjoint bookkeeping, point by point (the conditioner C zeroes w-bins 0-3):
+//   init:    lam_f = C lam_out, acc = lam_f, lam_k = a_f lam_f
+//   combine: acc += C mu, lam_k = a_f lam_f + a_mu C mu
+//   final:   lam_in = acc + mu
+__global__ void k_adj_rk(int mode, const float2* __restrict__ lam_out, float2* __restrict__ lam_f,
+                         float2* __restrict__ acc, float2* __restrict__ lam_k, const float2* __restrict__ mu,
+                         float2* __restrict__ lam_in, float a_f, float a_mu, size_t n, int S) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float cond = (i < (size_t)4 * S) ? 0.f : 1.f;
+        if (mode == 0) {
+            const float2 lf = cscale(lam_out[i], cond);
+            lam_f[i] = lf;
+            acc[i] = lf;
+            lam_k[i] = cscale(lf, a_f);
+        } else if (mode == 1) {
+            const float2 cm = cscale(mu[i], cond);
+            acc[i] = cadd(acc[i], cm);
+            lam_k[i] = cadd(cscale(lam_f[i], a_f), cscale(cm, a_mu));
+        } else {
+            lam_in[i] = cadd(acc[i], mu[i]);
+        }
+    }
+}
+
+cudaError_t launch_adj_rk(UppeHandle* h, int mode, const float2* lam_out, float2* lam_in, float a_f, float a_mu) {
+    h->launches++;
+    k_adj_rk<<<reduce_blocks_host(h->P), 256, 0, h->stream>>>(mode, lam_out, h->adj_lf, h->adj_acc, h->adj_lk,
+                                                               h->adj_mu, lam_in, a_f, a_mu, h->P, h->S);
+    return cudaGetLastError();
+}
+
 static int slice_threads(const UppeHandle* h) { return h->S / SLICE_ET; }
 
 cudaError_t uppe_configure_slice_kernels(size_t smem_bytes) {
@@ -308,6 +394,8 @@ cudaError_t uppe_configure_slice_kernels(size_t smem_bytes) {
         e = cudaFuncSetAttribute(k_spec_cart, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_fused_cart, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_adj_cart, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     return e;
 }
 

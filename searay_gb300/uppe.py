@@ -135,6 +135,33 @@ class DeviceGrid:
         self._check(self.lib.uppe_check_finite(self.h, ctypes.byref(flag)))
         return bool(flag.value)
 
+    # ---- adjoint ----
+    def set_chi3(self, chi3_over_nref):
+        self._check(self.lib.uppe_set_chi3(self.h, float(chi3_over_nref)))
+
+    def set_field(self, q_dev):
+        self._check(self.lib.uppe_set_field(self.h, ctypes.c_void_p(q_dev.data_ptr())))
+
+    def adjoint_step(self, q0_dev, lam_out_dev, lam_in_dev, z_phase, dz):
+        """VJP of one fixed RK4 step; returns d(loss)/d(chi3/nref) of the step."""
+        d = ctypes.c_double(0.0)
+        self._check(self.lib.uppe_adjoint_rk4_step(self.h, ctypes.c_void_p(q0_dev.data_ptr()),
+                                                   ctypes.c_void_p(lam_out_dev.data_ptr()),
+                                                   ctypes.c_void_p(lam_in_dev.data_ptr()), z_phase, dz, ctypes.byref(d)))
+        return d.value
+
+    def adjoint_load(self, lam_q_dev, lam_a_dev):
+        self._check(self.lib.uppe_adjoint_load(self.h, ctypes.c_void_p(lam_q_dev.data_ptr()),
+                                               ctypes.c_void_p(lam_a_dev.data_ptr())))
+
+    def adjoint_finish(self, z_phase, lam_A_dev, lam_q_dev):
+        self._check(self.lib.uppe_adjoint_finish(self.h, z_phase, ctypes.c_void_p(lam_A_dev.data_ptr()),
+                                                 ctypes.c_void_p(lam_q_dev.data_ptr())))
+
+    def finish_field(self, z_phase, A_dev):
+        """The field output of uppe_finish only (A = T^-1 exp(i(kz+kg)z) q)."""
+        self._check(self.lib.uppe_finish(self.h, z_phase, ctypes.c_void_p(A_dev.data_ptr()), None, None, None))
+
     def profile(self, enable):
         self._check(self.lib.uppe_profile_enable(self.h, 1 if enable else 0))
 

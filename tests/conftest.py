@@ -2,7 +2,7 @@ import pathlib
 import sys
 
 ROOT = pathlib.Path(__file__).resolve().parent.parent
-for p in (str(ROOT), str(ROOT / "tests" / "golden")):
+for p in (str(ROOT), str(ROOT / "tests"), str(ROOT / "tests" / "golden")):
     if p not in sys.path:
         sys.path.insert(0, p)
 

@@ -1,0 +1,118 @@
+"""The hand-written adjoint of the UPPE step (through the C ABI) against a plain-PyTorch FP64
+autograd of the same step (tests/torch_reference.py), and gradients of a loss through the
+checkpointed torch.autograd.Function against central finite differences."""
+import numpy as np
+import pytest
+
+import replay
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def cuda_ready():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from searay_gb300 import build
+    build.build()
+
+
+def rel_err(x, ref):
+    return float(np.max(np.abs(x - ref)) / np.max(np.abs(ref)))
+
+
+def _setup(name, precision, zmat):
+    from oracle import uppe_oracle as O
+    from searay_gb300 import grid, ionization, uppe
+    vd, _ = replay.load_case(name)
+    g = grid.VolumeGrid(vd)
+    rates = ionization.RateCoefficients(vd["ionizer"]) if vd.get("ionizer") else None
+    dev = uppe.DeviceGrid(g, vd, rates, precision)
+    chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+    mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0), vd["density reference"],
+                        vd.get("window speed", 1.0), vd["density lambda"])
+    mat.UpdateMaterial(zmat)
+    orc = O.Oracle(vd)
+    orc.mat.update(zmat)
+    return vd, g, dev, orc
+
+
+# tolerance of the VJP: FP32 transforms 2e-4, the tensor-core Hankel transform of the mixed form 2e-3
+@pytest.mark.parametrize("name,precision", [("cart_ion", "mixed"), ("cart_series", "fp32"), ("cyl_kerr", "fp32"),
+                                            ("cyl_kerr", "mixed")])
+def test_vjp_of_rk4_step_matches_torch_fp64(name, precision):
+    import torch
+    from torch_reference import TorchStep
+    vd, g, dev, orc = _setup(name, precision, 3000.0)
+    redchi3 = vd.get("chi3", 0.0) / vd["density reference"]
+    ts = TorchStep(orc)
+    q0 = orc.g.kspace(vd["incoming wave"](g.w, g.x1, g.x2))
+    rng = np.random.default_rng(7)
+    lam = (rng.standard_normal(q0.shape) + 1j * rng.standard_normal(q0.shape)) * (np.abs(q0) + 1e-3 * np.abs(q0).max())
+    z, dz = 1500.0, 2500.0
+    # torch FP64 autograd of the same step
+    x = torch.tensor(q0.real, requires_grad=True)
+    y = torch.tensor(q0.imag, requires_grad=True)
+    c3 = torch.tensor(redchi3, dtype=torch.float64, requires_grad=True)
+    q1 = ts.step(torch.complex(x, y), z, dz, c3)
+    L = (torch.as_tensor(lam).conj() * q1).real.sum()
+    L.backward()
+    g_ref = x.grad.numpy() + 1j * y.grad.numpy()
+    dred_ref = float(c3.grad)
+    # the CUDA adjoint
+    q0d = torch.from_numpy(q0.astype(np.complex64)).cuda()
+    lamd = torch.from_numpy(lam.astype(np.complex64)).cuda()
+    out = dev.empty_field()
+    dred = dev.adjoint_step(q0d, lamd, out, z, dz)
+    g_gpu = out.cpu().numpy()
+    e = rel_err(g_gpu, g_ref)
+    ed = abs(dred - dred_ref) / abs(dred_ref)
+    # the forward step itself
+    dev.set_field(q0d)
+    dev.rk4_step(z, dz, 0.0, dz)
+    qd = dev.empty_field()
+    dev.get_field(qd)
+    ef = rel_err(qd.cpu().numpy(), q1.detach().numpy())
+    print(name, precision, f"vjp {e:.2e} dchi3 {ed:.2e} forward {ef:.2e}")
+    tol = 2e-3 if (precision == "mixed" and not g.cartesian) else 2e-4
+    assert e < tol and ed < tol
+    dev.close()
+
+
+@pytest.mark.parametrize("name", ["cart_ion", "cyl_kerr"])
+def test_gradient_matches_finite_differences(name):
+    """L = the on-axis spectral energy in the self-phase-modulation wing 1.15 < w < 1.4 after 6 steps
+    (FP64 accumulation); gradient with respect to a Legendre spectral-phase coefficient and chi3,
+    against central differences."""
+    import torch
+    from searay_gb300 import adjoint
+    vd, g, dev, orc = _setup(name, "fp32", 0.0)
+    redchi3 = vd.get("chi3", 0.0) / vd["density reference"]
+    a_base = vd["incoming wave"](g.w, g.x1, g.x2)
+    xi = 2 * (g.w - g.w[0]) / (g.w[-1] - g.w[0]) - 1
+    P2 = torch.tensor(0.5 * (3 * xi ** 2 - 1))[:, None, None]
+    base = torch.tensor(a_base)
+    band = (g.w > 1.15) & (g.w < 1.4)
+    ax = (0, 0) if not g.cartesian else (g.N[1] // 2, g.N[2] // 2)
+    nsteps, dz = 6, 1500.0
+
+    def loss(theta, chi):
+        a0 = (base * torch.exp(1j * theta * P2)).to(torch.complex64).cuda()
+        A = adjoint.propagate(dev, a0, chi, dz, nsteps, checkpoint_every=4)
+        sel = A[torch.as_tensor(band), ax[0], ax[1]].to(torch.complex128)
+        return (sel.abs() ** 2).sum()
+
+    theta = torch.tensor(0.3, dtype=torch.float64, requires_grad=True)
+    chi = torch.tensor(redchi3, dtype=torch.float64, requires_grad=True)
+    L = loss(theta, chi)
+    L.backward()
+    ht, hc = 1e-2, 1e-2 * redchi3
+    with torch.no_grad():
+        fd_t = (loss(theta + ht, chi) - loss(theta - ht, chi)).item() / (2 * ht)
+        fd_c = (loss(theta, chi + hc) - loss(theta, chi - hc)).item() / (2 * hc)
+    et = abs(theta.grad.item() - fd_t) / abs(fd_t)
+    ec = abs(chi.grad.item() - fd_c) / abs(fd_c)
+    print(name, f"dtheta {theta.grad.item():.6e} fd {fd_t:.6e} ({et:.1e}); dchi3 {chi.grad.item():.6e} fd {fd_c:.6e} ({ec:.1e})")
+    assert et < 2e-2 and ec < 2e-2
+    dev.close()

@@ -106,3 +106,27 @@ def test_grid_checks():
     vd, _ = _gaussian_case((65, 100, 128, 3))
     with pytest.raises(ValueError, match="x-nodes"):
         O.Oracle(vd)
+
+
+def test_torch_reference_step_matches_oracle():
+    """The PyTorch FP64 step used to check the adjoint equals the oracle's RK4 step."""
+    import torch
+    from torch_reference import TorchStep
+    for name in ("cart_ion", "cyl_kerr"):
+        vd, _ = replay.load_case(name)
+        orc = O.Oracle(vd)
+        orc.mat.update(3000.0)
+        g = orc.g
+        q0 = g.kspace(vd["incoming wave"](g.w, g.x1, g.x2))
+        z, dz = 1500.0, 2500.0
+        q1t = TorchStep(orc).step(torch.tensor(q0), z, dz, vd.get("chi3", 0.0) / vd["density reference"]).numpy()
+        cond = orc.conditioner[:, None, None]
+        k1 = orc.load_source(q0, z)
+        qf = q0 + dz / 6 * k1
+        k2 = orc.load_source((q0 + dz / 2 * k1) * cond, z + dz / 2)
+        qf = qf + dz / 3 * k2
+        k3 = orc.load_source((q0 + dz / 2 * k2) * cond, z + dz / 2)
+        qf = qf + dz / 3 * k3
+        k4 = orc.load_source((q0 + dz * k3) * cond, z + dz)
+        q1o = (qf + dz / 6 * k4) * cond
+        assert np.max(np.abs(q1t - q1o)) / np.max(np.abs(q1o)) < 1e-13
