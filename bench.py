@@ -196,6 +196,27 @@ def run_device(args, vd, ws, rank, local):
         torch.distributed.barrier()
     clk = clocks.stop()
     finite = not dev.nonfinite()
+    # forward + adjoint: K_a vector-Jacobian products of the RK4 step (each recomputes its stage
+    # states from the step's input, as the checkpointed backward pass does)
+    adj = None
+    if args.adjoint_steps > 0:
+        q = dev.empty_field()
+        dev.get_field(q)
+        gen = torch.Generator(device="cuda").manual_seed(0)
+        lam = torch.randn(q.shape, dtype=torch.complex64, device="cuda", generator=gen)
+        out = dev.empty_field()
+        for _ in range(2):
+            dev.adjoint_step(q, lam, out, step[0] * dz, dz, want_dchi3=False)
+        torch.cuda.synchronize()
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(stream)
+        for i in range(args.adjoint_steps):
+            dev.adjoint_step(q, lam, out, (step[0] + i) * dz, dz, want_dchi3=False)
+            lam, out = out, lam
+        a1.record(stream)
+        torch.cuda.synchronize()
+        adj = a0.elapsed_time(a1) / args.adjoint_steps
     # per-kernel-class timing (separate region; event records between launches)
     nprof = min(args.steps, 20)
     dev.profile(True)
@@ -204,7 +225,7 @@ def run_device(args, vd, ws, rank, local):
     prof = dev.profile_read()
     dev.profile(False)
     dev.close()
-    return P, ms, launches, clk, prof, finite
+    return P, ms, launches, clk, prof, finite, adj
 
 
 def run_e2e(args, vd):
@@ -313,6 +334,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=20,
+                    help="adjoint (VJP) steps timed for the forward+adjoint rate; 0 to skip")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -328,7 +351,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     else:
         torch.cuda.set_device(0)
-    P, ms, launches, clk, prof, finite = run_device(args, vd, ws, rank, local)
+    P, ms, launches, clk, prof, finite, adj_ms = run_device(args, vd, ws, rank, local)
     if ws > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -372,6 +395,12 @@ def main():
                    "l2": f"working set ({working_set_mb(vd):.0f} MB of fields and operator) vs the 129 MB L2"},
         "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk, "finite": finite,
     }
+    if adj_ms is not None:
+        fwd_ms = ms / args.steps
+        line["fwd_adjoint"] = {"value": P * ws / ((fwd_ms + adj_ms) / 1e3), "unit": UNIT,
+                               "adjoint_ms_per_step": adj_ms, "forward_ms_per_step": fwd_ms,
+                               "note": "one forward step plus one vector-Jacobian product of the step; the "
+                                       "VJP recomputes the step's stage states (checkpointed backward pass)"}
     if rank == 0 and not args.no_e2e:
         e2e, h2d, d2h, ok = run_e2e(args, vd)
         line["e2e"] = {"value": e2e * ws, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,

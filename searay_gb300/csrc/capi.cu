@@ -175,6 +175,12 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (tc > h->S) tc = h->S;
     h->time_cols = tc;
     h->redchi3 = c.chi3_over_nref;
+    // time-pass thread layout: 16 samples per thread (512 threads per 8192 samples, 2 blocks per SM)
+    // where the block stays within 1024 threads, else 32; SEARAY_UPPE_TIME_SPT=32 forces the latter
+    h->time_spt = (Nt * tc / 16 <= 1024) ? 16 : 32;
+    if (const char* v = getenv("SEARAY_UPPE_TIME_SPT")) {
+        if (atoi(v) == 32) h->time_spt = 32;
+    }
     int nt = Nt;
     if (c.n1 > nt) nt = c.n1;
     if (c.n2 > nt) nt = c.n2;

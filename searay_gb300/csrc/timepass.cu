@@ -29,6 +29,7 @@ struct TimeParams {
     float y0, ypow, yexp;  // explicit form: rate = 2^(y0 + ypow log2(Em) + yexp / Em)
     float lrc2;            // series form: log2(rate_conv)
     float c2[6];           // series form: log2(e) * c_i, polynomial in L = ln(Em)
+    float em_min;          // below this Em the rate is below FP32's smallest normal (taken as 0)
     int wcut, wwid, plain;
 };
 
@@ -37,6 +38,7 @@ struct TimeParams {
 // Ionization rate in simulation units from the field in simulation units.
 __device__ __forceinline__ float ion_rate(const TimeParams& tp, float e) {
     const float em = fmaf(tp.fconv, fabsf(e), tp.cutoff);
+    if (em < tp.em_min) return 0.f;
     const float l2 = __log2f(em);
     if (tp.rate_form == UPPE_RATE_EXPLICIT) {
         return exp2f(fmaf(tp.ypow, l2, fmaf(tp.yexp, __frcp_rn(em), tp.y0)));
@@ -97,12 +99,19 @@ __device__ __forceinline__ float2 real_spectrum(float2 Za, float2 Zb_raw, float2
     return cscale(csub(s, cmul_i(d)), 0.5f);
 }
 
+__device__ __forceinline__ void cp_async16_time(void* smem_dst, const void* gsrc) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc));
+}
+
 __device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
     const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gsrc));
 }
 
-__global__ void __launch_bounds__(256, 3) k_time(int mode, const float2* __restrict__ E, float2* __restrict__ out0,
+// ET: complex FFT elements per thread (16: 256 threads for C*Nt = 8192; 8: 512 threads)
+template <int ET>
+__global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : 2) k_time(int mode, const float2* __restrict__ E, float2* __restrict__ out0,
                                                   float2* __restrict__ out1, const float* __restrict__ ng,
                                                   const float* __restrict__ wv, const float* __restrict__ filt,
                                                   const float2* __restrict__ tw, int twLog, TimeParams tp) {
@@ -121,10 +130,19 @@ __global__ void __launch_bounds__(256, 3) k_time(int mode, const float2* __restr
     const TwHalfShared tws{twl, tp.logNt};
 
     // ---- 1. stage the half spectrum X[k][c], k in [0, M], with asynchronous copies ----
-    for (int it = tid; it < (M + 1) * C; it += T) {
-        const int c = it & (C - 1);
-        const int k = it >> logC;
-        cp_async8(&Zj[it], &E[(size_t)k * S + col0 + c]);
+    if (C >= 2) {
+        const int hC = C >> 1;  // 16-byte copies of two adjacent columns
+        for (int it = tid; it < (M + 1) * hC; it += T) {
+            const int c2 = it & (hC - 1);
+            const int k = it >> (logC - 1);
+            cp_async16_time(&Zj[k * C + 2 * c2], &E[(size_t)k * S + col0 + 2 * c2]);
+        }
+    } else {
+        for (int it = tid; it < (M + 1) * C; it += T) {
+            const int c = it & (C - 1);
+            const int k = it >> logC;
+            cp_async8(&Zj[it], &E[(size_t)k * S + col0 + c]);
+        }
     }
     asm volatile("cp.async.commit_group;\n" ::);
     for (int j = tid; j < (Nt >> 1); j += T) twl[j] = __ldg(&tw[j << (twLog - tp.logNt)]);
@@ -151,7 +169,7 @@ __global__ void __launch_bounds__(256, 3) k_time(int mode, const float2* __restr
         }
     }
     __syncthreads();
-    fft_axis_tw<16>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
+    fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
 
     // ---- 2. sources, in place ----
     const int c = tid & (C - 1);
@@ -223,8 +241,8 @@ __global__ void __launch_bounds__(256, 3) k_time(int mode, const float2* __restr
 
     // ---- 3. forward FFTs (P, then Jpl) and the current ----
     const bool two = ionize || mode == TIME_CHI_NE;
-    fft_axis_tw<16>(Zp, tp.logM, logC, 1, C, tws, false, tid, T);
-    if (two) fft_axis_tw<16>(Zj, tp.logM, logC, 1, C, tws, false, tid, T);
+    fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, false, tid, T);
+    if (two) fft_axis_tw<ET>(Zj, tp.logM, logC, 1, C, tws, false, tid, T);
     for (int it = tid; it < (M + 1) * C; it += T) {
         const int cc = it & (C - 1);
         const int k = it >> logC;
@@ -249,7 +267,9 @@ __global__ void __launch_bounds__(256, 3) k_time(int mode, const float2* __restr
 }
 
 cudaError_t uppe_configure_time_kernel(size_t smem_bytes) {
-    return cudaFuncSetAttribute(k_time, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_time<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_time<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    return e;
 }
 
 static TimeParams make_time_params(const UppeHandle* h) {
@@ -262,8 +282,8 @@ static TimeParams make_time_params(const UppeHandle* h) {
     tp.C = h->time_cols;
     tp.logC = ilog2_exact(h->time_cols);
     tp.S = h->S;
-    const int T = h->Nt * h->time_cols / 32;
-    tp.spt = h->Nt * h->time_cols / T;
+    const int T = h->Nt * h->time_cols / h->time_spt;
+    tp.spt = h->time_spt;
     tp.inv_nt = (float)(1.0 / (double)h->Nt);
     tp.hdt = (float)(0.5 * c.dt);
     tp.redchi3 = (float)h->redchi3;
@@ -280,16 +300,50 @@ static TimeParams make_time_params(const UppeHandle* h) {
     tp.wcut = c.window_cutoff;
     tp.wwid = c.window_width;
     tp.plain = (c.precision == UPPE_PREC_FP32);
+    tp.em_min = 0.f;
+    if (c.rate_form != UPPE_RATE_NONE) {
+        // log2(rate) as a function of Em (atomic units); it rises from -inf at Em -> 0 for physical
+        // rate models.  Bisect for the Em where it crosses -150, well below FP32's 2^-126.
+        auto log2rate = [&](double em) {
+            if (c.rate_form == UPPE_RATE_EXPLICIT)
+                return log2(c.rate_conv * c.c_pre) + c.c_pow * log2(em) + c.c_exp * log2e / em;
+            const double L = log(em);
+            double p = c.clog[5];
+            for (int i = 4; i >= 0; --i) p = p * L + c.clog[i];
+            return log2(c.rate_conv) + p * log2e;
+        };
+        double lo = c.field_cutoff, hi = 10.0;
+        if (log2rate(lo) < -150.0 && log2rate(hi) > -150.0) {
+            for (int it = 0; it < 80; ++it) {
+                const double mid = 0.5 * (lo + hi);
+                if (log2rate(mid) < -150.0)
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            // only trust the threshold if the rate really stays below it on [cutoff, lo]
+            bool mono = true;
+            for (int i = 0; i <= 64; ++i) {
+                const double em = c.field_cutoff + (lo - c.field_cutoff) * i / 64.0;
+                if (log2rate(em) > -150.0) mono = false;
+            }
+            if (mono) tp.em_min = (float)lo;
+        }
+    }
     return tp;
 }
 
 cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1) {
     const TimeParams tp = make_time_params(h);
-    const int T = h->Nt * h->time_cols / 32;
+    const int T = h->Nt * h->time_cols / h->time_spt;
     const size_t smem = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
     h->launches++;
-    k_time<<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw, h->twLog,
-                                                         tp);
+    if (h->time_spt == 16)
+        k_time<8><<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
+                                                               h->twLog, tp);
+    else
+        k_time<16><<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
+                                                                h->twLog, tp);
     return cudaGetLastError();
 }
 
@@ -525,8 +579,9 @@ cudaError_t uppe_configure_time_adj_kernel(size_t smem_bytes) {
 }
 
 cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G, float2* gE, double* dred) {
-    const TimeParams tp = make_time_params(h);
+    TimeParams tp = make_time_params(h);
     const int T = h->Nt * h->time_cols / 32;
+    tp.spt = 32;
     const size_t smem = ((size_t)(h->M + 1) * 5 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
     h->launches++;
     k_time_adj<<<h->S / h->time_cols, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred);

@@ -47,6 +47,7 @@ struct UppeHandle {
     size_t P;                      // N0*N1*N2
     int twLog;                     // twiddle table size 2^twLog
     int time_cols;                 // transverse points per CTA in the time pass
+    int time_spt;                  // time samples per thread in the time pass (16 or 32)
     int num_sms;                   // multiprocessors of the device
     cudaStream_t stream;
     // library-owned device buffers

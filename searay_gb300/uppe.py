@@ -142,13 +142,15 @@ class DeviceGrid:
     def set_field(self, q_dev):
         self._check(self.lib.uppe_set_field(self.h, ctypes.c_void_p(q_dev.data_ptr())))
 
-    def adjoint_step(self, q0_dev, lam_out_dev, lam_in_dev, z_phase, dz):
-        """VJP of one fixed RK4 step; returns d(loss)/d(chi3/nref) of the step."""
+    def adjoint_step(self, q0_dev, lam_out_dev, lam_in_dev, z_phase, dz, want_dchi3=True):
+        """VJP of one fixed RK4 step; returns d(loss)/d(chi3/nref) of the step (None when not asked,
+        which also avoids the host read)."""
         d = ctypes.c_double(0.0)
         self._check(self.lib.uppe_adjoint_rk4_step(self.h, ctypes.c_void_p(q0_dev.data_ptr()),
                                                    ctypes.c_void_p(lam_out_dev.data_ptr()),
-                                                   ctypes.c_void_p(lam_in_dev.data_ptr()), z_phase, dz, ctypes.byref(d)))
-        return d.value
+                                                   ctypes.c_void_p(lam_in_dev.data_ptr()), z_phase, dz,
+                                                   ctypes.byref(d) if want_dchi3 else None))
+        return d.value if want_dchi3 else None
 
     def adjoint_load(self, lam_q_dev, lam_a_dev):
         self._check(self.lib.uppe_adjoint_load(self.h, ctypes.c_void_p(lam_q_dev.data_ptr()),

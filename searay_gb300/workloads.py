@@ -14,6 +14,8 @@ with N0 = 2^n + 1 frequency nodes):
   at 5 critical powers, 8-mode seeded transverse phase (0.05 rad, numpy default_rng(0)), Kerr
   (n2 = 3e-19 cm^2/W) + O2 tunneling ionization (PPT, Ip = 12.07 eV, Z = 0.53) at 5.4e18 cm^-3 +
   plasma current, 400 RK4 steps over 10 cm.
+* ``cyl_adjoint_256``: the physics of ``cyl_kerr_64`` on N0 = 1025 (Nt = 2048, band 0-6.9 w0),
+  Nr = Nk = 256, 200 RK4 steps over 10 cm; the forward + adjoint workload.
 * ``cyl_silica_512``: cylindrical Nr = Nk = 512 over R = 0.5 mm, N0 = 2049, 1 um 100 fs pulse at
   1e14 W/cm^2 in fused silica (Malitson Sellmeier, n2 = 2.5e-16 cm^2/W), PPT tunneling with
   Ip = 9 eV (Z = 1 assumed) at 2.2e22 cm^-3, 100 RK4 steps over 1 cm.
@@ -181,4 +183,16 @@ def cyl_silica_512(steps=100):
     return vd
 
 
-WORKLOADS = {"cyl_kerr_64": cyl_kerr_64, "cart_filament_128": cart_filament_128, "cyl_silica_512": cyl_silica_512}
+def cyl_adjoint_256(steps=200):
+    """The adjoint workload: cyl_kerr_64's physics on N0 = 1025 (band scaled with the grid), Nr = 256."""
+    vd = cyl_kerr_64(steps)
+    W = vd["frequency band"][1] * 1024 / 256
+    vd["wave grid"] = (1025, 256, 1, 2)
+    vd["radial modes"] = 256
+    vd["frequency band"] = (0.0, W)
+    vd["nonlinear band"] = (0.0, W)
+    return vd
+
+
+WORKLOADS = {"cyl_kerr_64": cyl_kerr_64, "cart_filament_128": cart_filament_128, "cyl_silica_512": cyl_silica_512,
+             "cyl_adjoint_256": cyl_adjoint_256}
