@@ -181,6 +181,12 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (const char* v = getenv("SEARAY_UPPE_TIME_SPT")) {
         if (atoi(v) == 32) h->time_spt = 32;
     }
+    // Cartesian slices of 16..128 points per axis use the register-resident transforms;
+    // SEARAY_UPPE_SLICE=generic selects the shared-memory Stockham form for them as well
+    h->slice_reg = !c.cylindrical && reg_slice_supported(c.n1, c.n2);
+    if (const char* v = getenv("SEARAY_UPPE_SLICE")) {
+        if (strcmp(v, "generic") == 0) h->slice_reg = 0;
+    }
     int nt = Nt;
     if (c.n1 > nt) nt = c.n1;
     if (c.n2 > nt) nt = c.n2;

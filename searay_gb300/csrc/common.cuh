@@ -126,6 +126,15 @@ UPPE_DEV float2 propagator_factor(const OpPoint& o, PhaseArgs pa, float sign) {
     return make_float2(amp * c, sign * amp * s);
 }
 
+// Ask the memory system to bring `bytes` (a multiple of 16, 16-byte aligned) into L2 ahead of use.
+UPPE_DEV void prefetch_l2(const void* p, size_t bytes) {
+    const char* c = (const char*)p;
+    for (size_t off = 0; off < bytes; off += 32768) {
+        const unsigned n = (unsigned)((bytes - off) < 32768 ? (bytes - off) : 32768);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(c + off), "r"(n) : "memory");
+    }
+}
+
 __host__ __device__ inline int ilog2_exact(int n) {
     int l = 0;
     while ((1 << l) < n) ++l;

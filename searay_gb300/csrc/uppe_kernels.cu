@@ -10,6 +10,7 @@
 
 #include "common.cuh"
 #include "fft_smem.cuh"
+#include "rk_stage.cuh"
 #include "uppe_internal.h"
 
 // =============================================================================================
@@ -120,15 +121,6 @@ __device__ __forceinline__ void cp_async8_slice(void* smem_dst, const void* gsrc
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gsrc));
 }
 
-// Ask the memory system to bring `bytes` (a multiple of 16, 16-byte aligned) into L2 ahead of use.
-__device__ __forceinline__ void prefetch_l2(const void* p, size_t bytes) {
-    const char* c = (const char*)p;
-    for (size_t off = 0; off < bytes; off += 32768) {
-        const unsigned n = (unsigned)((bytes - off) < 32768 ? (bytes - off) : 32768);
-        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(c + off), "r"(n) : "memory");
-    }
-}
-
 __device__ __forceinline__ void slice_load_async(float2* sm, const float2* __restrict__ src, int S, int logN2, int tid,
                                                  int nthr) {
     for (int e = tid; e < S; e += nthr) cp_async8_slice(&sm[slice_pad(e, logN2)], &src[e]);
@@ -198,44 +190,6 @@ __global__ void __launch_bounds__(1024) k_real_cart(int mode, const float2* __re
             E[base + e] = cmul(op_ikz(o), v);
         }
     }
-}
-
-// ODE right-hand side S = (i/2) exp(-i(kz+kg)z) J / Re kz (uppe.cl:73-91) and the RK4 bookkeeping of
-// RKStage/RKFinish (uppe.cl:22-52) with the DC conditioner (uppe_kernel.py:127-137) on the stage
-// estimate.  Returns the new stage estimate (qw), or S itself for SPEC_STORE_K.
-__device__ __forceinline__ float2 spec_update(int mode, size_t idx, float2 v, const OpPoint& o, float cond,
-                                              float2* __restrict__ q_out, float2* __restrict__ qf,
-                                              const float2* __restrict__ qi, float Cs, float Ce, const PhaseArgs& pa,
-                                              bool store_q) {
-    if (mode == SPEC_LOAD) {
-        q_out[idx] = v;
-        return v;
-    }
-    const float2 f = propagator_factor(o, pa, -1.f);
-    const float2 s = cscale(cmul_i(cmul(f, v)), 0.5f / o.kzr);
-    float2 qw;
-    switch (mode) {
-        case SPEC_STORE_K:
-            q_out[idx] = s;
-            return s;
-        case SPEC_STAGE1: {
-            const float2 a = qi[idx];
-            qf[idx] = cadd(a, cscale(s, Cs));
-            qw = cscale(cadd(a, cscale(s, Ce)), cond);
-        } break;
-        case SPEC_STAGE23: {
-            const float2 a = qi[idx];
-            const float2 b = qf[idx];
-            qf[idx] = cadd(b, cscale(s, Cs));
-            qw = cscale(cadd(a, cscale(s, Ce)), cond);
-        } break;
-        default: {  // SPEC_FINISH
-            const float2 b = qf[idx];
-            qw = cscale(cadd(b, cscale(s, Cs)), cond);
-        } break;
-    }
-    if (store_q) q_out[idx] = qw;
-    return qw;
 }
 
 __global__ void __launch_bounds__(1024) k_spec_cart(int mode, const float2* __restrict__ src, OpView opv,
@@ -348,6 +302,7 @@ __global__ void __launch_bounds__(1024) k_adj_cart(int mode, const float2* __res
 }
 
 cudaError_t launch_adj_cart(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z) {
+    if (h->slice_reg) return launch_adj_reg(h, mode, in, out, z);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
     k_adj_cart<<<h->N0, h->S / SLICE_ET, (size_t)(h->S + h->N1) * sizeof(float2), h->stream>>>(
@@ -396,12 +351,17 @@ cudaError_t uppe_configure_slice_kernels(size_t smem_bytes) {
         e = cudaFuncSetAttribute(k_fused_cart, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (e == cudaSuccess)
         e = cudaFuncSetAttribute(k_adj_cart, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    if (e == cudaSuccess) e = configure_fused_reg();
+    if (e == cudaSuccess) e = configure_real_reg();
+    if (e == cudaSuccess) e = configure_spec_reg();
+    if (e == cudaSuccess) e = configure_adj_reg();
     return e;
 }
 
 static size_t slice_smem(const UppeHandle* h) { return (size_t)(h->S + h->N1) * sizeof(float2); }
 
 cudaError_t launch_real_cart(UppeHandle* h, int mode, const float2* src, float2* A_out, StepArgs z) {
+    if (h->slice_reg) return launch_real_reg(h, mode, src, A_out, nullptr, nullptr, 0.f, 0.f, z);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
     k_real_cart<<<h->N0, slice_threads(h), slice_smem(h), h->stream>>>(mode, src, uppe_op_view(h), h->E, A_out,
@@ -411,6 +371,7 @@ cudaError_t launch_real_cart(UppeHandle* h, int mode, const float2* src, float2*
 }
 
 cudaError_t launch_apply1_cart(UppeHandle* h, float Cs, float Ce, StepArgs z) {
+    if (h->slice_reg) return launch_real_reg(h, REAL_APPLY1, h->qi, nullptr, h->k1, h->qf, Cs, Ce, z);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
     k_real_cart<<<h->N0, slice_threads(h), slice_smem(h), h->stream>>>(REAL_APPLY1, h->qi, uppe_op_view(h), h->E,
@@ -421,6 +382,7 @@ cudaError_t launch_apply1_cart(UppeHandle* h, float Cs, float Ce, StepArgs z) {
 
 cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, float2* q_out, float2* qf_io,
                              const float2* qi, float Cs, float Ce, StepArgs z) {
+    if (h->slice_reg) return launch_spec_reg(h, mode, src_real, q_out, qf_io, qi, Cs, Ce, z);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
     k_spec_cart<<<h->N0, slice_threads(h), slice_smem(h), h->stream>>>(mode, src_real, uppe_op_view(h), q_out, qf_io,
@@ -429,6 +391,7 @@ cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, fl
 }
 
 cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
+    if (h->slice_reg) return launch_fused_reg(h, mode, Cs, Ce, z_rhs, z_next);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
     k_fused_cart<<<h->N0, slice_threads(h), slice_smem(h), h->stream>>>(mode, h->J, uppe_op_view(h), h->qi, h->qf,
