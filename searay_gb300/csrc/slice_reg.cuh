@@ -9,7 +9,8 @@
 //       16-point DFT over m in registers -> a;  twiddle W_N^(j a);
 //       exchange within the R threads of the line (warp-private shared memory);
 //       R-point DFTs over j -> thread j holds X[j + R s + 16 b] (s < 16/R, b < R)
-//   mixed -> natural (m2n):  the same steps in reverse order.
+//   mixed -> natural (m2n):  the same steps in reverse order (the receiving lane j applies the
+//       twiddle W_N^(j a) after the exchange, so both directions use one per-thread twiddle set).
 //
 // A 2D transform is n2m along y (rows, the contiguous axis), one transpose through shared memory,
 // n2m along x; the inverse mirrors it.  Per slice that is six shared-memory round trips and six
@@ -86,21 +87,47 @@ UPPE_DEV float2 tw_at(const TwGlobal& tw, int k, int sh) {
     return t;
 }
 
+// v[a] *= W_N^(j a), a = 1..15, N = 2^LOGN: applied one bit of a at a time (W^j, W^2j, W^4j, W^8j
+// from the table), so a single twiddle is live; each v[a] takes at most four products.
+template <bool INV, int LOGN>
+UPPE_DEV void twiddle_line(float2 (&v)[16], int j, const TwGlobal& tw) {
+    const int sh = tw.log - LOGN;
+#pragma unroll
+    for (int bit = 1; bit < 16; bit <<= 1) {
+        const float2 t = tw_at<INV>(tw, j * bit, sh);
+#pragma unroll
+        for (int a = 1; a < 16; ++a)
+            if (a & bit) v[a] = cmul(v[a], t);
+    }
+}
+
+// Synchronisation of the threads of one line around an exchange: the R2 threads of a row line are
+// lanes of one warp; the R1 threads of a column line are lanes l and l + 16 of R1/2 warps, which
+// meet at a named barrier when R1 >= 4.
+template <bool NAMED>
+struct LineSync {
+    int id, count;
+    UPPE_DEV void operator()() const {
+        if constexpr (NAMED)
+            asm volatile("bar.sync %0, %1;\n" ::"r"(id), "r"(count) : "memory");
+        else
+            __syncwarp();
+    }
+};
+
 // natural -> mixed along one axis of length 16 R; `ex` is this line's exchange region, j the
 // thread's index within the line.  v[m] = x[j + R m]  ->  w[s R + b] = X[j + R s + 16 b].
-template <int R, int LOGN, bool INV>
-UPPE_DEV void reg_n2m(float2 (&v)[16], float2 (&w)[16], float2* ex, int j, const TwGlobal& tw) {
+template <int R, int LOGN, bool INV, class SY>
+UPPE_DEV void reg_n2m(float2 (&v)[16], float2 (&w)[16], float2* ex, int j, const TwGlobal& tw, const SY& sync) {
     dft16<INV>(v);
     if constexpr (R == 1) {
 #pragma unroll
         for (int a = 0; a < 16; ++a) w[a] = v[a];
     } else {
-        const int sh = tw.log - LOGN;
-#pragma unroll
-        for (int a = 1; a < 16; ++a) v[a] = cmul(v[a], tw_at<INV>(tw, j * a, sh));
+        twiddle_line<INV, LOGN>(v, j, tw);
 #pragma unroll
         for (int a = 0; a < 16; ++a) ex[j * 17 + a] = v[a];
-        __syncwarp();
+        sync();
 #pragma unroll
         for (int s = 0; s < 16 / R; ++s) {
             float2 u[R];
@@ -114,14 +141,13 @@ UPPE_DEV void reg_n2m(float2 (&v)[16], float2 (&w)[16], float2* ex, int j, const
 }
 
 // mixed -> natural along one axis: w[s R + b] = X[j + R s + 16 b]  ->  v[m] = x[j + R m].
-template <int R, int LOGN, bool INV>
-UPPE_DEV void reg_m2n(float2 (&w)[16], float2 (&v)[16], float2* ex, int j, const TwGlobal& tw) {
+template <int R, int LOGN, bool INV, class SY>
+UPPE_DEV void reg_m2n(float2 (&w)[16], float2 (&v)[16], float2* ex, int j, const TwGlobal& tw, const SY& sync) {
     if constexpr (R == 1) {
 #pragma unroll
         for (int a = 0; a < 16; ++a) v[a] = w[a];
     } else {
-        const int sh = tw.log - LOGN;
-        __syncwarp();  // the line's last reads of this region are done
+        sync();  // the line's last reads of this region are done
 #pragma unroll
         for (int s = 0; s < 16 / R; ++s) {
             float2 u[R];
@@ -129,16 +155,18 @@ UPPE_DEV void reg_m2n(float2 (&w)[16], float2 (&v)[16], float2* ex, int j, const
             for (int b = 0; b < R; ++b) u[b] = w[s * R + b];
             dft_small<R>(u, INV);
             const int a = j + R * s;
-            ex[a] = u[0];
 #pragma unroll
-            for (int jj = 1; jj < R; ++jj) ex[jj * 17 + a] = cmul(u[jj], tw_at<INV>(tw, jj * a, sh));
+            for (int jj = 0; jj < R; ++jj) ex[jj * 17 + a] = u[jj];
         }
-        __syncwarp();
+        sync();
 #pragma unroll
         for (int a = 0; a < 16; ++a) v[a] = ex[j * 17 + a];
+        twiddle_line<INV, LOGN>(v, j, tw);  // the receiving lane applies W^(j a)
     }
     dft16<INV>(v);
 }
+
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
 template <int LN1, int LN2>
 struct RegSlice {
@@ -147,22 +175,45 @@ struct RegSlice {
     static constexpr int P = N2 + 2;
     static constexpr int EXW = 544;
     static constexpr int NWARP = (T + 31) / 32;
-    static constexpr int SMEM = (N1 * P > NWARP * EXW ? N1 * P : NWARP * EXW) * (int)sizeof(float2);
+    static constexpr int QC = 17 * R1 + 1;  // column line region pitch (odd: conflict-free)
+    static constexpr int A1 = N1 * P > NWARP * EXW ? N1 * P : NWARP * EXW;
+    static constexpr int SMEM = (A1 > N2 * QC ? A1 : N2 * QC) * (int)sizeof(float2);
+    static constexpr bool COL_NAMED = R1 >= 4;
 };
 
-// Thread coordinates of both layouts.  Row layout: line x (row), lane jr; column layout: line ky
-// (column), lane ic.  exr / exc: the thread's line region for the exchanges.
+// Thread coordinates of both layouts.
+//  * Row layout: line x (row), lane jr; tid = x R2 + jr, so a row's R2 threads share a warp.
+//  * Column layout: line ky (column), lane ic; a warp holds 16 consecutive ky and two ic, so that
+//    its global accesses in this layout are two 128-byte row segments (the pointwise operands, the
+//    spectral outputs).  A column's R1 threads are lanes l, l + 16 of R1/2 warps.
+// exr / exc: the thread's line region for the exchanges (element (j, a) at j * LW + a, LW = 17 for
+// sixteen-value exchanges, 9 for eight-value halves): per warp for rows, per ky for columns.
 template <class RS>
 struct RegCoords {
     int x, jr, ky, ic;
     float2 *exr, *exc;
-    UPPE_DEV RegCoords(float2* sm, int tid) {
+    LineSync<RS::COL_NAMED> csync;
+    LineSync<false> rsync;
+    UPPE_DEV RegCoords(float2* xb, int tid, bool half) {
         x = tid / RS::R2;
         jr = tid % RS::R2;
-        ky = tid / RS::R1;
-        ic = tid % RS::R1;
-        exr = sm + (tid >> 5) * RS::EXW + ((tid & 31) / RS::R2) * 17 * RS::R2;
-        exc = sm + (tid >> 5) * RS::EXW + ((tid & 31) / RS::R1) * 17 * RS::R1;
+        constexpr int KB = RS::N2 / 16;
+        if constexpr (RS::R1 == 1) {
+            ky = tid;
+            ic = 0;
+            csync.id = 1;
+        } else {
+            const int warp = tid >> 5, lane = tid & 31;
+            ky = (warp % KB) * 16 + (lane & 15);
+            ic = (warp / KB) * 2 + (lane >> 4);
+            csync.id = 1 + warp % KB;
+        }
+        csync.count = 32 * (RS::R1 / 2 > 0 ? RS::R1 / 2 : 1);
+        rsync.id = 0;
+        rsync.count = 0;
+        const int lw = half ? 9 : 17;
+        exr = xb + (tid >> 5) * (half ? 288 : 544) + ((tid & 31) / RS::R2) * lw * RS::R2;
+        exc = xb + ky * (lw * RS::R1 + 1);
     }
 };
 
@@ -202,9 +253,9 @@ UPPE_DEV void slice_fwd_from_global(const float2* __restrict__ src, float2 (&w)[
     const float2* p = src + (size_t)c.x * RS::N2 + c.jr;
 #pragma unroll
     for (int m = 0; m < 16; ++m) v[m] = p[RS::R2 * m];
-    reg_n2m<RS::R2, LN2, INV>(v, w, c.exr, c.jr, tw);
+    reg_n2m<RS::R2, LN2, INV>(v, w, c.exr, c.jr, tw, c.rsync);
     rows_to_cols<RS>(w, v, sm, c);
-    reg_n2m<RS::R1, LN1, INV>(v, w, c.exc, c.ic, tw);
+    reg_n2m<RS::R1, LN1, INV>(v, w, c.exc, c.ic, tw, c.csync);
 }
 
 // Inverse 2D transform: w in the column layout, mixed order -> v in the row layout, natural order
@@ -212,9 +263,9 @@ UPPE_DEV void slice_fwd_from_global(const float2* __restrict__ src, float2 (&w)[
 template <class RS, int LN1, int LN2, bool INV>
 UPPE_DEV void slice_inv_to_rows(float2 (&w)[16], float2 (&v)[16], float2* sm, const RegCoords<RS>& c,
                                 const TwGlobal& tw) {
-    reg_m2n<RS::R1, LN1, INV>(w, v, c.exc, c.ic, tw);
+    reg_m2n<RS::R1, LN1, INV>(w, v, c.exc, c.ic, tw, c.csync);
     cols_to_rows<RS>(v, w, sm, c);
-    reg_m2n<RS::R2, LN2, INV>(w, v, c.exr, c.jr, tw);
+    reg_m2n<RS::R2, LN2, INV>(w, v, c.exr, c.jr, tw, c.rsync);
 }
 
 // linear index (within the slice) of register r of the column layout
@@ -225,50 +276,321 @@ UPPE_DEV int col_elem(const RegCoords<RS>& c, int r) {
 }
 
 // ---------------------------------------------------------------------------------------------
+// Half-size exchanges for the persistent fused pass.  The line exchanges go through a 288-element
+// region per warp (line l at l * 9 R, element (j, a') at j * 9 + a', a' < 8) in two halves of eight
+// values; the transpose goes through an N1 x (N2/2 + 2) buffer in two phases, the diagonal
+// quadrants (top bit of x equal to the top bit of ky) and then the others.  In both layouts the top
+// bit of a thread's line (x or ky) is the top bit of its thread index, so each phase moves eight of
+// every thread's sixteen values and the register footprint stays at sixteen.
+// ---------------------------------------------------------------------------------------------
+template <int R, int LOGN, bool INV, class SY>
+UPPE_DEV void reg_n2m_h(float2 (&v)[16], float2 (&w)[16], float2* ex, int j, const TwGlobal& tw, const SY& sync) {
+    dft16<INV>(v);
+    if constexpr (R == 1) {
+#pragma unroll
+        for (int a = 0; a < 16; ++a) w[a] = v[a];
+    } else {
+        twiddle_line<INV, LOGN>(v, j, tw);
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (h) sync();  // the line's reads of the first half are done
+#pragma unroll
+            for (int ap = 0; ap < 8; ++ap) ex[j * 9 + ap] = v[8 * h + ap];
+            sync();
+#pragma unroll
+            for (int s = 8 * h / R; s < (8 * h + 8) / R; ++s) {
+                float2 u[R];
+#pragma unroll
+                for (int jj = 0; jj < R; ++jj) u[jj] = ex[jj * 9 + j + R * s - 8 * h];
+                dft_small<R>(u, INV);
+#pragma unroll
+                for (int b = 0; b < R; ++b) w[s * R + b] = u[b];
+            }
+        }
+    }
+}
+
+template <int R, int LOGN, bool INV, class SY>
+UPPE_DEV void reg_m2n_h(float2 (&w)[16], float2 (&v)[16], float2* ex, int j, const TwGlobal& tw, const SY& sync) {
+    if constexpr (R == 1) {
+#pragma unroll
+        for (int a = 0; a < 16; ++a) v[a] = w[a];
+    } else {
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            sync();  // the line's previous reads of this region are done
+#pragma unroll
+            for (int s = 8 * h / R; s < (8 * h + 8) / R; ++s) {
+                float2 u[R];
+#pragma unroll
+                for (int b = 0; b < R; ++b) u[b] = w[s * R + b];
+                dft_small<R>(u, INV);
+                const int a = j + R * s;
+#pragma unroll
+                for (int jj = 0; jj < R; ++jj) ex[jj * 9 + a - 8 * h] = u[jj];
+            }
+            sync();
+#pragma unroll
+            for (int ap = 0; ap < 8; ++ap) v[8 * h + ap] = ex[j * 9 + ap];
+        }
+        twiddle_line<INV, LOGN>(v, j, tw);  // the receiving lane applies W^(j a)
+    }
+    dft16<INV>(v);
+}
+
+// Register pairs of the two layouts whose points differ only in the top bit of the transposed
+// axis: row layout pair i = (lo, hi) with ky(hi) = ky(lo) + N2/2; column layout pair (i, i + 8)
+// with x differing by N1/2.  A phase moves one member of every pair, chosen by the thread's top
+// bit with selects, so every register index stays compile-time.
+template <class RS>
+UPPE_DEV void row_pair(int i, int& lo, int& hi) {
+    if constexpr (RS::R2 >= 2) {
+        constexpr int HB = RS::R2 / 2;
+        const int s = i / HB, b = i % HB;
+        lo = s * RS::R2 + b;
+        hi = lo + HB;
+    } else {
+        lo = i;
+        hi = i + 8;
+    }
+}
+template <class RS>
+UPPE_DEV int row_pair_ky(int i, int jr) {  // ky of the lo member, top bit clear
+    if constexpr (RS::R2 >= 2) {
+        constexpr int HB = RS::R2 / 2;
+        return jr + RS::R2 * (i / HB) + 16 * (i % HB);
+    } else {
+        return i;
+    }
+}
+
+template <class RS>
+UPPE_DEV void rows_to_cols_h(float2 (&w)[16], float2 (&v)[16], float2* xb, const RegCoords<RS>& c) {
+    constexpr int PH = RS::N2 / 2 + 2, HM = RS::N2 / 2 - 1;
+    const int top = c.x >> (ilog2c(RS::N1) - 1);   // row role: top bit of x
+    const int topc = c.ky >> (ilog2c(RS::N2) - 1);  // column role: top bit of ky
+    const int cshift = topc * (RS::N1 / 2) * PH;  // column-side offset of the phase-0 half
+    float2 snd1[8], rcv0[8];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {  // phase 0: the diagonal quadrants (top bit of x == top bit of ky)
+        int lo, hi;
+        row_pair<RS>(i, lo, hi);
+        xb[c.x * PH + (row_pair_ky<RS>(i, c.jr) & HM)] = top ? w[hi] : w[lo];
+        snd1[i] = top ? w[lo] : w[hi];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) rcv0[i] = xb[(c.ic + RS::R1 * i) * PH + cshift + (c.ky & HM)];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) xb[c.x * PH + (row_pair_ky<RS>(i, c.jr) & HM)] = snd1[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float2 r1 = xb[(c.ic + RS::R1 * i) * PH + ((RS::N1 / 2) * PH - cshift) + (c.ky & HM)];
+        v[i] = topc ? r1 : rcv0[i];
+        v[i + 8] = topc ? rcv0[i] : r1;
+    }
+    __syncthreads();
+}
+
+template <class RS>
+UPPE_DEV void cols_to_rows_h(float2 (&v)[16], float2 (&w)[16], float2* xb, const RegCoords<RS>& c) {
+    constexpr int PH = RS::N2 / 2 + 2, HM = RS::N2 / 2 - 1;
+    const int top = c.x >> (ilog2c(RS::N1) - 1);
+    const int topc = c.ky >> (ilog2c(RS::N2) - 1);
+    const int cshift = topc * (RS::N1 / 2) * PH;
+    float2 snd1[8], rcv0[8];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        xb[(c.ic + RS::R1 * i) * PH + cshift + (c.ky & HM)] = topc ? v[i + 8] : v[i];
+        snd1[i] = topc ? v[i] : v[i + 8];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) rcv0[i] = xb[c.x * PH + (row_pair_ky<RS>(i, c.jr) & HM)];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) xb[(c.ic + RS::R1 * i) * PH + ((RS::N1 / 2) * PH - cshift) + (c.ky & HM)] = snd1[i];
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        int lo, hi;
+        row_pair<RS>(i, lo, hi);
+        const float2 r1 = xb[c.x * PH + (row_pair_ky<RS>(i, c.jr) & HM)];
+        w[lo] = top ? r1 : rcv0[i];
+        w[hi] = top ? rcv0[i] : r1;
+    }
+    __syncthreads();
+}
+
+// Shared-memory plan of the persistent fused pass.
+//  * staging buffer: the next slice's current, row pitch N2 + 8 (conflict-free row-layout reads);
+//    during the pointwise phase a ring of NSLOT operand slots, slot r % NSLOT holding K, qi and qf
+//    of register r of every thread (T points per array, in thread order);
+//  * the half-size exchange buffer.
+// All copies are 16-byte cp.async.cg, which go from L2 to shared memory without allocating in L1:
+// beside 200+ KB of shared memory the L1 is small, and L1-allocating loads in flight are capped by
+// its size.  A ring copy moves the points (kx, ky) and (kx, ky + 1) at once, for the thread with
+// even ky and for its neighbour in the next lane; a __syncwarp after the wait publishes it.
+template <int LN1, int LN2>
+struct FusedPlan {
+    using RS = RegSlice<LN1, LN2>;
+    static constexpr int JP = RS::N2 + 8;
+    static constexpr int JSTAGE = RS::N1 * JP;
+    static constexpr int SLOT = 3 * RS::T;
+    static constexpr int XT = RS::N1 * (RS::N2 / 2 + 2);
+    static constexpr int XE = RS::NWARP * 288;
+    static constexpr int XC = RS::N2 * (9 * RS::R1 + 1);
+    static constexpr int XBUF = (XT > XE ? XT : XE) > XC ? (XT > XE ? XT : XE) : XC;
+    static constexpr int NSLOT = (JSTAGE / SLOT) < 6 ? (JSTAGE / SLOT) : 6;
+    static constexpr int SMEM = (JSTAGE + XBUF) * (int)sizeof(float2);
+    static constexpr unsigned WMASK = RS::T >= 32 ? 0xffffffffu : ((1u << RS::T) - 1u);
+    static_assert(NSLOT >= 2, "operand ring too small");
+    static_assert(RS::N2 % 2 == 0 && (JP * 8) % 16 == 0, "16-byte copies");
+};
+
+UPPE_DEV void stage_async16(float2* smem_dst, const float2* gsrc) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(gsrc) : "memory");
+}
+
+// ---------------------------------------------------------------------------------------------
 // Fused evaluation tail (the same contract as the generic k_fused_cart): forward 2D FFT of J,
 // S = (i/2) exp(-i(kz+kg) z) J / Re kz and the RK stage, then E for the next evaluation,
 // E = IFFT2(i kz exp(i(kz+kg) z_next) qw)  (uppe.cl:22-52,73-108; uppe_kernel.py:210-213).
+//
+// Persistent: one CTA per multiprocessor walks the slices iw = blockIdx.x, + gridDim.x, ...  The
+// next slice's current is copied into the staging buffer during this slice's inverse transform;
+// the pointwise operands stream through the ring during the forward transform and the pointwise
+// loop.
 // ---------------------------------------------------------------------------------------------
 template <int LN1, int LN2>
 __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     k_fused_reg(int mode, const float2* __restrict__ J, OpView opv, float2* __restrict__ qi_out,
                 float2* __restrict__ qf, const float2* __restrict__ qi, float2* __restrict__ E, float Cs, float Ce,
-                const float2* __restrict__ tw, int twLog, StepArgs z_rhs, StepArgs z_next, int next_wave) {
+                const float2* __restrict__ tw, int twLog, StepArgs z_rhs, StepArgs z_next, int n0) {
     using RS = RegSlice<LN1, LN2>;
-    extern __shared__ float2 sm[];
-    const int tid = threadIdx.x, iw = blockIdx.x;
-    const size_t base = (size_t)iw * RS::S;
-    if (tid == 0) {
-        // operator and RK state of this slice are read after the forward FFT: fetch them into L2 now;
-        // also the current of the slice a CTA of the next wave will take
-        constexpr size_t fb = (size_t)RS::S * sizeof(float2);
-        prefetch_l2(opv.K + base, fb);
-        if (mode != SPEC_FINISH) prefetch_l2(qi + base, fb);
-        if (mode != SPEC_STAGE1) prefetch_l2(qf + base, fb);
-        if ((int)(iw + next_wave) < (int)gridDim.x) prefetch_l2(J + base + (size_t)next_wave * RS::S, fb);
-    }
-    const TwGlobal twg{tw, twLog};
-    const RegCoords<RS> c(sm, tid);
-    float2 w[16], v[16];
-    slice_fwd_from_global<RS, LN1, LN2, false>(J + base, w, sm, c, twg);
-
+    using FP = FusedPlan<LN1, LN2>;
+    extern __shared__ __align__(16) float2 sm[];
+    float2* jst = sm;
+    float2* xb = sm + FP::JSTAGE;
+    const int tid = threadIdx.x;
     const PhaseArgs pr{z_rhs.zhi, z_rhs.zlo, z_rhs.plain};
     const PhaseArgs pn{z_next.zhi, z_next.zlo, z_next.plain};
-    const float cond = (iw < 4) ? 0.f : 1.f;
-    const float2 kgw = opv.kg[iw];
-    const bool last = (mode == SPEC_FINISH);
+    const bool need_qi = (mode != SPEC_FINISH), need_qf = (mode != SPEC_STAGE1);
+
+    // the current of slice iw -> staging buffer, 16-byte chunks, consecutive threads on consecutive chunks
+    auto issue_J = [&](int iw) {
+        const float2* src = J + (size_t)iw * RS::S;
 #pragma unroll
-    for (int r = 0; r < 16; ++r) {
-        const size_t idx = base + col_elem(c, r);
-        const OpPoint o = op_at(opv, idx, kgw);
-        const float2 qw = spec_update(mode, idx, w[r], o, cond, qi_out, qf, qi, Cs, Ce, pr, last);
-        w[r] = cmul(op_ikz(o), cmul(propagator_factor(o, pn, 1.f), qw));
+        for (int k = 0; k < 8; ++k) {
+            const int ch = tid + k * RS::T;  // chunk of two points
+            const int x = ch / (RS::N2 / 2), y = 2 * (ch % (RS::N2 / 2));
+            stage_async16(jst + x * FP::JP + y, src + x * RS::N2 + y);
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+    if ((int)blockIdx.x < n0) issue_J(blockIdx.x);
+
+    for (int iw = blockIdx.x; iw < n0; iw += gridDim.x) {
+        const size_t base = (size_t)iw * RS::S;
+        // The twiddles and thread coordinates are the same for every slice; taking the thread index
+        // and the table address through asm here keeps the compiler from hoisting them out of the
+        // slice loop into registers.
+        int tl;
+        const float2* twl;
+        asm volatile("mov.u32 %0, %%tid.x;" : "=r"(tl));
+        asm volatile("mov.b64 %0, %1;" : "=l"(twl) : "l"(tw));
+        const TwGlobal twg{twl, twLog};
+        const RegCoords<RS> c(xb, tl, true);
+        // ring position of this thread: thread order; the pair (ky even, ky + 1) are adjacent lanes
+        const int rpos = tl;
+        const bool copier = (c.ky & 1) == 0;
+        float2 w[16], v[16];
+
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        __syncthreads();
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v[m] = jst[c.x * FP::JP + c.jr + RS::R2 * m];
+        __syncthreads();  // staging buffer free: operand ring
+
+        auto issue = [&](int r) {
+            if (r < 16 && copier) {
+                const size_t idx = base + col_elem(c, r);  // even ky: idx, idx + 1 are 16-byte aligned
+                float2* slot = jst + (r % FP::NSLOT) * FP::SLOT + rpos;
+                stage_async16(slot, opv.K + idx);
+                if (need_qi) stage_async16(slot + RS::T, qi + idx);
+                if (need_qf) stage_async16(slot + 2 * RS::T, qf + idx);
+            }
+            asm volatile("cp.async.commit_group;\n" ::: "memory");  // empty groups keep the count uniform
+        };
+#pragma unroll
+        for (int r = 0; r < FP::NSLOT; ++r) issue(r);
+
+        reg_n2m_h<RS::R2, LN2, false>(v, w, c.exr, c.jr, twg, c.rsync);
+        rows_to_cols_h<RS>(w, v, xb, c);
+        reg_n2m_h<RS::R1, LN1, false>(v, w, c.exc, c.ic, twg, c.csync);
+
+        const float cond = (iw < 4) ? 0.f : 1.f;
+        const float2 kgw = opv.kg[iw];
+        // Two registers per trip, then the register array rotates by two, so the loop body exists
+        // once in the code rather than sixteen times (the fully unrolled form thrashed the
+        // instruction cache); after eight trips w is back in order.
+#pragma unroll 1
+        for (int r0 = 0; r0 < 16; r0 += 2) {
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                const int r = r0 + d;
+                asm volatile("cp.async.wait_group %0;\n" ::"n"(FP::NSLOT - 1) : "memory");
+                __syncwarp(FP::WMASK);  // the copying lane's data is visible to its neighbour
+                const size_t idx = base + col_elem(c, r);
+                const float2* slot = jst + (r % FP::NSLOT) * FP::SLOT + rpos;
+                const float2 K = slot[0];
+                const float2 qiv = need_qi ? slot[RS::T] : make_float2(0.f, 0.f);
+                const float2 qfv = need_qf ? slot[2 * RS::T] : make_float2(0.f, 0.f);
+                OpPoint o;
+                o.Khi = K.x;
+                o.Klo = K.y;
+                o.kzr = (K.x - kgw.x) + (K.y - kgw.y);
+                o.kzi = opv.ki ? opv.ki[idx] : 0.f;
+                // S and the RK stage (the arithmetic of spec_update, on staged values)
+                const float2 f = propagator_factor(o, pr, -1.f);
+                const float2 sv = cscale(cmul_i(cmul(f, w[d])), 0.5f / o.kzr);
+                float2 qw;
+                if (mode == SPEC_STAGE1) {
+                    qf[idx] = cadd(qiv, cscale(sv, Cs));
+                    qw = cscale(cadd(qiv, cscale(sv, Ce)), cond);
+                } else if (mode == SPEC_STAGE23) {
+                    qf[idx] = cadd(qfv, cscale(sv, Cs));
+                    qw = cscale(cadd(qiv, cscale(sv, Ce)), cond);
+                } else {
+                    qw = cscale(cadd(qfv, cscale(sv, Cs)), cond);
+                    qi_out[idx] = qw;
+                }
+                w[d] = cmul(op_ikz(o), cmul(propagator_factor(o, pn, 1.f), qw));
+                __syncwarp(FP::WMASK);  // both lanes of the pair have read the slot before it is refilled
+                issue(r + FP::NSLOT);
+            }
+            const float2 t0 = w[0], t1 = w[1];
+#pragma unroll
+            for (int i = 0; i < 14; ++i) w[i] = w[i + 2];
+            w[14] = t0;
+            w[15] = t1;
+        }
+        __syncthreads();  // every ring slot has been read: the staging buffer takes the next current
+        if (iw + (int)gridDim.x < n0) issue_J(iw + gridDim.x);
+
+        reg_m2n_h<RS::R1, LN1, true>(w, v, c.exc, c.ic, twg, c.csync);
+        cols_to_rows_h<RS>(v, w, xb, c);
+        reg_m2n_h<RS::R2, LN2, true>(w, v, c.exr, c.jr, twg, c.rsync);
+        float2* dst = E + base + (size_t)c.x * RS::N2 + c.jr;
+        constexpr float scale = 1.0f / (float)RS::S;
+#pragma unroll
+        for (int m = 0; m < 16; ++m) dst[RS::R2 * m] = cscale(v[m], scale);
     }
-    slice_inv_to_rows<RS, LN1, LN2, true>(w, v, sm, c, twg);
-    float2* dst = E + base + (size_t)c.x * RS::N2 + c.jr;
-    constexpr float scale = 1.0f / (float)RS::S;
-#pragma unroll
-    for (int m = 0; m < 16; ++m) dst[RS::R2 * m] = cscale(v[m], scale);
 }
 
 // Inverse transverse transform (modes of k_real_cart): E = IFFT2(i kz e^{..} q), the finish form
@@ -283,7 +605,7 @@ __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     const int tid = threadIdx.x, iw = blockIdx.x;
     const size_t base = (size_t)iw * RS::S;
     const TwGlobal twg{tw, twLog};
-    const RegCoords<RS> c(sm, tid);
+    const RegCoords<RS> c(sm, tid, false);
     const PhaseArgs pa{z.zhi, z.zlo, z.plain};
     const float2 kgw = opv.kg[iw];
     const float cond = (iw < 4) ? 0.f : 1.f;
@@ -331,7 +653,7 @@ __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     const int tid = threadIdx.x, iw = blockIdx.x;
     const size_t base = (size_t)iw * RS::S;
     const TwGlobal twg{tw, twLog};
-    const RegCoords<RS> c(sm, tid);
+    const RegCoords<RS> c(sm, tid, false);
     float2 w[16];
     slice_fwd_from_global<RS, LN1, LN2, false>(src + base, w, sm, c, twg);
     const PhaseArgs pa{z.zhi, z.zlo, z.plain};
@@ -356,7 +678,7 @@ __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     const int tid = threadIdx.x, iw = blockIdx.x;
     const size_t base = (size_t)iw * RS::S;
     const TwGlobal twg{tw, twLog};
-    const RegCoords<RS> c(sm, tid);
+    const RegCoords<RS> c(sm, tid, false);
     const PhaseArgs pa{z.zhi, z.zlo, z.plain};
     const float2 kgw = opv.kg[iw];
     float2 w[16], v[16];

@@ -5,13 +5,13 @@ template <int LN1, int LN2>
 struct FusedReg {
     static cudaError_t configure() {
         return cudaFuncSetAttribute(k_fused_reg<LN1, LN2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    RegSlice<LN1, LN2>::SMEM);
+                                    FusedPlan<LN1, LN2>::SMEM);
     }
     static cudaError_t run(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
         using RS = RegSlice<LN1, LN2>;
-        k_fused_reg<LN1, LN2><<<h->N0, RS::T, RS::SMEM, h->stream>>>(mode, h->J, uppe_op_view(h), h->qi, h->qf, h->qi,
-                                                                     h->E, Cs, Ce, h->tw, h->twLog, z_rhs, z_next,
-                                                                     h->num_sms);
+        const int grid = h->N0 < h->num_sms ? h->N0 : h->num_sms;  // persistent: one CTA per multiprocessor
+        k_fused_reg<LN1, LN2><<<grid, RS::T, FusedPlan<LN1, LN2>::SMEM, h->stream>>>(
+            mode, h->J, uppe_op_view(h), h->qi, h->qf, h->qi, h->E, Cs, Ce, h->tw, h->twLog, z_rhs, z_next, h->N0);
         return cudaGetLastError();
     }
 };
