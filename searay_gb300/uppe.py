@@ -16,7 +16,7 @@ import logging
 import numpy as np
 import torch
 
-from . import _native
+from . import _native, raywave
 from .grid import VolumeGrid, cell_centers, cell_walls
 from .ionization import RateCoefficients
 
@@ -255,9 +255,11 @@ def track(cl, xp, eikonal, vg, vol_dict):
     """Propagate the UPPE volume's wave through its diagnostic planes (uppe_kernel.py:333-424).
 
     :param cl: ignored (the reference's OpenCL bundle); the device is CUDA device 0 / current.
-    :param numpy.array xp: ray phase space (bundles, rays, 8), only used by the ray relaunch.
-    :param numpy.array eikonal: ray eikonal data (bundles, 4).
-    :param numpy.array vg: ray group velocity (bundles, rays, 4).
+    :param numpy.array xp: ray phase space (bundles, rays, 8).  Without an ``incoming wave`` the
+        primary rays give the field on the first plane; at the end the rays are relaunched from the
+        last plane (modified in place).  May be None with an ``incoming wave`` (no relaunch).
+    :param numpy.array eikonal: ray eikonal data (bundles, 4), modified in place.
+    :param numpy.array vg: ray group velocity (bundles, rays, 4), modified in place.
     :param dict vol_dict: the volume's input dictionary.
     :returns: A, J, chiNL, ne (complex128, shape ``wave grid``) and dom4d (8,)."""
     band = vol_dict["frequency band"]
@@ -275,11 +277,14 @@ def track(cl, xp, eikonal, vg, vol_dict):
     chi3 = vol_dict.get("chi3", 0.0)
 
     grid = VolumeGrid(vol_dict)
+    field_grid = raywave.FieldGrid(grid)
     if "incoming wave" not in vol_dict:
-        raise NotImplementedError("UPPE start from ray data (GetBoundaryFields) is not built; "
-                                  "give the volume an 'incoming wave'")
-    logging.info("Start UPPE propagation using wave data")
-    A[..., 0] = vol_dict["incoming wave"](grid.w, grid.x1, grid.x2)
+        logging.info("Start UPPE propagation using ray data.")
+        logging.warning("Polarization information is lost upon entering UPPE region.")
+        A[..., 0] = raywave.boundary_fields(field_grid, xp[:, 0, :], eikonal, 1)
+    else:
+        logging.info("Start UPPE propagation using wave data")
+        A[..., 0] = vol_dict["incoming wave"](grid.w, grid.x1, grid.x2)
 
     chi = vol_dict["dispersion inside"].chi(grid.w).astype(np.cdouble)
     rates = None
@@ -313,4 +318,8 @@ def track(cl, xp, eikonal, vg, vol_dict):
             a_dev, outs = A0, (dev.empty_field(), J0, c0, n0)
     finally:
         dev.close()
+    # relaunch the rays from the last plane (uppe_kernel.py:420-423)
+    if xp is not None:
+        relaunch = raywave.relaunch_rays_full if vol_dict.get("full relaunch", False) else raywave.relaunch_rays
+        relaunch(field_grid, xp, eikonal, vg, A[..., -1], size[3], vol_dict["dispersion inside"])
     return A, J, chiNL, ne, dom4d
