@@ -138,8 +138,10 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
         return UPPE_E_ARG;
     }
     const long S = (long)c.n1 * c.n2;
-    if (!c.cylindrical && (S < 16 || S > 16384)) {
-        uppe_set_error(nullptr, "Cartesian slice of %ld points outside the supported 16..16384 (128x128)", S);
+    if (!c.cylindrical && (S < 16 || (S > 16384 && !big_slice_supported(c.n1, c.n2)))) {
+        uppe_set_error(nullptr,
+                       "Cartesian slice %d x %d outside the supported 16 points .. 128 x 128, 128 x 256, 256 x 128 "
+                       "and 256 x 256", c.n1, c.n2);
         return UPPE_E_ARG;
     }
     if (c.cylindrical && (c.radial_modes < 1 || c.radial_modes > c.n1)) {
@@ -183,6 +185,7 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     }
     // Cartesian slices of 16..128 points per axis use the register-resident transforms;
     // SEARAY_UPPE_SLICE=generic selects the shared-memory Stockham form for them as well
+    h->slice_big = !c.cylindrical && big_slice_supported(c.n1, c.n2);
     h->slice_reg = !c.cylindrical && reg_slice_supported(c.n1, c.n2);
     if (const char* v = getenv("SEARAY_UPPE_SLICE")) {
         if (strcmp(v, "generic") == 0) h->slice_reg = 0;

@@ -1,0 +1,268 @@
+// Cartesian passes for slices larger than one CTA's shared memory holds (more than 128 x 128 points,
+// up to 256 x 256): the 2D transform is split into a row pass and a column pass through HBM.
+//
+//   row pass:    batched 1D FFT of every row (N2 points, the contiguous axis) of every slice,
+//                forward (natural -> natural) or inverse (+ optional 1/S scale and the finish outputs);
+//   column pass: one CTA per (slice, tile of 16 columns): the column FFT (N1 points) of each column
+//                of the tile, the pointwise work of the pass (RK stage, propagator phase, i kz, the
+//                adjoint factors), and/or the inverse column FFT.
+//
+// Both use the register-resident line transforms of slice_reg.cuh (16 values per thread, a 16-point
+// DFT in registers, the line's R = N/16 threads exchange through shared memory).  In the column
+// pass a warp holds 16 consecutive columns and two line lanes, so its global accesses are 128-byte
+// row segments; a column's lines span several warps and meet at the CTA barrier.
+//
+// Sources and destinations may be the same buffer (each CTA owns its rows or columns whole).
+// A fused evaluation tail is rows(J -> J), columns(J -> J, RK stage), rows^-1(J -> E): three
+// launches in place in J (J is consumed by the evaluation).  The same contracts as the one-kernel
+// slice passes (uppe_kernels.cu, slice_reg.cuh) hold for every mode.
+#include <math.h>
+
+#include "slice_reg.cuh"
+
+template <int LN2, bool INV>
+__global__ void __launch_bounds__(256)
+    k_rows_big(const float2* src, float2* dst, float scale, int finish, float2* __restrict__ A_out, OpView opv,
+               int N1, const float2* __restrict__ tw, int twLog) {
+    constexpr int N2 = 1 << LN2, R2 = N2 / 16, ROWS = 256 / R2;
+    __shared__ float2 xb[8 * 544];
+    const int tid = threadIdx.x;
+    const size_t row = (size_t)blockIdx.x * ROWS + tid / R2;
+    const int j = tid % R2;
+    float2* ex = xb + (tid >> 5) * 544 + ((tid & 31) / R2) * 17 * R2;
+    const LineSync<false> sync{0, 0};
+    const TwGlobal twg{tw, twLog};
+    const float2* s = src + row * N2;
+    float2* d = dst + row * N2;
+    float2 v[16], w[16];
+    if constexpr (!INV) {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v[m] = s[j + R2 * m];
+        reg_n2m<R2, LN2, false>(v, w, ex, j, twg, sync);
+#pragma unroll
+        for (int r = 0; r < 16; ++r) d[j + R2 * (r / R2) + 16 * (r % R2)] = cscale(w[r], scale);
+    } else {
+#pragma unroll
+        for (int r = 0; r < 16; ++r) w[r] = s[j + R2 * (r / R2) + 16 * (r % R2)];
+        reg_m2n<R2, LN2, true>(w, v, ex, j, twg, sync);
+        if (!finish) {
+#pragma unroll
+            for (int m = 0; m < 16; ++m) d[j + R2 * m] = cscale(v[m], scale);
+        } else {
+            // finish: A = IFFT2(e^{..} q), E = i kz A at the same point (uppe_kernel.py:250-253)
+            const float2 kgw = opv.kg[row / N1];
+#pragma unroll
+            for (int m = 0; m < 16; ++m) {
+                const size_t idx = row * N2 + j + R2 * m;
+                const float2 val = cscale(v[m], scale);
+                if (A_out) A_out[idx] = val;
+                d[j + R2 * m] = cmul(op_ikz(op_at(opv, idx, kgw)), val);
+            }
+        }
+    }
+}
+
+enum BigColKind {
+    BC_FUSED = 0,    // forward column FFT, RK stage (SPEC_STAGE1/STAGE23/FINISH), next phase, inverse column FFT
+    BC_SPEC = 1,     // forward column FFT, spectral update (SPEC_* modes)
+    BC_REAL = 2,     // pointwise from q (REAL_* modes), inverse column FFT
+    BC_ADJ_IN = 3,   // ADJ_S / ADJ_LOAD pointwise, inverse column FFT (unnormalised)
+    BC_ADJ_FWD = 4,  // forward column FFT, ADJ_E / ADJ_FIN pointwise with 1/S
+};
+
+struct BigColArgs {
+    int kind, mode;
+    const float2* src;
+    float2* dst;
+    float2 *q_out, *qf;
+    const float2 *qi, *k1;
+    float Cs, Ce;
+    StepArgs z0, z1;
+};
+
+template <int LN1, int LN2>
+__global__ void __launch_bounds__(16 << (LN1 - 4)) k_cols_big(BigColArgs a, OpView opv, const float2* __restrict__ tw,
+                                                              int twLog) {
+    constexpr int N1 = 1 << LN1, N2 = 1 << LN2, R1 = N1 / 16, T = 16 * R1, TILES = N2 / 16;
+    constexpr int QC = 17 * R1 + 1;
+    __shared__ float2 xb[16 * QC];
+    const int tid = threadIdx.x;
+    const int iw = blockIdx.x / TILES;
+    const int c = tid & 15, i = tid >> 4;
+    const int ky = (blockIdx.x % TILES) * 16 + c;
+    const size_t base = (size_t)iw * N1 * N2;
+    float2* ex = xb + c * QC;
+    const LineSync<true> sync{0, T};
+    const TwGlobal twg{tw, twLog};
+    const PhaseArgs p0{a.z0.zhi, a.z0.zlo, a.z0.plain};
+    const PhaseArgs p1{a.z1.zhi, a.z1.zlo, a.z1.plain};
+    const float cond = (iw < 4) ? 0.f : 1.f;
+    const float2 kgw = opv.kg[iw];
+    const int kind = a.kind, mode = a.mode;
+    float2 v[16], w[16];
+
+    if (kind == BC_FUSED || kind == BC_SPEC || kind == BC_ADJ_FWD) {
+#pragma unroll
+        for (int m = 0; m < 16; ++m) v[m] = a.src[base + (size_t)(i + R1 * m) * N2 + ky];
+        reg_n2m<R1, LN1, false>(v, w, ex, i, twg, sync);
+    }
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const int kx = i + R1 * (r / R1) + 16 * (r % R1);
+        const size_t idx = base + (size_t)kx * N2 + ky;
+        if (kind == BC_FUSED) {
+            const OpPoint o = op_at(opv, idx, kgw);
+            const float2 qw = spec_update(mode, idx, w[r], o, cond, a.q_out, a.qf, a.qi, a.Cs, a.Ce, p0,
+                                          mode == SPEC_FINISH);
+            w[r] = cmul(op_ikz(o), cmul(propagator_factor(o, p1, 1.f), qw));
+        } else if (kind == BC_SPEC) {
+            OpPoint o;
+            if (mode != SPEC_LOAD) o = op_at(opv, idx, kgw);
+            spec_update(mode, idx, w[r], o, cond, a.q_out, a.qf, a.qi, a.Cs, a.Ce, p0, true);
+        } else if (kind == BC_REAL) {
+            const OpPoint o = op_at(opv, idx, kgw);
+            float2 val;
+            if (mode == REAL_APPLY1) {
+                const float2 q0 = a.qi[idx], s = a.k1[idx];
+                a.qf[idx] = cadd(q0, cscale(s, a.Cs));
+                val = cscale(cadd(q0, cscale(s, a.Ce)), cond);
+            } else {
+                val = a.src[idx];
+            }
+            val = cmul(propagator_factor(o, p0, 1.f), val);
+            if (mode != REAL_FINISH) val = cmul(op_ikz(o), val);
+            w[r] = val;
+        } else if (kind == BC_ADJ_IN) {
+            float2 val = a.src[idx];
+            if (mode == ADJ_S) {
+                const OpPoint o = op_at(opv, idx, kgw);
+                const float2 f = cconj(propagator_factor(o, p0, -1.f));
+                val = cscale(cmul_mi(cmul(f, val)), 0.5f / o.kzr);
+            }
+            w[r] = val;
+        } else {  // BC_ADJ_FWD
+            const OpPoint o = op_at(opv, idx, kgw);
+            float2 val = cmul(cconj(propagator_factor(o, p0, 1.f)), cscale(w[r], 1.0f / (float)(N1 * N2)));
+            if (mode == ADJ_E) val = cmul(cconj(op_ikz(o)), val);
+            a.dst[idx] = val;
+        }
+    }
+    if (kind == BC_FUSED || kind == BC_REAL || kind == BC_ADJ_IN) {
+        reg_m2n<R1, LN1, true>(w, v, ex, i, twg, sync);
+#pragma unroll
+        for (int m = 0; m < 16; ++m) a.dst[base + (size_t)(i + R1 * m) * N2 + ky] = v[m];
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// Launch helpers
+// ---------------------------------------------------------------------------------------------
+bool big_slice_supported(int N1, int N2) {
+    auto ok = [](int n) { return n == 128 || n == 256; };
+    return ok(N1) && ok(N2) && N1 * N2 > 16384;
+}
+
+template <bool INV>
+static cudaError_t rows(UppeHandle* h, const float2* src, float2* dst, float scale, int finish, float2* A_out) {
+    const size_t nrows = (size_t)h->N0 * h->N1;
+    h->launches++;
+    const OpView opv = uppe_op_view(h);
+    if (h->N2 == 256) {
+        k_rows_big<8, INV><<<(unsigned)(nrows / 16), 256, 0, h->stream>>>(src, dst, scale, finish, A_out, opv, h->N1,
+                                                                         h->tw, h->twLog);
+    } else {
+        k_rows_big<7, INV><<<(unsigned)(nrows / 32), 256, 0, h->stream>>>(src, dst, scale, finish, A_out, opv, h->N1,
+                                                                         h->tw, h->twLog);
+    }
+    return cudaGetLastError();
+}
+
+static cudaError_t cols(UppeHandle* h, const BigColArgs& a) {
+    h->launches++;
+    const OpView opv = uppe_op_view(h);
+    const unsigned grid = (unsigned)(h->N0 * (h->N2 / 16));
+    if (h->N1 == 256 && h->N2 == 256)
+        k_cols_big<8, 8><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+    else if (h->N1 == 256)
+        k_cols_big<8, 7><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+    else
+        k_cols_big<7, 8><<<grid, 128, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
+    cudaError_t e = rows<false>(h, h->J, h->J, 1.f, 0, nullptr);
+    BigColArgs a{};
+    a.kind = BC_FUSED;
+    a.mode = mode;
+    a.src = h->J;
+    a.dst = h->J;
+    a.q_out = h->qi;
+    a.qf = h->qf;
+    a.qi = h->qi;
+    a.Cs = Cs;
+    a.Ce = Ce;
+    a.z0 = z_rhs;
+    a.z1 = z_next;
+    if (e == cudaSuccess) e = cols(h, a);
+    if (e == cudaSuccess) e = rows<true>(h, h->J, h->E, 1.0f / (float)h->S, 0, nullptr);
+    return e;
+}
+
+cudaError_t launch_real_big(UppeHandle* h, int mode, const float2* src, float2* A_out, const float2* k1, float2* qf,
+                            float Cs, float Ce, StepArgs z) {
+    BigColArgs a{};
+    a.kind = BC_REAL;
+    a.mode = mode;
+    a.src = src;
+    a.dst = h->E;
+    a.qi = src;
+    a.k1 = k1;
+    a.qf = qf;
+    a.Cs = Cs;
+    a.Ce = Ce;
+    a.z0 = z;
+    cudaError_t e = cols(h, a);
+    if (e == cudaSuccess) e = rows<true>(h, h->E, h->E, 1.0f / (float)h->S, mode == REAL_FINISH, A_out);
+    return e;
+}
+
+cudaError_t launch_spec_big(UppeHandle* h, int mode, const float2* src, float2* q_out, float2* qf, const float2* qi,
+                            float Cs, float Ce, StepArgs z) {
+    // the row transform goes to J when the source is J (consumed), else to E (then stale)
+    float2* tmp = (src == h->J) ? h->J : h->E;
+    if (tmp == h->E) h->E_valid = 0;
+    cudaError_t e = rows<false>(h, src, tmp, 1.f, 0, nullptr);
+    BigColArgs a{};
+    a.kind = BC_SPEC;
+    a.mode = mode;
+    a.src = tmp;
+    a.q_out = q_out;
+    a.qf = qf;
+    a.qi = qi;
+    a.Cs = Cs;
+    a.Ce = Ce;
+    a.z0 = z;
+    if (e == cudaSuccess) e = cols(h, a);
+    return e;
+}
+
+cudaError_t launch_adj_big(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z) {
+    BigColArgs a{};
+    a.mode = mode;
+    a.z0 = z;
+    if (mode == ADJ_S || mode == ADJ_LOAD) {
+        a.kind = BC_ADJ_IN;
+        a.src = in;
+        a.dst = out;
+        cudaError_t e = cols(h, a);
+        if (e == cudaSuccess) e = rows<true>(h, out, out, 1.f, 0, nullptr);
+        return e;
+    }
+    a.kind = BC_ADJ_FWD;
+    cudaError_t e = rows<false>(h, in, out, 1.f, 0, nullptr);
+    a.src = out;
+    a.dst = out;
+    if (e == cudaSuccess) e = cols(h, a);
+    return e;
+}

@@ -115,6 +115,15 @@ struct LineSync {
     }
 };
 
+// R-point DFT across the lanes of a line after the exchange (R = 2, 4, 8, 16)
+template <int R, bool INV>
+UPPE_DEV void dft_line(float2 (&u)[R]) {
+    if constexpr (R == 16)
+        dft16<INV>(u);
+    else
+        dft_small<R>(u, INV);
+}
+
 // natural -> mixed along one axis of length 16 R; `ex` is this line's exchange region, j the
 // thread's index within the line.  v[m] = x[j + R m]  ->  w[s R + b] = X[j + R s + 16 b].
 template <int R, int LOGN, bool INV, class SY>
@@ -133,7 +142,7 @@ UPPE_DEV void reg_n2m(float2 (&v)[16], float2 (&w)[16], float2* ex, int j, const
             float2 u[R];
 #pragma unroll
             for (int jj = 0; jj < R; ++jj) u[jj] = ex[jj * 17 + j + R * s];
-            dft_small<R>(u, INV);
+            dft_line<R, INV>(u);
 #pragma unroll
             for (int b = 0; b < R; ++b) w[s * R + b] = u[b];
         }
@@ -153,7 +162,7 @@ UPPE_DEV void reg_m2n(float2 (&w)[16], float2 (&v)[16], float2* ex, int j, const
             float2 u[R];
 #pragma unroll
             for (int b = 0; b < R; ++b) u[b] = w[s * R + b];
-            dft_small<R>(u, INV);
+            dft_line<R, INV>(u);
             const int a = j + R * s;
 #pragma unroll
             for (int jj = 0; jj < R; ++jj) ex[jj * 17 + a] = u[jj];
@@ -302,7 +311,7 @@ UPPE_DEV void reg_n2m_h(float2 (&v)[16], float2 (&w)[16], float2* ex, int j, con
                 float2 u[R];
 #pragma unroll
                 for (int jj = 0; jj < R; ++jj) u[jj] = ex[jj * 9 + j + R * s - 8 * h];
-                dft_small<R>(u, INV);
+                dft_line<R, INV>(u);
 #pragma unroll
                 for (int b = 0; b < R; ++b) w[s * R + b] = u[b];
             }
@@ -324,7 +333,7 @@ UPPE_DEV void reg_m2n_h(float2 (&w)[16], float2 (&v)[16], float2* ex, int j, con
                 float2 u[R];
 #pragma unroll
                 for (int b = 0; b < R; ++b) u[b] = w[s * R + b];
-                dft_small<R>(u, INV);
+                dft_line<R, INV>(u);
                 const int a = j + R * s;
 #pragma unroll
                 for (int jj = 0; jj < R; ++jj) ex[jj * 9 + a - 8 * h] = u[jj];

@@ -50,6 +50,7 @@ struct UppeHandle {
     int time_spt;                  // time samples per thread in the time pass (16 or 32)
     int num_sms;                   // multiprocessors of the device
     int slice_reg;                 // Cartesian slices use the register-resident transforms (slice_reg.cuh)
+    int slice_big;                 // Cartesian slices above 128 x 128: row and column passes (slice_big.cu)
     cudaStream_t stream;
     // library-owned device buffers
     float2 *q, *qi, *qf, *k1, *E, *J, *scratch;
@@ -126,6 +127,15 @@ cudaError_t launch_real_reg(UppeHandle* h, int mode, const float2* src, float2* 
 cudaError_t launch_spec_reg(UppeHandle* h, int mode, const float2* src, float2* q_out, float2* qf, const float2* qi,
                             float Cs, float Ce, StepArgs z);
 cudaError_t launch_adj_reg(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z);
+
+// ---- Cartesian slices of 128 x 256, 256 x 128, 256 x 256 (slice_big.cu): row + column passes ----
+bool big_slice_supported(int N1, int N2);
+cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next);
+cudaError_t launch_real_big(UppeHandle* h, int mode, const float2* src, float2* A_out, const float2* k1, float2* qf,
+                            float Cs, float Ce, StepArgs z);
+cudaError_t launch_spec_big(UppeHandle* h, int mode, const float2* src, float2* q_out, float2* qf, const float2* qi,
+                            float Cs, float Ce, StepArgs z);
+cudaError_t launch_adj_big(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z);
 cudaError_t launch_adj_rk(UppeHandle* h, int mode, const float2* lam_out, float2* lam_in, float a_f, float a_mu);
 cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G, float2* gE, double* dred);
 cudaError_t uppe_configure_time_adj_kernel(size_t smem_bytes);

@@ -302,6 +302,7 @@ __global__ void __launch_bounds__(1024) k_adj_cart(int mode, const float2* __res
 }
 
 cudaError_t launch_adj_cart(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z) {
+    if (h->slice_big) return launch_adj_big(h, mode, in, out, z);
     if (h->slice_reg) return launch_adj_reg(h, mode, in, out, z);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
@@ -361,6 +362,7 @@ cudaError_t uppe_configure_slice_kernels(size_t smem_bytes) {
 static size_t slice_smem(const UppeHandle* h) { return (size_t)(h->S + h->N1) * sizeof(float2); }
 
 cudaError_t launch_real_cart(UppeHandle* h, int mode, const float2* src, float2* A_out, StepArgs z) {
+    if (h->slice_big) return launch_real_big(h, mode, src, A_out, nullptr, nullptr, 0.f, 0.f, z);
     if (h->slice_reg) return launch_real_reg(h, mode, src, A_out, nullptr, nullptr, 0.f, 0.f, z);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
@@ -371,6 +373,7 @@ cudaError_t launch_real_cart(UppeHandle* h, int mode, const float2* src, float2*
 }
 
 cudaError_t launch_apply1_cart(UppeHandle* h, float Cs, float Ce, StepArgs z) {
+    if (h->slice_big) return launch_real_big(h, REAL_APPLY1, h->qi, nullptr, h->k1, h->qf, Cs, Ce, z);
     if (h->slice_reg) return launch_real_reg(h, REAL_APPLY1, h->qi, nullptr, h->k1, h->qf, Cs, Ce, z);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
@@ -382,6 +385,7 @@ cudaError_t launch_apply1_cart(UppeHandle* h, float Cs, float Ce, StepArgs z) {
 
 cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, float2* q_out, float2* qf_io,
                              const float2* qi, float Cs, float Ce, StepArgs z) {
+    if (h->slice_big) return launch_spec_big(h, mode, src_real, q_out, qf_io, qi, Cs, Ce, z);
     if (h->slice_reg) return launch_spec_reg(h, mode, src_real, q_out, qf_io, qi, Cs, Ce, z);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
@@ -391,6 +395,7 @@ cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, fl
 }
 
 cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
+    if (h->slice_big) return launch_fused_big(h, mode, Cs, Ce, z_rhs, z_next);
     if (h->slice_reg) return launch_fused_reg(h, mode, Cs, Ce, z_rhs, z_next);
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;

@@ -14,6 +14,9 @@ with N0 = 2^n + 1 frequency nodes):
   at 5 critical powers, 8-mode seeded transverse phase (0.05 rad, numpy default_rng(0)), Kerr
   (n2 = 3e-19 cm^2/W) + O2 tunneling ionization (PPT, Ip = 12.07 eV, Z = 0.53) at 5.4e18 cm^-3 +
   plasma current, 400 RK4 steps over 10 cm.
+* ``cart_filament_256``: Cartesian 256 x 256 over 3 mm, N0 = 1025 (band 0-4 w0), 800 nm 40 fs pulse at
+  10 critical powers, the 8-mode seeded transverse phase of ``cart_filament_128`` (scaled to the
+  box), the same medium, 1000 RK4 steps over 10 cm.
 * ``cyl_adjoint_256``: the physics of ``cyl_kerr_64`` on N0 = 1025 (Nt = 2048, band 0-6.9 w0),
   Nr = Nk = 256, 200 RK4 steps over 10 cm; the forward + adjoint workload.
 * ``cyl_silica_512``: cylindrical Nr = Nk = 512 over R = 0.5 mm, N0 = 2049, 1 um 100 fs pulse at
@@ -162,6 +165,31 @@ def cart_filament_128(steps=400, n_perp=128):
     return vd
 
 
+def cart_filament_256(steps=1000):
+    x1 = 0.8e-6 / (2 * np.pi)
+    u = Units(x1)
+    air = dispersion.SimpleAir(x1)
+    n2 = 3e-23
+    r0 = u.mm(0.3)
+    P = 10 * critical_power_W(0.8e-6, 1.0, n2)
+    I0 = 2 * P / (np.pi * (0.3e-3) ** 2) * 1e-4  # W/cm^2
+    E0 = field_from_intensity(u, I0)
+    L = u.cm(10.0)
+    box = u.mm(3.0)
+    vd = {
+        "wave grid": (1025, 256, 256, 2), "wave coordinates": "cartesian",
+        "frequency band": (0.0, 4.0), "nonlinear band": (0.0, 3.5),
+        "size": (box, box, L), "subcycles": steps, "minimum step": L / steps,
+        "chi3": u.chi3(1.0, n2), "density reference": u.cm3(5.4e18),
+        "window speed": air.GroupVelocityMagnitude(1.0),
+        "dispersion inside": air,
+        "ionizer": ionization.PPT_Tunneling(x1, False, u.eV(12.07), 0.53),
+        "density lambda": lambda x, y, z, r2: np.ones(x.shape),
+        "incoming wave": gaussian_pulse(E0, u.fs(40.0), r0, screen=seeded_phase_screen(8, 0.05, box, 0)),
+    }
+    return vd
+
+
 def cyl_silica_512(steps=100):
     x1 = 1.0e-6 / (2 * np.pi)
     u = Units(x1)
@@ -194,5 +222,5 @@ def cyl_adjoint_256(steps=200):
     return vd
 
 
-WORKLOADS = {"cyl_kerr_64": cyl_kerr_64, "cart_filament_128": cart_filament_128, "cyl_silica_512": cyl_silica_512,
-             "cyl_adjoint_256": cyl_adjoint_256}
+WORKLOADS = {"cyl_kerr_64": cyl_kerr_64, "cart_filament_128": cart_filament_128, "cart_filament_256": cart_filament_256,
+             "cyl_silica_512": cyl_silica_512, "cyl_adjoint_256": cyl_adjoint_256}
