@@ -182,3 +182,90 @@ UPPE_DEV void fft_axis(float2* buf, int logN, int lognb, int bs, int es, const f
                        bool inv, int tid, int nthr) {
     fft_axis_tw<ET>(buf, logN, lognb, bs, es, TwGlobal{tw, twLog}, inv, tid, nthr);
 }
+
+// ---------------------------------------------------------------------------------------------
+// Compile-time form for batch-fast data (element e of transform b at buf[b + e * NB], NB = 2^LOGNB
+// transforms of 2^LOGN points, NB * N / ET threads): every stride, offset and twiddle shift is a
+// constant, so a stage is its loads, twiddles, butterfly and stores.  Twiddles from a shared
+// half table of 2^(TWLOG-1) entries of exp(-2 pi i j / 2^TWLOG).
+// ---------------------------------------------------------------------------------------------
+template <int TWLOG>
+struct TwHalfSharedCT {
+    const float2* p;
+    UPPE_DEV float2 get(int j) const {
+        constexpr int half = 1 << (TWLOG - 1);
+        const float2 v = p[j & (half - 1)];
+        return (j & half) ? make_float2(-v.x, -v.y) : v;
+    }
+};
+
+template <int R, int ITEMS, int LOGN, int LOGP, int LOGNB, int TWLOG>
+UPPE_DEV void stockham_stage_ct(float2* buf, const TwHalfSharedCT<TWLOG>& tw, bool inv, int tid) {
+    constexpr int LOGR = (R == 2) ? 1 : (R == 4) ? 2 : 3;
+    constexpr int NQ = 1 << (LOGN - LOGR), P = 1 << LOGP, NB = 1 << LOGNB;
+    constexpr int NTHR = (NB << LOGN) / (R * ITEMS);
+    constexpr int SH = TWLOG - LOGP - LOGR;
+    float2 u[ITEMS][R];
+    int dst[ITEMS];
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+        const int g = tid + it * NTHR;
+        const int b = g & (NB - 1);
+        const int i = g >> LOGNB;
+        const int k = i & (P - 1);
+        const float2* src = buf + b + i * NB;
+#pragma unroll
+        for (int r = 0; r < R; ++r) u[it][r] = src[r * NQ * NB];
+        if constexpr (LOGP > 0) {
+            if constexpr (R == 8) {
+                float2 w1 = tw.get(k << SH), w2 = tw.get((2 * k) << SH), w4 = tw.get((4 * k) << SH);
+                if (inv) {
+                    w1.y = -w1.y;
+                    w2.y = -w2.y;
+                    w4.y = -w4.y;
+                }
+                const float2 w3 = cmul(w1, w2);
+                u[it][1] = cmul(u[it][1], w1);
+                u[it][2] = cmul(u[it][2], w2);
+                u[it][3] = cmul(u[it][3], w3);
+                u[it][4] = cmul(u[it][4], w4);
+                u[it][5] = cmul(u[it][5], cmul(w4, w1));
+                u[it][6] = cmul(u[it][6], cmul(w4, w2));
+                u[it][7] = cmul(u[it][7], cmul(w4, w3));
+            } else {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    float2 w = tw.get((r * k) << SH);
+                    if (inv) w.y = -w.y;
+                    u[it][r] = cmul(u[it][r], w);
+                }
+            }
+        }
+        dft_small<R>(u[it], inv);
+        dst[it] = b + (((i - k) << LOGR) + k) * NB;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int it = 0; it < ITEMS; ++it) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) buf[dst[it] + r * P * NB] = u[it][r];
+    }
+    __syncthreads();
+}
+
+template <int ET, int LOGN, int LOGNB, int TWLOG, int LOGP = 0>
+UPPE_DEV void fft_axis_ct(float2* buf, const TwHalfSharedCT<TWLOG>& tw, bool inv, int tid) {
+    if constexpr (LOGP < LOGN) {
+        constexpr int REM = LOGN - LOGP;
+        if constexpr (ET >= 8 && REM >= 3) {
+            stockham_stage_ct<8, ET / 8, LOGN, LOGP, LOGNB, TWLOG>(buf, tw, inv, tid);
+            fft_axis_ct<ET, LOGN, LOGNB, TWLOG, LOGP + 3>(buf, tw, inv, tid);
+        } else if constexpr (ET >= 4 && REM >= 2) {
+            stockham_stage_ct<4, ET / 4, LOGN, LOGP, LOGNB, TWLOG>(buf, tw, inv, tid);
+            fft_axis_ct<ET, LOGN, LOGNB, TWLOG, LOGP + 2>(buf, tw, inv, tid);
+        } else {
+            stockham_stage_ct<2, ET / 2, LOGN, LOGP, LOGNB, TWLOG>(buf, tw, inv, tid);
+            fft_axis_ct<ET, LOGN, LOGNB, TWLOG, LOGP + 1>(buf, tw, inv, tid);
+        }
+    }
+}

@@ -12,8 +12,8 @@
 //      uppe_kernel.py:169); P and Jpl are written back packed as even/odd pairs, in place,
 //   3. two M-point forward FFTs (P, then Jpl), split into the real spectra and
 //      J = -i w P + Jpl / (0.1 - i w), times the NL filter (fft.cl:282-329, uppe_kernel.py:171-186).
-// The density sum is a two-pass blocked scan: every thread sums its own 32 consecutive samples,
-// then adds the totals of all later segments of its column (the sum runs from high to low t).
+// The density sum is a two-pass blocked scan: every thread sums its own consecutive samples, then
+// adds the totals of all later segments of its column (the sum runs from high to low t).
 // The sums are float-float in the mixed form.
 #include <math.h>
 
@@ -110,7 +110,9 @@ __device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
 }
 
 // ET: complex FFT elements per thread (16: 256 threads for C*Nt = 8192; 8: 512 threads)
-template <int ET>
+// LOGM > 0: compile-time sizes M = 2^LOGM, C = 2^LOGC (constant-folded index arithmetic and the
+// compile-time Stockham transforms); LOGM = 0: sizes from the parameters.
+template <int ET, int LOGM = 0, int LOGC = -1>
 __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : 2) k_time(int mode, const float2* __restrict__ E, float2* __restrict__ out0,
                                                   float2* __restrict__ out1, const float* __restrict__ ng,
                                                   const float* __restrict__ wv, const float* __restrict__ filt,
@@ -120,11 +122,13 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : 2) k_time
     // for j < Nt/2, one float-float segment total per thread.  Rows of C float2 keep the
     // column-batched FFT accesses of a warp on distinct banks.
     extern __shared__ float2 Zp[];
-    const int C = tp.C, logC = tp.logC, Nt = tp.Nt, M = tp.M, S = tp.S;
+    constexpr bool CT = LOGM > 0;
+    const int C = CT ? (1 << LOGC) : tp.C, logC = CT ? LOGC : tp.logC;
+    const int Nt = CT ? (2 << LOGM) : tp.Nt, M = CT ? (1 << LOGM) : tp.M, S = tp.S;
     float2* Zj = Zp + (size_t)(M + 1) * C;
     float2* twl = Zj + (size_t)(M + 1) * C;
     ffloat* tot = reinterpret_cast<ffloat*>(twl + (Nt >> 1));
-    const int tid = threadIdx.x, T = blockDim.x;
+    const int tid = threadIdx.x, T = CT ? ((2 << LOGM) << LOGC) / (2 * ET) : (int)blockDim.x;
     const size_t col0 = (size_t)blockIdx.x * C;
     const bool ionize = tp.rate_form != UPPE_RATE_NONE;
     const TwHalfShared tws{twl, tp.logNt};
@@ -169,7 +173,10 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : 2) k_time
         }
     }
     __syncthreads();
-    fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
+    if constexpr (CT)
+        fft_axis_ct<ET, LOGM, LOGC, LOGM + 1>(Zp, TwHalfSharedCT<LOGM + 1>{twl}, true, tid);
+    else
+        fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
 
     // ---- 2. sources, in place ----
     const int c = tid & (C - 1);
@@ -181,9 +188,9 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : 2) k_time
     const float kerr = ngc * tp.redchi3;
     const float inv = tp.inv_nt;
     float r_next = 0.f;
+    ffloat part = {0.f, 0.f};
     if (ionize) {
         if (t1 <= Nt - 2) r_next = ion_rate(tp, Zp[(t1 >> 1) * C + c].x * inv);
-        ffloat part = {0.f, 0.f};
         float rn = r_next;
         for (int m = m0 + mps - 1; m >= m0; --m) {
             const float2 zv = Zp[m * C + c];
@@ -195,19 +202,48 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : 2) k_time
             rn = r0;
             Zj[m * C + c] = make_float2(r0, r1);  // this thread's own slot, reused below
         }
-        tot[tid] = part;
     }
-    __syncthreads();  // all segment totals written; from here each thread touches only its own pairs
+    // Sum of the later segments of this column.  A warp holds 32/C consecutive segments of each of
+    // the C columns (lanes C apart): a shuffle suffix scan gives the sums within the warp, and the
+    // warps' column totals, published in shared memory, the sums beyond it.
     ffloat Sacc = {0.f, 0.f};
-    if (ionize) {
-        const int nseg = T >> logC;
-        for (int s2 = seg + 1; s2 < nseg; ++s2) {
+    if (ionize && T < 32) {  // a block smaller than a warp (17 frequencies, under 16 points): sequential
+        tot[tid] = part;
+        __syncthreads();
+        for (int s2 = seg + 1; s2 < (T >> logC); ++s2) {
             const ffloat v = tot[(s2 << logC) + c];
             if (tp.plain)
                 Sacc.hi += v.hi;
             else
                 Sacc = ff_add(Sacc, v);
         }
+    } else if (ionize) {
+        const int lane = tid & 31, warp = tid >> 5, nwarps = T >> 5;
+        ffloat incl = part;
+        for (int d = C; d < 32; d <<= 1) {
+            const float hi = __shfl_down_sync(0xffffffffu, incl.hi, d);
+            const float lo = __shfl_down_sync(0xffffffffu, incl.lo, d);
+            if (lane + d < 32) {
+                if (tp.plain)
+                    incl.hi += hi;
+                else
+                    incl = ff_add(incl, ffloat{hi, lo});
+            }
+        }
+        Sacc.hi = __shfl_down_sync(0xffffffffu, incl.hi, C);
+        Sacc.lo = __shfl_down_sync(0xffffffffu, incl.lo, C);
+        if (lane + C >= 32) Sacc = ffloat{0.f, 0.f};
+        if (lane < C) tot[warp * C + lane] = incl;  // this warp's total of column `lane`
+        __syncthreads();
+        for (int w2 = warp + 1; w2 < nwarps; ++w2) {
+            const ffloat v = tot[w2 * C + c];
+            if (tp.plain)
+                Sacc.hi += v.hi;
+            else
+                Sacc = ff_add(Sacc, v);
+        }
+    } else {
+        __syncthreads();  // pass 2 overwrites pairs that pass 1 of the previous segment read
     }
     {
         float rn = r_next;
@@ -241,8 +277,13 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : 2) k_time
 
     // ---- 3. forward FFTs (P, then Jpl) and the current ----
     const bool two = ionize || mode == TIME_CHI_NE;
-    fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, false, tid, T);
-    if (two) fft_axis_tw<ET>(Zj, tp.logM, logC, 1, C, tws, false, tid, T);
+    if constexpr (CT) {
+        fft_axis_ct<ET, LOGM, LOGC, LOGM + 1>(Zp, TwHalfSharedCT<LOGM + 1>{twl}, false, tid);
+        if (two) fft_axis_ct<ET, LOGM, LOGC, LOGM + 1>(Zj, TwHalfSharedCT<LOGM + 1>{twl}, false, tid);
+    } else {
+        fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, false, tid, T);
+        if (two) fft_axis_tw<ET>(Zj, tp.logM, logC, 1, C, tws, false, tid, T);
+    }
     for (int it = tid; it < (M + 1) * C; it += T) {
         const int cc = it & (C - 1);
         const int k = it >> logC;
@@ -266,9 +307,17 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : 2) k_time
     }
 }
 
+// The time-pass shapes with compile-time sizes: C Nt = 8192 with 16 samples per thread (512 threads),
+// M = 256 .. 2048.
+#define UPPE_TIME_CT(X) X(8, 4) X(9, 3) X(10, 2) X(11, 1)
+
 cudaError_t uppe_configure_time_kernel(size_t smem_bytes) {
     cudaError_t e = cudaFuncSetAttribute(k_time<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_time<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+#define UPPE_TIME_CONF(A_, B_) \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_time<8, A_, B_>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    UPPE_TIME_CT(UPPE_TIME_CONF)
+#undef UPPE_TIME_CONF
     return e;
 }
 
@@ -339,8 +388,18 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
     const size_t smem = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
     h->launches++;
     if (h->time_spt == 16)
+    {
+#define UPPE_TIME_CASE(A_, B_)                                                                                      \
+        if (tp.logM == A_ && tp.logC == B_) {                                                                          \
+            k_time<8, A_, B_><<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, \
+                                                                            h->tw, h->twLog, tp);                    \
+            return cudaGetLastError();                                                                             \
+        }
+        UPPE_TIME_CT(UPPE_TIME_CASE)
+#undef UPPE_TIME_CASE
         k_time<8><<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
                                                                h->twLog, tp);
+    }
     else
         k_time<16><<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
                                                                 h->twLog, tp);

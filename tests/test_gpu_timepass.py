@@ -1,0 +1,51 @@
+"""The time-axis pass at the frequency grids of the benchmark configurations (N0 = 257, 513, 1025,
+2049), where it runs with compile-time sizes (searay_gb300/csrc/timepass.cu): one fixed RK4 step and
+the finish against the FP64 oracle, on a 16 x 16 Cartesian grid with the filamentation medium and a
+pulse strong enough to ionize.  Bounds: the golden parity tolerances (field 2e-5; J, chi, ne 1e-4)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def cuda_ready():
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA GPU")
+    from searay_gb300 import build
+    build.build()
+
+
+def rel_err(x, ref):
+    return float(np.max(np.abs(x - ref)) / np.max(np.abs(ref)))
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp32"])
+@pytest.mark.parametrize("n0", [257, 513, 1025, 2049])
+def test_time_pass_rk4_step_vs_oracle(n0, precision):
+    import torch
+    from oracle import uppe_oracle as O
+    from searay_gb300 import grid, ionization, uppe, workloads
+    vd = workloads.cart_filament_128(steps=400, n_perp=16)
+    vd["wave grid"] = (n0, 16, 16, 2)
+    vd["frequency band"] = (0.0, 4.0 * (n0 - 1) / 512)
+    vd["nonlinear band"] = (0.0, 3.5 * (n0 - 1) / 512)
+    wave = vd["incoming wave"]
+    vd["incoming wave"] = lambda w, x1, x2: 3.0 * wave(w, x1, x2)
+    g = grid.VolumeGrid(vd)
+    dev = uppe.DeviceGrid(g, vd, ionization.RateCoefficients(vd["ionizer"]), precision)
+    chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+    mat = uppe.Material(dev, g, "cartesian", None, chi, vd["chi3"], vd["density reference"], vd["window speed"],
+                        vd["density lambda"])
+    L = vd["size"][2] / 400
+    a = vd["incoming wave"](g.w, g.x1, g.x2)
+    A_ref, J_ref, chi_ref, ne_ref, nsteps = O.Oracle(vd).propagator(a, 0.0, L, 1, L)
+    A, J, chi_w, ne, evals = uppe.propagator(dev, mat, torch.from_numpy(a.astype(np.complex64)).cuda(), 1, 0.0, L, L)
+    assert nsteps == 1 and evals == 4
+    errs = {"A": rel_err(A.cpu().numpy(), A_ref), "J": rel_err(J.cpu().numpy(), J_ref),
+            "chi": rel_err(chi_w.cpu().numpy(), chi_ref), "ne": rel_err(ne.cpu().numpy(), ne_ref)}
+    print(n0, precision, {k: f"{v:.2e}" for k, v in errs.items()})
+    assert np.max(np.abs(ne_ref)) > 0
+    assert errs["A"] < 2e-5 and errs["J"] < 1e-4 and errs["chi"] < 1e-4 and errs["ne"] < 1e-4
+    dev.close()
