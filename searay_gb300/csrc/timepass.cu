@@ -113,7 +113,8 @@ __device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
 // LOGM > 0: compile-time sizes M = 2^LOGM, C = 2^LOGC (constant-folded index arithmetic and the
 // compile-time Stockham transforms); LOGM = 0: sizes from the parameters.
 template <int ET, int LOGM = 0, int LOGC = -1>
-__global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : 2) k_time(int mode, const float2* __restrict__ E, float2* __restrict__ out0,
+// (three blocks per multiprocessor where shared memory allows it: M <= 512)
+__global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : ((LOGM > 0 && LOGM <= 9) ? 3 : 2)) k_time(int mode, const float2* __restrict__ E, float2* __restrict__ out0,
                                                   float2* __restrict__ out1, const float* __restrict__ ng,
                                                   const float* __restrict__ wv, const float* __restrict__ filt,
                                                   const float2* __restrict__ tw, int twLog, TimeParams tp) {
