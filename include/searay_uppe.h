@@ -123,6 +123,14 @@ int uppe_check_finite(UppeHandle* h, int* nonfinite);
 /* Replace chi3 / density reference (the Kerr coefficient, uppe_kernel.py:52) used from now on. */
 int uppe_set_chi3(UppeHandle* h, double chi3_over_nref);
 
+/* Rotational Raman response (SeaRay's 'rotator', rotations.py:13-73, added to chi before the Kerr
+ * term as uppe_kernel.py:173-179 does, by AddChiUPPE, rotations.cl:85-129).  Host arrays of a
+ * Rotator's tables, nstates entries: Tj (population differences T_j) and Wj (complex transition
+ * frequencies W_j interleaved as re, im), with its dalpha and hbar; transitions j -> j-2 for
+ * j >= 2.  nstates = 0 removes the response.  The adjoint entry points refuse a handle with a
+ * rotator (UPPE_E_ARG). */
+int uppe_set_rotator(UppeHandle* h, int nstates, const double* Tj, const double* Wj, double dalpha, double hbar);
+
 /* Set the spectral amplitude q directly (a checkpoint restart), device complex64 [N0][N1][N2]. */
 int uppe_set_field(UppeHandle* h, const void* q);
 

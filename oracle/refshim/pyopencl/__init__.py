@@ -83,9 +83,15 @@ class _KernelSig:
 _KERNEL_RE = re.compile(r"__kernel\s+void\s+(\w+)\s*\(([^)]*)\)", re.S)
 
 
+def _strip_comments(text):
+    # parameter lists may carry comments, some with parentheses (rotations.cl:88-98)
+    text = re.sub(r"/\*.*?\*/", " ", text, flags=re.S)
+    return re.sub(r"//[^\n]*", " ", text)
+
+
 def _parse_kernels(text):
     sigs = []
-    for m in _KERNEL_RE.finditer(text):
+    for m in _KERNEL_RE.finditer(_strip_comments(text)):
         name = m.group(1)
         params = [p.strip() for p in m.group(2).split(",") if p.strip()]
         decls = []

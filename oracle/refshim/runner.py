@@ -46,7 +46,7 @@ def cl_refs():
         ctx = pyopencl.Context()
         q = pyopencl.CommandQueue(ctx)
         cl = init.cl_refs(ctx, ctx.devices[0], q)
-        for prog in ("fft", "uppe", "paraxial", "ionization"):
+        for prog in ("fft", "uppe", "paraxial", "ionization", "rotations"):
             cl.add_program(str(REF / "kernels"), prog)
         _CL = cl
     return _CL
@@ -57,7 +57,7 @@ def modules():
     _setup_path()
     import importlib
     names = ("uppe_kernel", "grid_tools", "caustic_tools", "ionization", "photoionization_base",
-             "dispersion", "input_tools", "volume")
+             "dispersion", "input_tools", "volume", "rotations")
     return {n: importlib.import_module(n) for n in names}
 
 

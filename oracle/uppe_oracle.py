@@ -232,6 +232,31 @@ def propagator_phase(kz, kg, z):
     return np.exp(-kz.imag * z) * (np.cos((kz.real + kg) * z) + 1j * np.sin((kz.real + kg) * z))
 
 
+def raman_chi(rotator, Et, ng, dt):
+    """Rotational Raman susceptibility, AddChiUPPE (kernels/rotations.cl:85-129), FP64.
+
+    For every j -> j-2 transition (j >= 2) the density-matrix element is driven by the field along the
+    reference's time order (index Nt-1 down to 0, step n): with h = exp(i wdt / 2), wdt = W_j dt,
+        rho_n = -i dt sum_{m < n} F_m h^(2m+1),   F = (dalpha / hbar) E^2 / 2,
+        chi_n += sum_{n' <= n} 2 Im(T_j S_j rho_n' conj(h^(2n')) wdt) ng dalpha,
+    S_j = 2 j (j-1) / (15 (2j-1)).  The reference multiplies the phasor by h twice per step; here
+    the powers are formed directly, which agrees to rounding."""
+    Nt = Et.shape[0]
+    Er = Et[::-1]  # processing order n = Nt-1-k
+    F = 0.5 * (rotator.dalpha / rotator.hbar) * Er ** 2
+    n = np.arange(Nt, dtype=float)[:, None, None]
+    chi = np.zeros_like(Et)
+    for j in range(2, rotator.Wj.shape[0]):
+        wdt = rotator.Wj[j] * dt
+        S = 2.0 * j * (j - 1) / (15 * (2 * j - 1))
+        h2n = np.exp(1j * wdt * n)            # h^(2n)
+        a = F * h2n * np.exp(0.5j * wdt)      # F_m h^(2m+1)
+        rho = -1j * dt * (np.cumsum(a, axis=0) - a)  # exclusive prefix
+        term = rotator.Tj[j] * S * rho * np.conj(h2n) * wdt
+        chi += np.cumsum(2 * term.imag * ng[None] * rotator.dalpha, axis=0)[::-1]
+    return chi
+
+
 class Medium:
     """Material (uppe_kernel.py:32-90): kz, kGalileo and the gas density plane at one z."""
 
@@ -297,6 +322,7 @@ class Oracle:
         self.mat = Medium(self.g, vol_dict, self.window_speed)
         iz = vol_dict.get("ionizer", None)
         self.rates = RateCoefficients(iz) if iz is not None else None
+        self.rotator = vol_dict.get("rotator", None)
         self.dphi = 0.4
         self.rel_amin = 1e-2
         g = self.g
@@ -327,6 +353,8 @@ class Oracle:
             Jw = scipy.fft.rfft(ne * Et, axis=0, workers=_WORKERS)
             Jw = Jw / (0.1 - 1j * w)
         chi = mat.ng[None, ...] * mat.redchi3 * Et * Et
+        if self.rotator is not None:  # uppe_kernel.py:174-176, before the Kerr term
+            chi = chi + raman_chi(self.rotator, Et, mat.ng, g.dt)
         P = scipy.fft.rfft(chi * Et, axis=0, workers=_WORKERS)
         Jw = Jw + (-1j * w) * P
         Jw = Jw * self.nl_filter[:, None, None]

@@ -10,6 +10,7 @@
 
 #include <new>
 #include <utility>
+#include <complex>
 #include <vector>
 
 #include "common.cuh"
@@ -112,7 +113,7 @@ static void free_buffers(UppeHandle* h) {
     void* ptrs[] = {h->q,  h->qi,   h->qf,   h->k1,   h->E,     h->J,      h->scratch, h->opK,  h->opKi, h->kg2,
                     h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red, h->dev_err, h->Minv_tc, h->Mfwd_tc,
                     h->adj_q1, h->adj_q2, h->adj_q3, h->adj_lf, h->adj_acc, h->adj_lk, h->adj_mu, h->MfwdT, h->MinvT,
-                    h->dred_d};
+                    h->dred_d, h->rot};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -621,6 +622,66 @@ extern "C" int uppe_set_chi3(UppeHandle* h, double chi3_over_nref) {
     return UPPE_OK;
 }
 
+extern "C" int uppe_set_rotator(UppeHandle* h, int nstates, const double* Tj, const double* Wj, double dalpha,
+                                double hbar) {
+    if (!h || nstates < 0 || (nstates > 0 && (!Tj || !Wj))) {
+        if (h) uppe_set_error(h, "uppe_set_rotator: invalid arguments");
+        return UPPE_E_ARG;
+    }
+    if (nstates > 0 && !(hbar > 0.0)) {
+        uppe_set_error(h, "uppe_set_rotator: hbar must be positive (got %g)", hbar);
+        return UPPE_E_ARG;
+    }
+    // transitions j -> j-2 for j >= 2 that contribute (T_j = 0 adds exactly nothing)
+    std::vector<int> js;
+    for (int j = 2; j < nstates; ++j)
+        if (Tj[j] != 0.0) js.push_back(j);
+    if (h->rot) {
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        CUDA_TRY(h, cudaFree(h->rot));
+        h->rot = nullptr;
+    }
+    h->rot_states = 0;
+    h->E_valid = 0;
+    if (js.empty()) return UPPE_OK;
+    const int ns = (int)js.size(), nseg = h->Nt / 16;
+    const double dt = h->cfg.dt, Nt = (double)h->Nt;
+    std::vector<float> tab((size_t)ns * 8 + (size_t)ns * nseg * 2, 0.f);
+    for (int s = 0; s < ns; ++s) {
+        const int j = js[s];
+        const std::complex<double> wdt = std::complex<double>(Wj[2 * j], Wj[2 * j + 1]) * dt;
+        const std::complex<double> I(0.0, 1.0);
+        const std::complex<double> h1 = std::exp(0.5 * I * wdt), h2 = std::exp(I * wdt);
+        const double S = 2.0 * j * (j - 1) / (15.0 * (2 * j - 1));
+        // cq = 2 dalpha T_j S_j wdt (-i dt) conj(1/h) (dalpha / 2 hbar) / Nt^2
+        const std::complex<double> cq = 2.0 * dalpha * Tj[j] * S * wdt * (-I * dt) * std::conj(1.0 / h1) *
+                                        (0.5 * dalpha / hbar) / (Nt * Nt);
+        float* t = &tab[(size_t)8 * s];
+        t[0] = (float)h2.real();
+        t[1] = (float)h2.imag();
+        t[2] = (float)std::norm(h2);
+        t[4] = (float)cq.real();
+        t[5] = (float)cq.imag();
+        // phasor p = e^{i wdt (n + 1/2)} at the first sample n = Nt - 16 (seg + 1) of each segment
+        float* p0 = &tab[(size_t)8 * ns + (size_t)2 * nseg * s];
+        for (int seg = 0; seg < nseg; ++seg) {
+            const std::complex<double> p = std::exp(I * wdt * (Nt - 16.0 * (seg + 1) + 0.5));
+            p0[2 * seg] = (float)p.real();
+            p0[2 * seg + 1] = (float)p.imag();
+        }
+    }
+    void* d = nullptr;
+    if (cudaMalloc(&d, tab.size() * sizeof(float)) != cudaSuccess) {
+        cudaGetLastError();
+        uppe_set_error(h, "uppe_set_rotator: device allocation of %zu bytes failed", tab.size() * sizeof(float));
+        return UPPE_E_NOMEM;
+    }
+    h->rot = (float*)d;
+    CUDA_TRY(h, cudaMemcpy(h->rot, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
+    h->rot_states = ns;
+    return UPPE_OK;
+}
+
 extern "C" int uppe_set_field(UppeHandle* h, const void* q) {
     if (!h || !q) return UPPE_E_ARG;
     if (!h->have_grid) {
@@ -636,6 +697,10 @@ extern "C" int uppe_set_field(UppeHandle* h, const void* q) {
 static int ensure_adjoint(UppeHandle* h) {
     if (h->cfg.cylindrical && h->N2 != 1) {
         uppe_set_error(h, "the adjoint supports cylindrical grids with one azimuthal node only");
+        return UPPE_E_ARG;
+    }
+    if (h->rot_states > 0) {
+        uppe_set_error(h, "the adjoint does not include the rotational Raman response (uppe_set_rotator)");
         return UPPE_E_ARG;
     }
     if (h->adj_mu) return UPPE_OK;

@@ -31,6 +31,11 @@ struct TimeParams {
     float c2[6];           // series form: log2(e) * c_i, polynomial in L = ln(Em)
     float em_min;          // below this Em the rate is below FP32's smallest normal (taken as 0)
     int wcut, wwid, plain;
+    // rotational Raman: per transition two float4 {h2.x, h2.y, d, 0}, {cq.x, cq.y, 0, 0} and the
+    // phasor table p0[state][segment] (raman_pass)
+    int rot_states;
+    const float4* rot_tab;
+    const float2* rot_p0;
 };
 
 #define UPPE_LN2 0.69314718055994530942f
@@ -109,10 +114,132 @@ __device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gsrc));
 }
 
+// Shuffle of a two-float value (a complex number or a float-float) down the warp.
+template <class V>
+__device__ __forceinline__ V shfl_down2(V v, int d) {
+    const float a = __shfl_down_sync(0xffffffffu, reinterpret_cast<const float*>(&v)[0], d);
+    const float b = __shfl_down_sync(0xffffffffu, reinterpret_cast<const float*>(&v)[1], d);
+    V r;
+    reinterpret_cast<float*>(&r)[0] = a;
+    reinterpret_cast<float*>(&r)[1] = b;
+    return r;
+}
+
+// Sum of `part` over the later segments (seg' > seg) of this thread's column, for threads laid
+// out as (seg, c) = (tid >> logC, tid & (C - 1)): a shuffle suffix scan within the warp (a warp
+// holds 32/C consecutive segments of each column) and the warps' column totals through `tot`
+// (T entries).  Synchronises the block first, so `tot` may still be read by a previous call.
+template <class V, class Add>
+__device__ __forceinline__ V later_segments_sum(V part, V* tot, int C, int logC, int T, int tid, Add add) {
+    const int c = tid & (C - 1);
+    V acc;
+    reinterpret_cast<float*>(&acc)[0] = 0.f;
+    reinterpret_cast<float*>(&acc)[1] = 0.f;
+    __syncthreads();
+    if (T < 32) {
+        tot[tid] = part;
+        __syncthreads();
+        for (int s2 = (tid >> logC) + 1; s2 < (T >> logC); ++s2) acc = add(acc, tot[(s2 << logC) + c]);
+        return acc;
+    }
+    const int lane = tid & 31, warp = tid >> 5, nwarps = T >> 5;
+    V incl = part;
+    for (int d = C; d < 32; d <<= 1) {
+        const V o = shfl_down2(incl, d);
+        if (lane + d < 32) incl = add(incl, o);
+    }
+    const V nxt = shfl_down2(incl, C);
+    if (lane + C < 32) acc = nxt;
+    if (lane < C) tot[warp * C + lane] = incl;
+    __syncthreads();
+    for (int w2 = warp + 1; w2 < nwarps; ++w2) acc = add(acc, tot[w2 * C + c]);
+    return acc;
+}
+
+// Rotational Raman susceptibility of this thread's SPT samples t = 2 m0 .. 2 m0 + SPT - 1 of
+// column c, written to Zr as pairs (AddChiUPPE, rotations.cl:85-129; rotations.py:40-73).
+//
+// For every j -> j-2 transition the reference runs, in its time order n = Nt-1-t, with
+// h = e^{i wdt/2}, wdt = W_j dt, p_n = h^{2n+1}, F = (dalpha/hbar) E^2 / 2:
+//     R_n = sum_{m<n} F_m p_m,   chi_n += sum_{n'<=n} 2 dalpha ng Im(T_j S_j wdt (-i dt) R_n' conj(h^{2n'})).
+// With u_n = R_n conj(p_n) and rho_n = |p_n|^2 the output is Im(cq u_n), cq = 2 dalpha T_j S_j wdt
+// (-i dt) conj(1/h) (times the field scales), and u obeys u_{n+1} = (u_n + F_n rho_n) conj(h^2),
+// rho_{n+1} = rho_n |h^2|^2.  Per transition: pass 1 sums F_m p_m over the segment (p advanced by
+// h^2 from the segment's first phasor p0, tabulated in FP64 on the host), the sums of the later
+// segments give R at the segment's first sample, and pass 2 runs the u recurrence.  The transition
+// terms of each sample add up in registers; a last suffix sum (float-float in the mixed form) over
+// t gives chi.  Zp holds z = Nt E as pairs; F = z^2 (the scale is folded into cq).
+template <int SPT>
+__device__ __forceinline__ void raman_pass(const TimeParams& tp, const float2* Zp, float2* Zr, ffloat* tot, int C,
+                                           int logC, int T, int tid, int c, int seg, int m0, float ngc) {
+    constexpr int MPS = SPT / 2;
+    const int nseg = T >> logC;
+    float g[SPT];
+#pragma unroll
+    for (int i = 0; i < SPT; ++i) g[i] = 0.f;
+    float2* totc = reinterpret_cast<float2*>(tot);
+    const auto cadd2 = [](float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); };
+    for (int s = 0; s < tp.rot_states; ++s) {
+        const float4 a = __ldg(&tp.rot_tab[2 * s]);      // h2, d
+        const float4 b = __ldg(&tp.rot_tab[2 * s + 1]);  // cq
+        const float2 p0 = __ldg(&tp.rot_p0[(size_t)s * nseg + seg]);
+        // pass 1: sum of F p over this segment, t descending
+        float2 p = p0, acc = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int k = MPS - 1; k >= 0; --k) {
+            const float2 zv = Zp[(m0 + k) * C + c];
+            const float f1 = zv.y * zv.y, f0 = zv.x * zv.x;
+            acc.x = fmaf(f1, p.x, acc.x);
+            acc.y = fmaf(f1, p.y, acc.y);
+            p = cmul(p, make_float2(a.x, a.y));
+            acc.x = fmaf(f0, p.x, acc.x);
+            acc.y = fmaf(f0, p.y, acc.y);
+            p = cmul(p, make_float2(a.x, a.y));
+        }
+        const float2 R = later_segments_sum(acc, totc, C, logC, T, tid, cadd2);
+        // pass 2: u = R conj(p), rho = |p|^2
+        float2 u = cmul(R, cconj(p0));
+        float rho = p0.x * p0.x + p0.y * p0.y;
+        const float2 c2 = make_float2(a.x, -a.y);
+#pragma unroll
+        for (int k = MPS - 1; k >= 0; --k) {
+            const float2 zv = Zp[(m0 + k) * C + c];
+            g[2 * k + 1] = fmaf(b.x, u.y, fmaf(b.y, u.x, g[2 * k + 1]));
+            u.x = fmaf(zv.y * zv.y, rho, u.x);
+            u = cmul(u, c2);
+            rho *= a.z;
+            g[2 * k] = fmaf(b.x, u.y, fmaf(b.y, u.x, g[2 * k]));
+            u.x = fmaf(zv.x * zv.x, rho, u.x);
+            u = cmul(u, c2);
+            rho *= a.z;
+        }
+    }
+    // chi(t) = ng sum_{t' >= t} g(t')
+    ffloat part = {0.f, 0.f};
+#pragma unroll
+    for (int i = SPT - 1; i >= 0; --i) acc_add(part, g[i], tp.plain);
+    const int plain = tp.plain;
+    ffloat cum = later_segments_sum(part, tot, C, logC, T, tid, [plain](ffloat x, ffloat y) {
+        if (plain) return ffloat{x.hi + y.hi, 0.f};
+        return ff_add(x, y);
+    });
+#pragma unroll
+    for (int k = MPS - 1; k >= 0; --k) {
+        acc_add(cum, g[2 * k + 1], tp.plain);
+        const float chi1 = ngc * ff_value(cum);
+        acc_add(cum, g[2 * k], tp.plain);
+        const float chi0 = ngc * ff_value(cum);
+        Zr[(m0 + k) * C + c] = make_float2(chi0, chi1);
+    }
+    __syncthreads();  // `tot` is reused by the density scan
+}
+
 // ET: complex FFT elements per thread (16: 256 threads for C*Nt = 8192; 8: 512 threads)
 // LOGM > 0: compile-time sizes M = 2^LOGM, C = 2^LOGC (constant-folded index arithmetic and the
 // compile-time Stockham transforms); LOGM = 0: sizes from the parameters.
-template <int ET, int LOGM = 0, int LOGC = -1>
+// RAMAN: adds the rotational Raman susceptibility (raman_pass, 16 samples per thread; the Raman
+// chi pairs take a third array Zr [M][C] after the segment totals).
+template <int ET, int LOGM = 0, int LOGC = -1, bool RAMAN = false>
 // (three blocks per multiprocessor where shared memory allows it: M <= 512)
 __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : ((LOGM > 0 && LOGM <= 9) ? 3 : 2)) k_time(int mode, const float2* __restrict__ E, float2* __restrict__ out0,
                                                   float2* __restrict__ out1, const float* __restrict__ ng,
@@ -188,6 +315,8 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : ((LOGM > 
     const float ngc = ng[col0 + c];
     const float kerr = ngc * tp.redchi3;
     const float inv = tp.inv_nt;
+    float2* Zr = reinterpret_cast<float2*>(tot + T);
+    if constexpr (RAMAN) raman_pass<16>(tp, Zp, Zr, tot, C, logC, T, tid, c, seg, m0, ngc);
     float r_next = 0.f;
     ffloat part = {0.f, 0.f};
     if (ionize) {
@@ -264,7 +393,12 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : ((LOGM > 
                 ne0 = ngc * one_minus_exp_neg(ff_value(Sacc));
                 if (t - 1 < wlo || t - 1 > whi) ne0 *= soft_window(t - 1, Nt, tp.wcut, tp.wwid);
             }
-            const float chi1 = kerr * e1 * e1, chi0 = kerr * e0 * e0;
+            float chi1 = kerr * e1 * e1, chi0 = kerr * e0 * e0;
+            if constexpr (RAMAN) {  // the Raman chi comes first in the reference's sum (uppe_kernel.py:173-179)
+                const float2 zr = Zr[m * C + c];
+                chi1 = zr.y + chi1;
+                chi0 = zr.x + chi0;
+            }
             if (mode == TIME_J) {
                 Zp[m * C + c] = make_float2(chi0 * e0, chi1 * e1);
                 Zj[m * C + c] = make_float2(ne0 * e0, ne1 * e1);
@@ -319,6 +453,7 @@ cudaError_t uppe_configure_time_kernel(size_t smem_bytes) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_time<8, A_, B_>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     UPPE_TIME_CT(UPPE_TIME_CONF)
 #undef UPPE_TIME_CONF
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_time<8, 0, -1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     return e;
 }
 
@@ -350,6 +485,9 @@ static TimeParams make_time_params(const UppeHandle* h) {
     tp.wcut = c.window_cutoff;
     tp.wwid = c.window_width;
     tp.plain = (c.precision == UPPE_PREC_FP32);
+    tp.rot_states = h->rot_states;
+    tp.rot_tab = reinterpret_cast<const float4*>(h->rot);
+    tp.rot_p0 = reinterpret_cast<const float2*>(h->rot + 8 * h->rot_states);
     tp.em_min = 0.f;
     if (c.rate_form != UPPE_RATE_NONE) {
         // log2(rate) as a function of Em (atomic units); it rises from -inf at Em -> 0 for physical
@@ -388,6 +526,16 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
     const int T = h->Nt * h->time_cols / h->time_spt;
     const size_t smem = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
     h->launches++;
+    if (h->rot_states > 0) {  // 16 samples per thread, Zr after the segment totals
+        TimeParams tr = tp;
+        tr.spt = 16;
+        const int Tr = h->Nt * h->time_cols / 16;
+        const size_t smem_r = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) +
+                              (size_t)Tr * sizeof(ffloat) + (size_t)h->M * h->time_cols * sizeof(float2);
+        k_time<8, 0, -1, true><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w,
+                                                                              h->nlfilt, h->tw, h->twLog, tr);
+        return cudaGetLastError();
+    }
     if (h->time_spt == 16)
     {
 #define UPPE_TIME_CASE(A_, B_)                                                                                      \

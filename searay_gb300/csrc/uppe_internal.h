@@ -75,6 +75,8 @@ struct UppeHandle {
     double max_abs_K;   // max |Re kz + kg| of the current operator
     double max_Ki;      // max Im kz of the current operator
     double redchi3;        // chi3 / density reference in use (uppe_set_chi3)
+    int rot_states;        // rotational Raman transitions in use (uppe_set_rotator), 0 = none
+    float* rot;            // their tables: [rot_states][8] then the phasors [rot_states][Nt/16] (float2)
     // adjoint work buffers (allocated by the first adjoint call)
     float2 *adj_q1, *adj_q2, *adj_q3, *adj_lf, *adj_acc, *adj_lk, *adj_mu;
     float* MfwdT;          // cylindrical adjoint: [Nr][Nr], MfwdT[r][k] = Mfwd[k][r]

@@ -139,6 +139,20 @@ class DeviceGrid:
     def set_chi3(self, chi3_over_nref):
         self._check(self.lib.uppe_set_chi3(self.h, float(chi3_over_nref)))
 
+    def set_rotator(self, rotator):
+        """Rotational Raman response from a Rotator (this package's or SeaRay's own: the attributes
+        Wj, Tj, dalpha, hbar); None removes it."""
+        if rotator is None:
+            self._check(self.lib.uppe_set_rotator(self.h, 0, None, None, 0.0, 0.0))
+            return
+        Tj = np.ascontiguousarray(rotator.Tj, dtype=np.float64)
+        Wj = np.ascontiguousarray(np.asarray(rotator.Wj, dtype=np.cdouble).view(np.float64))
+        if Wj.shape[0] != 2 * Tj.shape[0]:
+            raise ValueError("rotator: Wj and Tj differ in length")
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._check(self.lib.uppe_set_rotator(self.h, int(Tj.shape[0]), Tj.ctypes.data_as(dp), Wj.ctypes.data_as(dp),
+                                              float(rotator.dalpha), float(rotator.hbar)))
+
     def set_field(self, q_dev):
         self._check(self.lib.uppe_set_field(self.h, ctypes.c_void_p(q_dev.data_ptr())))
 
@@ -290,11 +304,10 @@ def track(cl, xp, eikonal, vg, vol_dict):
     rates = None
     if vol_dict.get("ionizer", None) is not None:
         rates = RateCoefficients(vol_dict["ionizer"])
-    if vol_dict.get("rotator", None) is not None:
-        raise NotImplementedError("rotational Raman response (rotator) is not built in the GB300 propagator")
 
     dev = DeviceGrid(grid, vol_dict, rates, vol_dict.get("precision", "mixed"))
     try:
+        dev.set_rotator(vol_dict.get("rotator", None))
         mat = Material(dev, grid, vol_dict["wave coordinates"], vol_dict.get("object", None), chi, chi3,
                        vol_dict["density reference"], window_speed, vol_dict.get("density lambda", None))
         dens_nodes = cell_centers(-size[3] / 2, size[3] / 2, steps)

@@ -88,7 +88,27 @@ CASES = {
         medium="SimpleAir", ionizer=dict(kind="PPT", Uion_eV=12.07, Z=0.53, terms=40),
         wave=dict(E0=0.0085, w0=1.0, dw=0.15, r0=180.0),
         density="np.ones(x.shape)"),
+    # cylindrical, Kerr + rotational Raman of N2 (32 states, 100 ps dephasing, 90 Torr), no ionization
+    "cyl_raman": dict(
+        keys={"wave grid": (257, 32, 1, 2), "wave coordinates": "cylindrical", "radial modes": 24,
+              "frequency band": (0.0, 4.0), "nonlinear band": (0.0, 3.5),
+              "size": (1600.0, 1600.0, 2.0e4), "subcycles": 4, "minimum step": 2.5e3,
+              "chi3": 0.8437031382441211, "density reference": 0.015499784379078858, "window speed": 1.0},
+        medium="SimpleAir", ionizer=None,
+        rotator=dict(B=2.5464790894703257e-05, dalpha=0.014666374631675184, kT=4.892377952275014e-08,
+                     damp=4.247069967100916e-06, hbar=3.032887794225397e-06, states=32),
+        wave=dict(E0=0.0046, w0=1.0, dw=0.03, r0=400.0, cylindrical=True),
+        density="0.1184*np.ones(x.shape)"),
 }
+
+
+def rotator_args(spec):
+    """Arguments of the Rotator constructor (B, dalpha, kT, dnuc, damp, hbar) for a rotator spec: N2
+    nuclear degeneracy 6 for even j and 3 for odd j, one damping for every level."""
+    j = np.arange(spec["states"])
+    dnuc = 6.0 - 3.0 * (j % 2)
+    damp = spec["damp"] * np.ones(spec["states"])
+    return spec["B"], spec["dalpha"], spec["kT"], dnuc, damp, spec["hbar"]
 
 
 def density_lambda(expr):

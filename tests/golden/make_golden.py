@@ -8,7 +8,9 @@ Also stores reference Hankel bases (``grid_tools.HankelTransformTool``).
 
 Needs the reference source tree (``SEARAY_REF``, default ``/root/reference``)::
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]
+
+With case names, only those fixtures are written (and not the Hankel bases).
 """
 import json
 import pathlib
@@ -50,16 +52,18 @@ def build_ref_case(name, m):
     vd = dict(keys)
     vd["dispersion inside"] = medium
     vd["ionizer"] = iz
+    if c.get("rotator") is not None:
+        vd["rotator"] = m["rotations"].Rotator(*cases.rotator_args(c["rotator"]))
     vd["density lambda"] = cases.density_lambda(c["density"])
     vd["incoming wave"] = cases.make_wave(c["wave"], keys["size"][0])
     return vd, medium, iz
 
 
-def main():
+def main(names=None):
     if not runner.available():
         raise SystemExit("reference tree not found")
     m = runner.modules()
-    for name in cases.CASES:
+    for name in names or cases.CASES:
         vd, medium, iz = build_ref_case(name, m)
         A, J, chi, ne, dom4d, log = runner.reference_track(vd)
         N = vd["wave grid"]
@@ -80,6 +84,10 @@ def main():
         meta["density"] = cases.CASES[name]["density"]
         meta["rate"] = rate
         meta["evals_log"] = log.strip().splitlines()[-1] if log.strip() else ""
+        rot = vd.get("rotator")
+        meta["rotator"] = {} if rot is None else {
+            "Wj": [[float(v.real), float(v.imag)] for v in rot.Wj], "Tj": [float(v) for v in rot.Tj],
+            "dalpha": float(rot.dalpha), "hbar": float(rot.hbar)}
         np.savez_compressed(
             HERE / f"uppe_{name}.npz",
             meta=np.array(json.dumps(meta)),
@@ -89,6 +97,8 @@ def main():
             A=A[..., 1:], J=J[..., 1:], chi=chi[..., 1:], ne=ne[..., 1:], dom4d=dom4d)
         print(name, A.shape, "max|A|", np.abs(A[..., -1]).max(), "max|ne|", np.abs(ne).max(), meta["evals_log"], file=sys.stderr)
         assert w == N[0]
+    if names:
+        return
     # Hankel bases from the reference's HankelTransformTool (grid_tools.py:252-298)
     gt = m["grid_tools"]
     bases = {}
@@ -102,4 +112,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

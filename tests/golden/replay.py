@@ -4,7 +4,8 @@ The fixture ``uppe_<case>.npz`` (written by ``make_golden.py``) holds the resolv
 incoming field on the grid, chi(w) of the medium, the rate-model coefficients and (series form) the
 rate table the fit is made from.  The small duck-typed objects below stand in for the reference's
 dispersion and rate-model classes and expose just the methods ``uppe_kernel.track`` and
-``ionization.Ionizer`` call: ``chi(w)``, ``GetCoeff()``, ``get_mks_length()``, ``Rate(E)``.
+``ionization.Ionizer`` call: ``chi(w)``, ``GetCoeff()``, ``get_mks_length()``, ``Rate(E)``, and the
+rotator's transition table (``Wj``, ``Tj``, ``dalpha``, ``hbar``).
 """
 import json
 import pathlib
@@ -12,7 +13,7 @@ import pathlib
 import numpy as np
 
 HERE = pathlib.Path(__file__).resolve().parent
-CASE_NAMES = ("cyl_kerr", "cart_ion", "cyl_az_adk", "cart_series")
+CASE_NAMES = ("cyl_kerr", "cart_ion", "cyl_az_adk", "cart_series", "cyl_raman")
 
 
 class StoredDispersion:
@@ -47,6 +48,16 @@ class StoredRate:
         raise ValueError("stored rate queried off its table")
 
 
+class StoredRotator:
+    """The attributes of the reference's rotations.Rotator that AddChi reads (Wj, Tj, dalpha, hbar)."""
+
+    def __init__(self, rot):
+        self.Wj = np.array([complex(a, b) for a, b in rot["Wj"]])
+        self.Tj = np.array(rot["Tj"], dtype=float)
+        self.dalpha = rot["dalpha"]
+        self.hbar = rot["hbar"]
+
+
 def density_lambda(expr):
     code = compile(expr, "<density>", "eval")
     return lambda x, y, z, r2: eval(code, {"np": np}, {"x": x, "y": y, "z": z, "r2": r2})
@@ -59,7 +70,7 @@ def load_case(name):
     meta = json.loads(str(d["meta"]))
     vd = {}
     for k, v in meta.items():
-        if k in ("density", "rate", "evals_log"):
+        if k in ("density", "rate", "evals_log", "rotator"):
             continue
         vd[k] = tuple(v) if isinstance(v, list) else v
     A0 = d["A0"]
@@ -67,6 +78,8 @@ def load_case(name):
     vd["dispersion inside"] = StoredDispersion(d["w_nodes"], d["chi_w"])
     vd["ionizer"] = StoredRate(meta["rate"]) if meta["rate"] else None
     vd["density lambda"] = density_lambda(meta["density"])
+    if meta.get("rotator"):
+        vd["rotator"] = StoredRotator(meta["rotator"])
     expected = {k: d[k] for k in ("A", "J", "chi", "ne", "dom4d")}
     expected["evals_log"] = meta.get("evals_log", "")
     expected["rate"] = meta["rate"]

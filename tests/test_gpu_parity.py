@@ -65,6 +65,7 @@ def _device_case(name, precision="mixed"):
     g = grid.VolumeGrid(vd)
     rates = ionization.RateCoefficients(vd["ionizer"]) if vd.get("ionizer") else None
     dev = uppe.DeviceGrid(g, vd, rates, precision)
+    dev.set_rotator(vd.get("rotator"))
     chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
     mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0), vd["density reference"],
                         vd.get("window speed", 1.0), vd["density lambda"])

@@ -83,3 +83,19 @@ def test_track_rejects_bad_grids_before_device_use():
         v["wave grid"] = N
         with pytest.raises(ValueError, match=msg):
             uppe.track(None, None, None, None, v)
+
+
+def test_rotator_matches_reference():
+    """Rotator tables (rotations.py:15-44) against those of the reference's own Rotator stored with
+    the N2 Raman case, and the normalisation sum (2j+1) rho0_j = 1 of the thermal populations."""
+    import cases
+    from searay_gb300 import rotations
+    vd, _ = replay.load_case("cyl_raman")
+    rot = rotations.Rotator(*cases.rotator_args(cases.CASES["cyl_raman"]["rotator"]))
+    ref = vd["rotator"]
+    np.testing.assert_allclose(rot.Wj, ref.Wj, rtol=1e-15, atol=0)
+    np.testing.assert_allclose(rot.Tj, ref.Tj, rtol=1e-15, atol=0)
+    assert rot.dalpha == ref.dalpha and rot.hbar == ref.hbar
+    j = np.arange(rot.wj.shape[0])
+    assert np.sum((2 * j + 1) * rot.rho0jm) == pytest.approx(1.0, rel=1e-14)
+    assert rot.Wj[0] == 0 and rot.Wj[1] == 0 and rot.Tj[0] == 0 and rot.Tj[1] == 0
