@@ -201,6 +201,10 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
         if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
             h->num_sms = nsm;
         if (h->num_sms <= 0) h->num_sms = 152;
+        int smsm = 0;
+        if (cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess)
+            h->smem_per_sm = smsm;
+        if (h->smem_per_sm <= 0) h->smem_per_sm = 228 * 1024;
     }
 
     const size_t fbytes = h->P * sizeof(float2);
@@ -636,38 +640,58 @@ extern "C" int uppe_set_rotator(UppeHandle* h, int nstates, const double* Tj, co
     std::vector<int> js;
     for (int j = 2; j < nstates; ++j)
         if (Tj[j] != 0.0) js.push_back(j);
+    if (js.size() > 128) {
+        uppe_set_error(h, "uppe_set_rotator: %zu contributing transitions exceed the 128 supported", js.size());
+        return UPPE_E_ARG;
+    }
     if (h->rot) {
         CUDA_TRY(h, cudaStreamSynchronize(h->stream));
         CUDA_TRY(h, cudaFree(h->rot));
         h->rot = nullptr;
     }
-    h->rot_states = 0;
+    h->rot_pairs = 0;
     h->E_valid = 0;
     if (js.empty()) return UPPE_OK;
-    const int ns = (int)js.size(), nseg = h->Nt / 16;
+    // transitions in pairs (A, B); an odd count gets a null partner (h2 = 1, cq = 0: adds exactly 0)
+    const int npair = ((int)js.size() + 1) / 2, nseg = h->Nt / 16;
     const double dt = h->cfg.dt, Nt = (double)h->Nt;
-    std::vector<float> tab((size_t)ns * 8 + (size_t)ns * nseg * 2, 0.f);
-    for (int s = 0; s < ns; ++s) {
+    // per pair 20 float4: the constants (4) and the powers h2^i, i < 16; then the phasors
+    std::vector<float> tab((size_t)npair * 80 + (size_t)npair * nseg * 4, 0.f);
+    for (size_t s = 0; s < 2 * (size_t)npair; ++s) {
+        const int pr = (int)(s / 2), lane = (int)(s % 2);
+        float* t = &tab[(size_t)80 * pr];
+        float* p0 = &tab[(size_t)80 * npair + (size_t)4 * nseg * pr];
+        if (s >= js.size()) {
+            t[0 + lane] = 1.f;  // h2 = 1
+            t[6 + lane] = 1.f;  // |h2|^2 = 1
+            for (int i = 0; i < 16; ++i) t[16 + 4 * i + lane] = 1.f;
+            for (int seg = 0; seg < nseg; ++seg) p0[4 * seg + lane] = 1.f;
+            continue;
+        }
         const int j = js[s];
-        const std::complex<double> wdt = std::complex<double>(Wj[2 * j], Wj[2 * j + 1]) * dt;
         const std::complex<double> I(0.0, 1.0);
+        const std::complex<double> wdt = std::complex<double>(Wj[2 * j], Wj[2 * j + 1]) * dt;
         const std::complex<double> h1 = std::exp(0.5 * I * wdt), h2 = std::exp(I * wdt);
         const double S = 2.0 * j * (j - 1) / (15.0 * (2 * j - 1));
         // cq = 2 dalpha T_j S_j wdt (-i dt) conj(1/h) (dalpha / 2 hbar) / Nt^2
         const std::complex<double> cq = 2.0 * dalpha * Tj[j] * S * wdt * (-I * dt) * std::conj(1.0 / h1) *
                                         (0.5 * dalpha / hbar) / (Nt * Nt);
-        float* t = &tab[(size_t)8 * s];
-        t[0] = (float)h2.real();
-        t[1] = (float)h2.imag();
-        t[2] = (float)std::norm(h2);
-        t[4] = (float)cq.real();
-        t[5] = (float)cq.imag();
+        t[0 + lane] = (float)h2.real();
+        t[2 + lane] = (float)h2.imag();
+        t[4 + lane] = (float)(-h2.imag());
+        t[6 + lane] = (float)std::norm(h2);
+        t[8 + lane] = (float)cq.real();
+        t[10 + lane] = (float)cq.imag();
+        for (int i = 0; i < 16; ++i) {
+            const std::complex<double> hp = std::exp(I * wdt * (double)i);
+            t[16 + 4 * i + lane] = (float)hp.real();
+            t[16 + 4 * i + 2 + lane] = (float)hp.imag();
+        }
         // phasor p = e^{i wdt (n + 1/2)} at the first sample n = Nt - 16 (seg + 1) of each segment
-        float* p0 = &tab[(size_t)8 * ns + (size_t)2 * nseg * s];
         for (int seg = 0; seg < nseg; ++seg) {
             const std::complex<double> p = std::exp(I * wdt * (Nt - 16.0 * (seg + 1) + 0.5));
-            p0[2 * seg] = (float)p.real();
-            p0[2 * seg + 1] = (float)p.imag();
+            p0[4 * seg + lane] = (float)p.real();
+            p0[4 * seg + 2 + lane] = (float)p.imag();
         }
     }
     void* d = nullptr;
@@ -678,7 +702,7 @@ extern "C" int uppe_set_rotator(UppeHandle* h, int nstates, const double* Tj, co
     }
     h->rot = (float*)d;
     CUDA_TRY(h, cudaMemcpy(h->rot, tab.data(), tab.size() * sizeof(float), cudaMemcpyHostToDevice));
-    h->rot_states = ns;
+    h->rot_pairs = npair;
     return UPPE_OK;
 }
 
@@ -699,7 +723,7 @@ static int ensure_adjoint(UppeHandle* h) {
         uppe_set_error(h, "the adjoint supports cylindrical grids with one azimuthal node only");
         return UPPE_E_ARG;
     }
-    if (h->rot_states > 0) {
+    if (h->rot_pairs > 0) {
         uppe_set_error(h, "the adjoint does not include the rotational Raman response (uppe_set_rotator)");
         return UPPE_E_ARG;
     }

@@ -31,11 +31,11 @@ struct TimeParams {
     float c2[6];           // series form: log2(e) * c_i, polynomial in L = ln(Em)
     float em_min;          // below this Em the rate is below FP32's smallest normal (taken as 0)
     int wcut, wwid, plain;
-    // rotational Raman: per transition two float4 {h2.x, h2.y, d, 0}, {cq.x, cq.y, 0, 0} and the
-    // phasor table p0[state][segment] (raman_pass)
-    int rot_states;
+    // rotational Raman: transitions in pairs, 20 float4 per pair (constants and powers of h^2) and
+    // the phasor table p0[pair][segment] (raman_pass)
+    int rot_pairs;
     const float4* rot_tab;
-    const float2* rot_p0;
+    const float4* rot_p0;
 };
 
 #define UPPE_LN2 0.69314718055994530942f
@@ -114,28 +114,29 @@ __device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
     asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(gsrc));
 }
 
-// Shuffle of a two-float value (a complex number or a float-float) down the warp.
+// Shuffle of a value of N floats (a complex number, a float-float, a float4) down the warp.
 template <class V>
-__device__ __forceinline__ V shfl_down2(V v, int d) {
-    const float a = __shfl_down_sync(0xffffffffu, reinterpret_cast<const float*>(&v)[0], d);
-    const float b = __shfl_down_sync(0xffffffffu, reinterpret_cast<const float*>(&v)[1], d);
+__device__ __forceinline__ V shfl_down_v(V v, int d) {
+    constexpr int N = sizeof(V) / sizeof(float);
     V r;
-    reinterpret_cast<float*>(&r)[0] = a;
-    reinterpret_cast<float*>(&r)[1] = b;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        reinterpret_cast<float*>(&r)[i] = __shfl_down_sync(0xffffffffu, reinterpret_cast<const float*>(&v)[i], d);
     return r;
 }
 
 // Sum of `part` over the later segments (seg' > seg) of this thread's column, for threads laid
 // out as (seg, c) = (tid >> logC, tid & (C - 1)): a shuffle suffix scan within the warp (a warp
 // holds 32/C consecutive segments of each column) and the warps' column totals through `tot`
-// (T entries).  Synchronises the block first, so `tot` may still be read by a previous call.
+// (T entries of V; (T/32) C entries when T >= 32).  Synchronises the block first, so `tot` may still
+// be read by a previous call; a caller that alternates between two disjoint `tot` areas of (T/32) C
+// entries passes entry_sync = false (blocks of fewer than 32 threads synchronise regardless).
 template <class V, class Add>
-__device__ __forceinline__ V later_segments_sum(V part, V* tot, int C, int logC, int T, int tid, Add add) {
+__device__ __forceinline__ V later_segments_sum(V part, V zero, V* tot, int C, int logC, int T, int tid, Add add,
+                                                bool entry_sync = true) {
     const int c = tid & (C - 1);
-    V acc;
-    reinterpret_cast<float*>(&acc)[0] = 0.f;
-    reinterpret_cast<float*>(&acc)[1] = 0.f;
-    __syncthreads();
+    V acc = zero;
+    if (entry_sync || T < 32) __syncthreads();
     if (T < 32) {
         tot[tid] = part;
         __syncthreads();
@@ -145,15 +146,40 @@ __device__ __forceinline__ V later_segments_sum(V part, V* tot, int C, int logC,
     const int lane = tid & 31, warp = tid >> 5, nwarps = T >> 5;
     V incl = part;
     for (int d = C; d < 32; d <<= 1) {
-        const V o = shfl_down2(incl, d);
+        const V o = shfl_down_v(incl, d);
         if (lane + d < 32) incl = add(incl, o);
     }
-    const V nxt = shfl_down2(incl, C);
+    const V nxt = shfl_down_v(incl, C);
     if (lane + C < 32) acc = nxt;
     if (lane < C) tot[warp * C + lane] = incl;
     __syncthreads();
     for (int w2 = warp + 1; w2 < nwarps; ++w2) acc = add(acc, tot[w2 * C + c]);
     return acc;
+}
+
+// Two FP32 lanes in one 64-bit register for the packed f32x2 arithmetic of sm_100 and later.
+struct f2x {
+    unsigned long long v;
+};
+__device__ __forceinline__ f2x pk2(float lo, float hi) {
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ float2 up2(f2x a) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(a.v));
+    return r;
+}
+__device__ __forceinline__ f2x fma2(f2x a, f2x b, f2x c) {
+    f2x r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+__device__ __forceinline__ f2x mul2(f2x a, f2x b) {
+    f2x r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
 }
 
 // Rotational Raman susceptibility of this thread's SPT samples t = 2 m0 .. 2 m0 + SPT - 1 of
@@ -164,62 +190,108 @@ __device__ __forceinline__ V later_segments_sum(V part, V* tot, int C, int logC,
 //     R_n = sum_{m<n} F_m p_m,   chi_n += sum_{n'<=n} 2 dalpha ng Im(T_j S_j wdt (-i dt) R_n' conj(h^{2n'})).
 // With u_n = R_n conj(p_n) and rho_n = |p_n|^2 the output is Im(cq u_n), cq = 2 dalpha T_j S_j wdt
 // (-i dt) conj(1/h) (times the field scales), and u obeys u_{n+1} = (u_n + F_n rho_n) conj(h^2),
-// rho_{n+1} = rho_n |h^2|^2.  Per transition: pass 1 sums F_m p_m over the segment (p advanced by
-// h^2 from the segment's first phasor p0, tabulated in FP64 on the host), the sums of the later
-// segments give R at the segment's first sample, and pass 2 runs the u recurrence.  The transition
-// terms of each sample add up in registers; a last suffix sum (float-float in the mixed form) over
-// t gives chi.  Zp holds z = Nt E as pairs; F = z^2 (the scale is folded into cq).
-template <int SPT>
-__device__ __forceinline__ void raman_pass(const TimeParams& tp, const float2* Zp, float2* Zr, ffloat* tot, int C,
-                                           int logC, int T, int tid, int c, int seg, int m0, float ngc) {
+// rho_{n+1} = rho_n |h^2|^2.  Per transition: pass 1 forms the segment's sum of F_m p_m as
+// p0 sum_i F_i h^{2i} from the powers h^{2i}, i < 16 (p0: the phasor of the segment's first sample,
+// tabulated in FP64 on the host), the sums of the later segments give R at the segment's first
+// sample, and pass 2 runs the u recurrence.
+//
+// Transitions go in pairs (A, B), one per lane of the packed f32x2 registers, with one block-wide
+// carry exchange per pair; an odd count is padded on the host with a transition that adds exactly
+// zero.  Per pair, in shared memory (Rs): four float4 {h2.re A, B, h2.im A, B}, {-h2.im A, B,
+// |h2|^2 A, B}, {cq.re A, B, cq.im A, B}, unused, then 16 float4 {Re h^{2i} A, B, Im h^{2i} A, B};
+// in global memory the phasors p0[pair][segment] = {p.re A, B, p.im A, B}.  The pair terms of each
+// sample add up in registers; a last suffix sum (float-float in the mixed form) over t gives chi.
+// Zp holds z = Nt E as pairs; F = z^2 (the scale is folded into cq).
+// KEEPF: hold the segment's F = z^2 packed in registers across the pairs (for the variant with
+// registers to spare) rather than forming it again in each pass.
+template <int SPT, bool KEEPF>
+__device__ __forceinline__ void raman_pass(const TimeParams& tp, const float4* Rs, const float2* Zp, float2* Zr,
+                                           ffloat* tot, int C, int logC, int T, int tid, int c, int seg, int m0,
+                                           float ngc) {
     constexpr int MPS = SPT / 2;
     const int nseg = T >> logC;
-    float g[SPT];
+    const int npair = tp.rot_pairs;
+    f2x g2[SPT];
 #pragma unroll
-    for (int i = 0; i < SPT; ++i) g[i] = 0.f;
-    float2* totc = reinterpret_cast<float2*>(tot);
-    const auto cadd2 = [](float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); };
-    for (int s = 0; s < tp.rot_states; ++s) {
-        const float4 a = __ldg(&tp.rot_tab[2 * s]);      // h2, d
-        const float4 b = __ldg(&tp.rot_tab[2 * s + 1]);  // cq
-        const float2 p0 = __ldg(&tp.rot_p0[(size_t)s * nseg + seg]);
-        // pass 1: sum of F p over this segment, t descending
-        float2 p = p0, acc = make_float2(0.f, 0.f);
+    for (int i = 0; i < SPT; ++i) g2[i] = pk2(0.f, 0.f);
+    f2x Fk[KEEPF ? SPT : 1];
+    if constexpr (KEEPF) {
 #pragma unroll
-        for (int k = MPS - 1; k >= 0; --k) {
+        for (int k = 0; k < MPS; ++k) {
             const float2 zv = Zp[(m0 + k) * C + c];
-            const float f1 = zv.y * zv.y, f0 = zv.x * zv.x;
-            acc.x = fmaf(f1, p.x, acc.x);
-            acc.y = fmaf(f1, p.y, acc.y);
-            p = cmul(p, make_float2(a.x, a.y));
-            acc.x = fmaf(f0, p.x, acc.x);
-            acc.y = fmaf(f0, p.y, acc.y);
-            p = cmul(p, make_float2(a.x, a.y));
+            Fk[2 * k] = pk2(zv.x * zv.x, zv.x * zv.x);
+            Fk[2 * k + 1] = pk2(zv.y * zv.y, zv.y * zv.y);
         }
-        const float2 R = later_segments_sum(acc, totc, C, logC, T, tid, cadd2);
-        // pass 2: u = R conj(p), rho = |p|^2
-        float2 u = cmul(R, cconj(p0));
-        float rho = p0.x * p0.x + p0.y * p0.y;
-        const float2 c2 = make_float2(a.x, -a.y);
+    }
+    const auto Fat = [&](int k, int h) -> f2x {
+        if constexpr (KEEPF) {
+            return Fk[2 * k + h];
+        } else {
+            const float2 zv = Zp[(m0 + k) * C + c];
+            const float z = h ? zv.y : zv.x;
+            return pk2(z * z, z * z);
+        }
+    };
+    // segment totals alternate between two areas of (T/32) C float4 (one barrier per pair)
+    float4* tot4 = reinterpret_cast<float4*>(tot);
+    const int half4 = (T >= 32) ? (T >> 5) * C : 0;
+    const auto add4 = [](float4 a, float4 b) { return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); };
+    float4 p0n = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (npair > 0) p0n = __ldg(&tp.rot_p0[seg]);
+    for (int r = 0; r < npair; ++r) {
+        const float4 p0 = p0n;
+        if (r + 1 < npair) p0n = __ldg(&tp.rot_p0[(size_t)(r + 1) * nseg + seg]);
+        const float4* Rp = Rs + 20 * r;
+        // pass 1: S = sum_i F_i h^{2i}, i the position in the reference's time order (t descending)
+        f2x sre = pk2(0.f, 0.f), sim = pk2(0.f, 0.f);
 #pragma unroll
         for (int k = MPS - 1; k >= 0; --k) {
-            const float2 zv = Zp[(m0 + k) * C + c];
-            g[2 * k + 1] = fmaf(b.x, u.y, fmaf(b.y, u.x, g[2 * k + 1]));
-            u.x = fmaf(zv.y * zv.y, rho, u.x);
-            u = cmul(u, c2);
-            rho *= a.z;
-            g[2 * k] = fmaf(b.x, u.y, fmaf(b.y, u.x, g[2 * k]));
-            u.x = fmaf(zv.x * zv.x, rho, u.x);
-            u = cmul(u, c2);
-            rho *= a.z;
+#pragma unroll
+            for (int h = 1; h >= 0; --h) {
+                const float4 H = Rp[4 + 2 * (MPS - 1 - k) + (1 - h)];
+                const f2x F = Fat(k, h);
+                sre = fma2(F, pk2(H.x, H.y), sre);
+                sim = fma2(F, pk2(H.z, H.w), sim);
+            }
+        }
+        // segment total p0 S, then the sums of the later segments: R at this segment's first sample
+        const f2x p0re = pk2(p0.x, p0.y), p0im = pk2(p0.z, p0.w), np0im = pk2(-p0.z, -p0.w);
+        const float2 a0 = up2(fma2(p0re, sre, mul2(np0im, sim))), a1 = up2(fma2(p0re, sim, mul2(p0im, sre)));
+        const float4 R = later_segments_sum(make_float4(a0.x, a0.y, a1.x, a1.y), make_float4(0.f, 0.f, 0.f, 0.f),
+                                            tot4 + (r & 1) * half4, C, logC, T, tid, add4, r < 2);
+        // pass 2: u = R conj(p0), rho = |p0|^2; u <- (u + F rho) conj(h2), rho <- rho |h2|^2
+        const float4 t0 = Rp[0], t1 = Rp[1], t2 = Rp[2];
+        const f2x hre = pk2(t0.x, t0.y), him = pk2(t0.z, t0.w), nhim = pk2(t1.x, t1.y);
+        const f2x Rre = pk2(R.x, R.y), Rim = pk2(R.z, R.w);
+        f2x ure = fma2(Rre, p0re, mul2(Rim, p0im));
+        f2x uim = fma2(Rim, p0re, mul2(Rre, np0im));
+        f2x rho = fma2(p0re, p0re, mul2(p0im, p0im));
+        const f2x d2 = pk2(t1.z, t1.w), cqre = pk2(t2.x, t2.y), cqim = pk2(t2.z, t2.w);
+#pragma unroll
+        for (int k = MPS - 1; k >= 0; --k) {
+#pragma unroll
+            for (int h = 1; h >= 0; --h) {
+                g2[2 * k + h] = fma2(cqim, ure, fma2(cqre, uim, g2[2 * k + h]));
+                ure = fma2(Fat(k, h), rho, ure);
+                const f2x nre = fma2(ure, hre, mul2(uim, him));
+                uim = fma2(ure, nhim, mul2(uim, hre));
+                ure = nre;
+                rho = mul2(rho, d2);
+            }
         }
     }
     // chi(t) = ng sum_{t' >= t} g(t')
+    float g[SPT];
+#pragma unroll
+    for (int i = 0; i < SPT; ++i) {
+        const float2 v = up2(g2[i]);
+        g[i] = v.x + v.y;
+    }
     ffloat part = {0.f, 0.f};
 #pragma unroll
     for (int i = SPT - 1; i >= 0; --i) acc_add(part, g[i], tp.plain);
     const int plain = tp.plain;
-    ffloat cum = later_segments_sum(part, tot, C, logC, T, tid, [plain](ffloat x, ffloat y) {
+    ffloat cum = later_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, [plain](ffloat x, ffloat y) {
         if (plain) return ffloat{x.hi + y.hi, 0.f};
         return ff_add(x, y);
     });
@@ -237,11 +309,14 @@ __device__ __forceinline__ void raman_pass(const TimeParams& tp, const float2* Z
 // ET: complex FFT elements per thread (16: 256 threads for C*Nt = 8192; 8: 512 threads)
 // LOGM > 0: compile-time sizes M = 2^LOGM, C = 2^LOGC (constant-folded index arithmetic and the
 // compile-time Stockham transforms); LOGM = 0: sizes from the parameters.
-// RAMAN: adds the rotational Raman susceptibility (raman_pass, 16 samples per thread; the Raman
-// chi pairs take a third array Zr [M][C] after the segment totals).
-template <int ET, int LOGM = 0, int LOGC = -1, bool RAMAN = false>
+// RAMAN: adds the rotational Raman susceptibility (raman_pass, 16 samples per thread; the segment
+// totals take 2T entries, followed by a third array Zr [M][C] for the Raman chi pairs and the pair
+// tables Rs, 20 float4 per pair).  RAMAN = 1: one block per multiprocessor, F kept in registers;
+// RAMAN = 2: two blocks per multiprocessor.
+template <int ET, int LOGM = 0, int LOGC = -1, int RAMAN = 0>
 // (three blocks per multiprocessor where shared memory allows it: M <= 512)
-__global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : ((LOGM > 0 && LOGM <= 9) ? 3 : 2)) k_time(int mode, const float2* __restrict__ E, float2* __restrict__ out0,
+__global__ void __launch_bounds__(ET == 16 ? 256 : 512,
+                                  RAMAN ? RAMAN : (ET == 16 ? 3 : ((LOGM > 0 && LOGM <= 9) ? 3 : 2))) k_time(int mode, const float2* __restrict__ E, float2* __restrict__ out0,
                                                   float2* __restrict__ out1, const float* __restrict__ ng,
                                                   const float* __restrict__ wv, const float* __restrict__ filt,
                                                   const float2* __restrict__ tw, int twLog, TimeParams tp) {
@@ -276,6 +351,10 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : ((LOGM > 
             cp_async8(&Zj[it], &E[(size_t)k * S + col0 + c]);
         }
     }
+    float2* Zr = reinterpret_cast<float2*>(tot + 2 * T);
+    float4* Rs = reinterpret_cast<float4*>(Zr + (size_t)M * C);
+    if constexpr (RAMAN != 0)
+        for (int i = tid; i < 20 * tp.rot_pairs; i += T) cp_async16_time(&Rs[i], &tp.rot_tab[i]);
     asm volatile("cp.async.commit_group;\n" ::);
     for (int j = tid; j < (Nt >> 1); j += T) twl[j] = __ldg(&tw[j << (twLog - tp.logNt)]);
     asm volatile("cp.async.wait_group 0;\n" ::);
@@ -315,8 +394,7 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : ((LOGM > 
     const float ngc = ng[col0 + c];
     const float kerr = ngc * tp.redchi3;
     const float inv = tp.inv_nt;
-    float2* Zr = reinterpret_cast<float2*>(tot + T);
-    if constexpr (RAMAN) raman_pass<16>(tp, Zp, Zr, tot, C, logC, T, tid, c, seg, m0, ngc);
+    if constexpr (RAMAN != 0) raman_pass<16, RAMAN == 1>(tp, Rs, Zp, Zr, tot, C, logC, T, tid, c, seg, m0, ngc);
     float r_next = 0.f;
     ffloat part = {0.f, 0.f};
     if (ionize) {
@@ -394,7 +472,7 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512, ET == 16 ? 3 : ((LOGM > 
                 if (t - 1 < wlo || t - 1 > whi) ne0 *= soft_window(t - 1, Nt, tp.wcut, tp.wwid);
             }
             float chi1 = kerr * e1 * e1, chi0 = kerr * e0 * e0;
-            if constexpr (RAMAN) {  // the Raman chi comes first in the reference's sum (uppe_kernel.py:173-179)
+            if constexpr (RAMAN != 0) {  // the Raman chi comes first in the reference's sum (uppe_kernel.py:173-179)
                 const float2 zr = Zr[m * C + c];
                 chi1 = zr.y + chi1;
                 chi0 = zr.x + chi0;
@@ -453,7 +531,12 @@ cudaError_t uppe_configure_time_kernel(size_t smem_bytes) {
     if (e == cudaSuccess) e = cudaFuncSetAttribute(k_time<8, A_, B_>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     UPPE_TIME_CT(UPPE_TIME_CONF)
 #undef UPPE_TIME_CONF
-    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_time<8, 0, -1, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+#define UPPE_TIME_RCONF(A_, B_)                                                                                     \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_time<8, A_, B_, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes); \
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(k_time<8, A_, B_, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    UPPE_TIME_CT(UPPE_TIME_RCONF)
+    UPPE_TIME_RCONF(0, -1)
+#undef UPPE_TIME_RCONF
     return e;
 }
 
@@ -485,9 +568,9 @@ static TimeParams make_time_params(const UppeHandle* h) {
     tp.wcut = c.window_cutoff;
     tp.wwid = c.window_width;
     tp.plain = (c.precision == UPPE_PREC_FP32);
-    tp.rot_states = h->rot_states;
+    tp.rot_pairs = h->rot_pairs;
     tp.rot_tab = reinterpret_cast<const float4*>(h->rot);
-    tp.rot_p0 = reinterpret_cast<const float2*>(h->rot + 8 * h->rot_states);
+    tp.rot_p0 = reinterpret_cast<const float4*>(h->rot + 80 * h->rot_pairs);
     tp.em_min = 0.f;
     if (c.rate_form != UPPE_RATE_NONE) {
         // log2(rate) as a function of Em (atomic units); it rises from -inf at Em -> 0 for physical
@@ -526,13 +609,33 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
     const int T = h->Nt * h->time_cols / h->time_spt;
     const size_t smem = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
     h->launches++;
-    if (h->rot_states > 0) {  // 16 samples per thread, Zr after the segment totals
+    if (h->rot_pairs > 0) {  // 16 samples per thread; Zr and the pair tables after the segment totals
         TimeParams tr = tp;
         tr.spt = 16;
         const int Tr = h->Nt * h->time_cols / 16;
         const size_t smem_r = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) +
-                              (size_t)Tr * sizeof(ffloat) + (size_t)h->M * h->time_cols * sizeof(float2);
-        k_time<8, 0, -1, true><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w,
+                              (size_t)2 * Tr * sizeof(ffloat) + (size_t)h->M * h->time_cols * sizeof(float2) +
+                              (size_t)20 * h->rot_pairs * sizeof(float4);
+        // two blocks per multiprocessor where their shared memory fits (64 registers, F formed in each
+        // pass), else one block with the segment's F held in registers (128 registers)
+        const bool occ2 = 2 * (smem_r + 1024) <= (size_t)h->smem_per_sm;
+#define UPPE_TIME_RCASE(A_, B_)                                                                                     \
+        if (tp.logM == A_ && tp.logC == B_) {                                                                          \
+            if (occ2)                                                                                                 \
+                k_time<8, A_, B_, 2><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w, \
+                                                                                 h->nlfilt, h->tw, h->twLog, tr);    \
+            else                                                                                                      \
+                k_time<8, A_, B_, 1><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w, \
+                                                                                 h->nlfilt, h->tw, h->twLog, tr);    \
+            return cudaGetLastError();                                                                             \
+        }
+        UPPE_TIME_CT(UPPE_TIME_RCASE)
+#undef UPPE_TIME_RCASE
+        if (occ2)
+            k_time<8, 0, -1, 2><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w,
+                                                                              h->nlfilt, h->tw, h->twLog, tr);
+        else
+            k_time<8, 0, -1, 1><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w,
                                                                               h->nlfilt, h->tw, h->twLog, tr);
         return cudaGetLastError();
     }

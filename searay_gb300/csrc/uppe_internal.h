@@ -49,6 +49,7 @@ struct UppeHandle {
     int time_cols;                 // transverse points per CTA in the time pass
     int time_spt;                  // time samples per thread in the time pass (16 or 32)
     int num_sms;                   // multiprocessors of the device
+    int smem_per_sm;               // shared memory per multiprocessor (bytes)
     int slice_reg;                 // Cartesian slices use the register-resident transforms (slice_reg.cuh)
     int slice_big;                 // Cartesian slices above 128 x 128: row and column passes (slice_big.cu)
     cudaStream_t stream;
@@ -75,8 +76,8 @@ struct UppeHandle {
     double max_abs_K;   // max |Re kz + kg| of the current operator
     double max_Ki;      // max Im kz of the current operator
     double redchi3;        // chi3 / density reference in use (uppe_set_chi3)
-    int rot_states;        // rotational Raman transitions in use (uppe_set_rotator), 0 = none
-    float* rot;            // their tables: [rot_states][8] then the phasors [rot_states][Nt/16] (float2)
+    int rot_pairs;         // rotational Raman transitions in use (uppe_set_rotator), in pairs; 0 = none
+    float* rot;            // their tables: [rot_pairs][80] then the phasors [rot_pairs][Nt/16] (float4)
     // adjoint work buffers (allocated by the first adjoint call)
     float2 *adj_q1, *adj_q2, *adj_q3, *adj_lf, *adj_acc, *adj_lk, *adj_mu;
     float* MfwdT;          // cylindrical adjoint: [Nr][Nr], MfwdT[r][k] = Mfwd[k][r]
