@@ -149,6 +149,7 @@ def build_device(vd, precision):
     g = grid.VolumeGrid(vd)
     rates = ionization.RateCoefficients(vd["ionizer"]) if vd.get("ionizer") is not None else None
     dev = uppe.DeviceGrid(g, vd, rates, precision)
+    dev.set_rotator(vd.get("rotator"))
     chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
     mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0), vd["density reference"],
                         vd.get("window speed", 1.0), vd["density lambda"])
@@ -199,7 +200,7 @@ def run_device(args, vd, ws, rank, local):
     # forward + adjoint: K_a vector-Jacobian products of the RK4 step (each recomputes its stage
     # states from the step's input, as the checkpointed backward pass does)
     adj = None
-    if args.adjoint_steps > 0:
+    if args.adjoint_steps > 0 and vd.get("rotator") is None:  # the adjoint has no Raman response
         q = dev.empty_field()
         dev.get_field(q)
         gen = torch.Generator(device="cuda").manual_seed(0)
@@ -374,6 +375,21 @@ def main():
                 entry.update({"algo_flops_per_launch": models[name]["flops"], "achieved_TFLOPs": tf,
                               "tensor_frac": tf / tpeak if tensor_path else None})
         kernels[name] = entry
+    rot = vd.get("rotator")
+    if rot is not None and "time_pass" in kernels:
+        # the Raman part of the time pass is FP32 arithmetic: per sample and transition 17 flops
+        # (pass 1: F h^{2i} into the segment sum, 4; pass 2: u + F rho, u conj(h2), rho |h2|^2 and
+        # Im(cq u) into the sample's sum, 13); peak = 2 flops x 128 lanes x SMs x the median SM clock
+        N = vd["wave grid"]
+        ntr = int(np.count_nonzero(np.asarray(rot.Tj)[2:]))
+        flops = 17.0 * (2 * N[0] - 2) * N[1] * N[2] * ntr
+        sec = kernels["time_pass"]["avg_us"] / 1e6
+        nsm = torch.cuda.get_device_properties(0).multi_processor_count
+        fp32_peak = 2 * 128 * nsm * (clk.get("sm_mhz") or 1900) * 1e6 / 1e12
+        kernels["time_pass"]["raman"] = {"transitions": ntr, "algo_flops_per_launch": flops,
+                                         "achieved_TFLOPs": flops / sec / 1e12, "fp32_peak_TFLOPs": fp32_peak,
+                                         "fp32_frac": flops / sec / 1e12 / fp32_peak,
+                                         "note": "FP32 peak from the SM count and the median SM clock under load"}
     dom = max((k for k in kernels if k in models), key=lambda k: kernels[k]["total_ms"])
     traffic = ncu_traffic(args.workload).get(dom)
     share = kernels[dom]["total_ms"] / sum(v["total_ms"] for v in kernels.values())

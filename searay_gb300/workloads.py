@@ -22,6 +22,8 @@ with N0 = 2^n + 1 frequency nodes):
 * ``cyl_silica_512``: cylindrical Nr = Nk = 512 over R = 0.5 mm, N0 = 2049, 1 um 100 fs pulse at
   1e14 W/cm^2 in fused silica (Malitson Sellmeier, n2 = 2.5e-16 cm^2/W), PPT tunneling with
   Ip = 9 eV (Z = 1 assumed) at 2.2e22 cm^-3, 100 RK4 steps over 1 cm.
+* ``cyl_raman_2049``: rotational Raman (N2, 32 states) with Kerr, cylindrical N0 = 2049 (band 0-8 w0),
+  Nr = Nk = 256 over R = 1 mm, 800 nm 40 fs pulse at 4.5e13 W/cm^2, 100 RK4 steps over 0.441 cm.
 """
 import numpy as np
 from scipy import constants as C
@@ -222,5 +224,41 @@ def cyl_adjoint_256(steps=200):
     return vd
 
 
+def n2_rotator(u):
+    """N2 rotations as SeaRay's rotational Raman example sets them: B = 2 cm^-1, dalpha = 4 pi 6.7e-25
+    cm^3, kT = 0.025 eV, 32 states with nuclear degeneracy 6 (even j) and 3 (odd j), 100 ps
+    dephasing; hbar in units of m_e c^2 / w1."""
+    from .rotations import Rotator
+    j = np.arange(32)
+    return Rotator(2.0 / u.cm(1.0), 4 * np.pi * 6.7e-25 / u.cm3(1.0), u.eV(0.025), 6 - 3 * (j % 2),
+                   np.ones(32) / u.fs(1e5), C.hbar * u.w1 / u.u1)
+
+
+def cyl_raman_2049(steps=100):
+    """Rotational Raman benchmark: SeaRay's example of that name with the UPPE propagator (cylindrical
+    N0 = 2049 over the band 0-8 w0, Nr = Nk = 256 over R = 1 mm, nonlinear band 0-4 w0), 800 nm
+    40 fs (FWHM intensity) pulse of 150 um radius at 4.5e13 W/cm^2 in N2 at 90 Torr: Kerr
+    (n2 = 14.8e-24 m^2/W) and the N2 rotator, no ionization.  Two-term air stands in for the
+    example's humid-air dispersion; fixed steps over the example's 0.441 cm."""
+    x1 = 0.8e-6 / (2 * np.pi)
+    u = Units(x1)
+    air = dispersion.SimpleAir(x1)
+    L = u.cm(0.441)
+    E0 = field_from_intensity(u, 4.5e13)
+    tau = u.fs(40.0) / np.sqrt(2 * np.log(2))
+    rel = 90.0 / 760.0
+    vd = {
+        "wave grid": (2049, 256, 1, 2), "wave coordinates": "cylindrical", "radial modes": 256,
+        "frequency band": (0.0, 8.0), "nonlinear band": (0.0, 4.0),
+        "size": (2 * u.mm(1.0), 2 * u.mm(1.0), L), "subcycles": steps, "minimum step": L / steps,
+        "chi3": u.chi3(1.0, 14.8e-24), "density reference": u.cm3(2.7e19),
+        "window speed": air.GroupVelocityMagnitude(1.0),
+        "dispersion inside": air, "ionizer": None, "rotator": n2_rotator(u),
+        "density lambda": lambda x, y, z, r2: rel * np.ones(x.shape),
+        "incoming wave": gaussian_pulse(E0, tau, u.um(150.0), cylindrical=True),
+    }
+    return vd
+
+
 WORKLOADS = {"cyl_kerr_64": cyl_kerr_64, "cart_filament_128": cart_filament_128, "cart_filament_256": cart_filament_256,
-             "cyl_silica_512": cyl_silica_512, "cyl_adjoint_256": cyl_adjoint_256}
+             "cyl_silica_512": cyl_silica_512, "cyl_adjoint_256": cyl_adjoint_256, "cyl_raman_2049": cyl_raman_2049}
