@@ -57,7 +57,7 @@ def modules():
     _setup_path()
     import importlib
     names = ("uppe_kernel", "grid_tools", "caustic_tools", "ionization", "photoionization_base",
-             "dispersion", "input_tools", "volume", "rotations")
+             "dispersion", "input_tools", "volume", "rotations", "paraxial_kernel")
     return {n: importlib.import_module(n) for n in names}
 
 
@@ -112,3 +112,25 @@ def reference_track_rays(vol_dict, xp, eikonal, vg, quiet=True):
     with contextlib.redirect_stdout(out) if quiet else contextlib.nullcontext():
         A, J, chi, ne, dom4d = m["uppe_kernel"].track(cl, xp, eikonal, vg, vd)
     return A, J, chi, ne, dom4d, xp, eikonal, vg
+
+
+def reference_paraxial(vol_dict, quiet=True):
+    """Run ``paraxial_kernel.track`` (``modules/paraxial_kernel.py:367-443``) with no rays entering
+    the grid (the ``incoming wave`` route), with the same harmless ray bundles as reference_track."""
+    cl_refs()
+    m = modules()
+    vd = dict(vol_dict)
+    if "object" not in vd:
+        vd["object"] = DensityObject(vd)
+    xp = np.zeros((2, 4, 8))
+    xp[..., 4] = 1.0
+    xp[..., 7] = 1.0
+    ang = np.arange(8).reshape(2, 4) * 0.4
+    xp[..., 1] = 1e-3 * np.cos(ang)
+    xp[..., 2] = 1e-3 * np.sin(ang)
+    eikonal = np.zeros((2, 4))
+    vg = np.zeros((2, 4, 4))
+    out = io.StringIO()
+    with contextlib.redirect_stdout(out) if quiet else contextlib.nullcontext():
+        A, J, chi, ne, dom4d = m["paraxial_kernel"].track(_CL, xp, eikonal, vg, vd)
+    return A, J, chi, ne, dom4d, out.getvalue()

@@ -1,8 +1,9 @@
 """Generate the golden fixtures in this folder from the reference itself.
 
 Runs SeaRay's own unmodified UPPE path (``modules/uppe_kernel.py:333-424`` with its OpenCL kernels
-``kernels/{fft,uppe,ionization,paraxial}.cl`` compiled as C++ by ``oracle/refshim``) on the cases
-of ``cases.py`` and stores, per case, the resolved inputs (incoming field, chi(w), rate
+``kernels/{fft,uppe,ionization,paraxial,rotations}.cl`` compiled as C++ by ``oracle/refshim``) on
+the cases of ``cases.py``, and its paraxial path (``modules/paraxial_kernel.py:367-443``) on the
+paraxial cases, and stores, per case, the resolved inputs (incoming field, chi(w), rate
 coefficients) and the outputs (A, J, chiNL, ne on every diagnostic plane after the first, dom4d).
 Also stores reference Hankel bases (``grid_tools.HankelTransformTool``).
 
@@ -28,7 +29,7 @@ import cases  # noqa: E402
 
 
 def build_ref_case(name, m):
-    c = cases.CASES[name]
+    c = cases.CASES[name] if name in cases.CASES else cases.PARAXIAL_CASES[name]
     keys = dict(c["keys"])
     helper = m["input_tools"].InputHelper(cases.MKS_LENGTH)
     disp = m["dispersion"]
@@ -63,9 +64,13 @@ def main(names=None):
     if not runner.available():
         raise SystemExit("reference tree not found")
     m = runner.modules()
-    for name in names or cases.CASES:
+    for name in names or (list(cases.CASES) + list(cases.PARAXIAL_CASES)):
         vd, medium, iz = build_ref_case(name, m)
-        A, J, chi, ne, dom4d, log = runner.reference_track(vd)
+        paraxial = name in cases.PARAXIAL_CASES
+        if paraxial:
+            A, J, chi, ne, dom4d, log = runner.reference_paraxial(vd)
+        else:
+            A, J, chi, ne, dom4d, log = runner.reference_track(vd)
         N = vd["wave grid"]
         w = A.shape[0]
         # resolved inputs, so the case can be replayed without the reference classes
@@ -81,7 +86,8 @@ def main(names=None):
                 rate["rate_table"] = iz.Rate(E_table).tolist()
                 rate["clog_reference"] = [float(v) for v in izr.Clog]
         meta = {k: v for k, v in vd.items() if isinstance(v, (int, float, str, tuple, list)) and k not in ("incoming wave",)}
-        meta["density"] = cases.CASES[name]["density"]
+        meta["density"] = (cases.PARAXIAL_CASES if paraxial else cases.CASES)[name]["density"]
+        meta["propagator"] = "paraxial" if paraxial else "uppe"
         meta["rate"] = rate
         meta["evals_log"] = log.strip().splitlines()[-1] if log.strip() else ""
         rot = vd.get("rotator")
@@ -89,7 +95,7 @@ def main(names=None):
             "Wj": [[float(v.real), float(v.imag)] for v in rot.Wj], "Tj": [float(v) for v in rot.Tj],
             "dalpha": float(rot.dalpha), "hbar": float(rot.hbar)}
         np.savez_compressed(
-            HERE / f"uppe_{name}.npz",
+            HERE / (f"{name}.npz" if paraxial else f"uppe_{name}.npz"),
             meta=np.array(json.dumps(meta)),
             w_nodes=w_nodes,
             chi_w=np.asarray(medium.chi(w_nodes)).astype(np.cdouble),

@@ -14,6 +14,7 @@ import numpy as np
 
 HERE = pathlib.Path(__file__).resolve().parent
 CASE_NAMES = ("cyl_kerr", "cart_ion", "cyl_az_adk", "cart_series", "cyl_raman")
+PARAXIAL_CASE_NAMES = ("par_cart_ion", "par_cyl_raman", "par_cyl_az_adk")
 
 
 class StoredDispersion:
@@ -66,11 +67,11 @@ def density_lambda(expr):
 def load_case(name):
     """Return (vol_dict, expected) for a stored case; expected holds A, J, chi, ne (planes >= 1)
     and dom4d as the reference produced them."""
-    d = np.load(HERE / f"uppe_{name}.npz")
+    d = np.load(HERE / (f"{name}.npz" if name in PARAXIAL_CASE_NAMES else f"uppe_{name}.npz"))
     meta = json.loads(str(d["meta"]))
     vd = {}
     for k, v in meta.items():
-        if k in ("density", "rate", "evals_log", "rotator"):
+        if k in ("density", "rate", "evals_log", "rotator", "propagator"):
             continue
         vd[k] = tuple(v) if isinstance(v, list) else v
     A0 = d["A0"]

@@ -130,3 +130,21 @@ def test_torch_reference_step_matches_oracle():
         k4 = orc.load_source((q0 + dz * k3) * cond, z + dz)
         q1o = (qf + dz / 6 * k4) * cond
         assert np.max(np.abs(q1t - q1o)) / np.max(np.abs(q1o)) < 1e-13
+
+
+@pytest.mark.parametrize("name", replay.PARAXIAL_CASE_NAMES)
+def test_paraxial_oracle_matches_reference(name):
+    """The paraxial oracle against the reference's own paraxial_kernel.track on the same inputs."""
+    from oracle import paraxial_oracle as PO
+    vd, exp = replay.load_case(name)
+    orc = PO.ParaxialOracle(vd)
+    A, J, chi, ne, dom4d = orc.track()
+    for key, arr in (("A", A), ("J", J), ("chi", chi), ("ne", ne)):
+        ref = exp[key]
+        scale = max(np.max(np.abs(ref)), 1e-300)
+        err = np.max(np.abs(arr[..., 1:] - ref)) / scale
+        print(name, key, f"{err:.2e}")
+        assert err < 1e-12, (key, err)
+    assert np.array_equal(dom4d, exp["dom4d"])
+    n_ref = int(exp["evals_log"].split()[-4])
+    assert 4 * orc.rk_steps[-1] == n_ref
