@@ -60,6 +60,11 @@ typedef struct UppeConfig {
     double damping;    /* iDtSpectral damping, 0.1 (uppe_kernel.py:171) */
     int window_cutoff; /* SoftTimeWindow cutoff, 4 (uppe_kernel.py:168) */
     int window_width;  /* SoftTimeWindow width, 64 */
+    int envelope;      /* 0: UPPE (uppe_kernel.py); 1: paraxial envelope solver (paraxial_kernel.py):
+                        * n0 = 2^n absolute frequencies in FFT order (np.fft.ifftshift of the band),
+                        * dt = 2 pi / bandwidth (paraxial_kernel.py:98-103), uppe_set_material takes the
+                        * envelope tables, no DC conditioner, NL filter or soft time window; Cartesian
+                        * slices up to 128 x 128; no adjoint */
 } UppeConfig;
 
 typedef struct UppeHandle UppeHandle;
@@ -87,6 +92,10 @@ int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, const doubl
  * with the reference's guards (Im kz >= 0; Re kz == 0 -> 1).  Replaces Material.UpdateMaterial's
  * kz/kg/ng uploads (uppe_kernel.py:67-90). */
 int uppe_set_material(UppeHandle* h, const double* w2n2, const double* kg, const double* ng);
+/* With cfg.envelope = 1 the same call takes the paraxial Material.UpdateMaterial tables
+ * (paraxial_kernel.py:67-91), in FFT order: w2n2 = f(w) = w^2 (1 + chi0 - ng^2) - w0^2 dn^2 - 2 w w0 ng dn
+ * (complex, interleaved), kg = k0(w) = w0 dn + w ng, ng = the gas density plane; the operator is
+ * kz = (f(w) - kperp^2) / (2 k0(w)) and the right-hand side divides by k0(w). */
 
 /* Load the incoming field a (device, real space, complex64) and transform it to the transverse
  * spectral representation q.  Replaces Source(...) + T.kspacex(qw) (uppe_kernel.py:290-291). */

@@ -43,6 +43,7 @@ class UppeConfig(ctypes.Structure):
         ("clog", ctypes.c_double * 6),
         ("damping", ctypes.c_double),
         ("window_cutoff", ctypes.c_int), ("window_width", ctypes.c_int),
+        ("envelope", ctypes.c_int),
     ]
 
 

@@ -125,7 +125,12 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     }
     *out = nullptr;
     const UppeConfig& c = *cfg;
-    if (c.n0 < 17 || !is_pow2(c.n0 - 1)) {
+    const bool env = c.envelope != 0;
+    if (env && (c.n0 < 16 || !is_pow2(c.n0))) {
+        uppe_set_error(nullptr, "Paraxial propagator requires 2**n w-nodes with n >= 4 (got %d)", c.n0);
+        return UPPE_E_ARG;
+    }
+    if (!env && (c.n0 < 17 || !is_pow2(c.n0 - 1))) {
         uppe_set_error(nullptr, "UPPE propagator requires 2**n+1 w-nodes with n >= 4 (got %d)", c.n0);
         return UPPE_E_ARG;
     }
@@ -133,12 +138,17 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
         uppe_set_error(nullptr, "UPPE propagator requires 2**n x-nodes and y-nodes (got %d, %d)", c.n1, c.n2);
         return UPPE_E_ARG;
     }
-    const int Nt = 2 * c.n0 - 2;
+    const int Nt = env ? c.n0 : 2 * c.n0 - 2;  // time samples (complex envelope: one per frequency)
     if (Nt > 8192) {
         uppe_set_error(nullptr, "time axis of %d samples exceeds the 8192 supported by the time pass", Nt);
         return UPPE_E_ARG;
     }
     const long S = (long)c.n1 * c.n2;
+    if (env && !c.cylindrical && (S < 16 || S > 16384)) {
+        uppe_set_error(nullptr, "paraxial Cartesian slice %d x %d outside the supported 16 points .. 128 x 128", c.n1,
+                       c.n2);
+        return UPPE_E_ARG;
+    }
     if (!c.cylindrical && (S < 16 || (S > 16384 && !big_slice_supported(c.n1, c.n2)))) {
         uppe_set_error(nullptr,
                        "Cartesian slice %d x %d outside the supported 16 points .. 128 x 128, 128 x 256, 256 x 128 "
@@ -169,12 +179,14 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     h->N2 = c.n2;
     h->Nk = c.cylindrical ? c.radial_modes : c.n1;
     h->Nt = Nt;
-    h->M = c.n0 - 1;
+    h->M = env ? c.n0 : c.n0 - 1;
     h->S = (int)S;
     h->P = (size_t)c.n0 * S;
-    int tc = 8192 / Nt;
+    // transverse points per time-pass block (the envelope pass holds two complex arrays per point);
+    // at most 32, so that a warp holds whole segments of its columns (later_segments_sum)
+    int tc = env ? 4096 / Nt : 8192 / Nt;
     if (tc < 1) tc = 1;
-    if (tc > 16) tc = 16;
+    if (tc > (env ? 32 : 16)) tc = env ? 32 : 16;
     if (tc > h->S) tc = h->S;
     h->time_cols = tc;
     h->redchi3 = c.chi3_over_nref;
@@ -186,8 +198,8 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     }
     // Cartesian slices of 16..128 points per axis use the register-resident transforms;
     // SEARAY_UPPE_SLICE=generic selects the shared-memory Stockham form for them as well
-    h->slice_big = !c.cylindrical && big_slice_supported(c.n1, c.n2);
-    h->slice_reg = !c.cylindrical && reg_slice_supported(c.n1, c.n2);
+    h->slice_big = !env && !c.cylindrical && big_slice_supported(c.n1, c.n2);
+    h->slice_reg = !env && !c.cylindrical && reg_slice_supported(c.n1, c.n2);
     if (const char* v = getenv("SEARAY_UPPE_SLICE")) {
         if (strcmp(v, "generic") == 0) h->slice_reg = 0;
     }
@@ -255,6 +267,7 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (e == cudaSuccess) e = uppe_configure_slice_kernels(227 * 1024);
     if (e == cudaSuccess) e = uppe_configure_time_kernel(227 * 1024);
     if (e == cudaSuccess) e = uppe_configure_time_adj_kernel(224 * 1024);  // leaves room for its static shared memory
+    if (e == cudaSuccess && env) e = uppe_configure_env_kernel(227 * 1024);
     if (e != cudaSuccess) {
         uppe_set_error(nullptr, "device set-up failed: %s", cudaGetErrorString(e));
         free_buffers(h);
@@ -287,7 +300,7 @@ extern "C" int uppe_set_stream(UppeHandle* h, void* stream) {
 extern "C" int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, const double* H, const double* Lambda) {
     if (!h || !w || !kr2) return h ? (uppe_set_error(h, "uppe_set_grid: null table"), UPPE_E_ARG) : UPPE_E_ARG;
     const UppeConfig& c = h->cfg;
-    if (w[0] != 0.0) {
+    if (!c.envelope && w[0] != 0.0) {
         uppe_set_error(h, "UPPE propagator requires frequency range [0,...]");
         return UPPE_E_ARG;
     }
@@ -357,8 +370,13 @@ extern "C" int uppe_set_material(UppeHandle* h, const double* w2n2, const double
     int cplx = 0;
     for (int k = 0; k < h->N0; ++k) {
         const float hi = (float)kg[k];
-        kg2[k] = make_float2(hi, (float)(kg[k] - (double)hi));
+        // envelope solver: kg holds k0(w), the divisor of the right-hand side
+        kg2[k] = h->cfg.envelope ? make_float2(hi, 0.f) : make_float2(hi, (float)(kg[k] - (double)hi));
         if (w2n2[2 * k + 1] != 0.0) cplx = 1;
+        if (h->cfg.envelope && kg[k] == 0.0) {
+            uppe_set_error(h, "paraxial k0(w) = w0 dn + w ng vanishes at frequency node %d", k);
+            return UPPE_E_ARG;
+        }
     }
     std::vector<float> ngf(h->S);
     for (int s = 0; s < h->S; ++s) ngf[s] = (float)ng[s];
@@ -644,6 +662,16 @@ extern "C" int uppe_set_rotator(UppeHandle* h, int nstates, const double* Tj, co
         uppe_set_error(h, "uppe_set_rotator: %zu contributing transitions exceed the 128 supported", js.size());
         return UPPE_E_ARG;
     }
+    if (h->cfg.envelope) {
+        const int keep = h->rot_pairs;
+        h->rot_pairs = ((int)js.size() + 1) / 2;
+        const size_t need = uppe_env_smem_bytes(h);
+        h->rot_pairs = keep;
+        if (need > 227 * 1024) {
+            uppe_set_error(h, "uppe_set_rotator: the envelope time pass would need %zu bytes of shared memory", need);
+            return UPPE_E_ARG;
+        }
+    }
     if (h->rot) {
         CUDA_TRY(h, cudaStreamSynchronize(h->stream));
         CUDA_TRY(h, cudaFree(h->rot));
@@ -673,9 +701,12 @@ extern "C" int uppe_set_rotator(UppeHandle* h, int nstates, const double* Tj, co
         const std::complex<double> wdt = std::complex<double>(Wj[2 * j], Wj[2 * j + 1]) * dt;
         const std::complex<double> h1 = std::exp(0.5 * I * wdt), h2 = std::exp(I * wdt);
         const double S = 2.0 * j * (j - 1) / (15.0 * (2 * j - 1));
-        // cq = 2 dalpha T_j S_j wdt (-i dt) conj(1/h) (dalpha / 2 hbar) / Nt^2
-        const std::complex<double> cq = 2.0 * dalpha * Tj[j] * S * wdt * (-I * dt) * std::conj(1.0 / h1) *
-                                        (0.5 * dalpha / hbar) / (Nt * Nt);
+        // cq = 2 dalpha T_j S_j wdt (-i dt) conj(1/h) fF / Nt^2: the drive F = fF z^2 of the time pass's
+        // unnormalised field z = Nt E, fF = dalpha / (2 hbar) for the real field (AddChiUPPE) and
+        // dalpha / (4 hbar) on |z|^2 for the envelope (AddChiParaxial: the cycle average of E^2 / 2)
+        const double fF = (h->cfg.envelope ? 0.25 : 0.5) * dalpha / hbar;
+        const std::complex<double> cq = 2.0 * dalpha * Tj[j] * S * wdt * (-I * dt) * std::conj(1.0 / h1) * fF /
+                                        (Nt * Nt);
         t[0 + lane] = (float)h2.real();
         t[2 + lane] = (float)h2.imag();
         t[4 + lane] = (float)(-h2.imag());
@@ -721,6 +752,10 @@ extern "C" int uppe_set_field(UppeHandle* h, const void* q) {
 static int ensure_adjoint(UppeHandle* h) {
     if (h->cfg.cylindrical && h->N2 != 1) {
         uppe_set_error(h, "the adjoint supports cylindrical grids with one azimuthal node only");
+        return UPPE_E_ARG;
+    }
+    if (h->cfg.envelope) {
+        uppe_set_error(h, "the adjoint is not built for the paraxial envelope solver");
         return UPPE_E_ARG;
     }
     if (h->rot_pairs > 0) {

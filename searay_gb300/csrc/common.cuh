@@ -85,7 +85,9 @@ UPPE_DEV float ff_phase(float Khi, float Klo, float zhi, float zlo) {
 struct OpView {
     const float2* __restrict__ K;    // [P] {hi, lo}
     const float* __restrict__ ki;    // [P] Im kz, or nullptr when the medium is real
-    const float2* __restrict__ kg;   // [N0] {hi, lo}
+    const float2* __restrict__ kg;   // [N0] {hi, lo}; envelope solver: {k0(w), 0}
+    int envelope;                    // paraxial envelope solver: E = A, RHS divisor k0(w)
+    int ncond;                       // w-bins zeroed by the DC conditioner (4, or 0 for the envelope)
 };
 
 struct OpPoint {
@@ -97,13 +99,18 @@ UPPE_DEV OpPoint op_at(const OpView& v, size_t idx, float2 kgw) {
     OpPoint o;
     o.Khi = k.x;
     o.Klo = k.y;
-    o.kzr = (k.x - kgw.x) + (k.y - kgw.y);
+    // kzr: Re kz (the RHS divisor and the i kz factor of E); the envelope solver divides by k0(w)
+    o.kzr = v.envelope ? kgw.x : (k.x - kgw.x) + (k.y - kgw.y);
     o.kzi = v.ki ? v.ki[idx] : 0.f;
     return o;
 }
 
 // i kz
 UPPE_DEV float2 op_ikz(const OpPoint& o) { return make_float2(-o.kzi, o.kzr); }
+
+// The field that the time pass reads, from the real-space spectral amplitude a: E = i kz a for UPPE
+// (uppe_kernel.py:212), a itself for the envelope solver (paraxial_kernel.py:196).
+UPPE_DEV float2 op_field(const OpView& v, const OpPoint& o, float2 a) { return v.envelope ? a : cmul(op_ikz(o), a); }
 
 struct PhaseArgs {
     float zhi, zlo;  // z as float-float

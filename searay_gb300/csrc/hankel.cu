@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(256) k_hankel_gemm(GemmArgs g) {
                 } else if (AMODE != A_PLAIN) {
                     const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
                     v = cmul(propagator_factor(o, pa, 1.f), v);
-                    if (AMODE == A_QPHASE_IKZ) v = cmul(op_ikz(o), v);
+                    if (AMODE == A_QPHASE_IKZ) v = op_field(g.op, o, v);
                 }
             }
             As[kk][ww] = v;
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(256) k_hankel_gemm(GemmArgs g) {
     for (int r = 0; r < 2; ++r) {
         const int w = w0 + ty * 2 + r;
         if (w >= g.N0) continue;
-        const float cond = (w < 4) ? 0.f : 1.f;
+        const float cond = (w < g.op.ncond) ? 0.f : 1.f;
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             const int i = i0 + tx * 4 + j;
@@ -109,7 +109,7 @@ __global__ void __launch_bounds__(256) k_hankel_gemm(GemmArgs g) {
             } else if (CMODE == C_FINISH1) {
                 const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
                 if (g.C0) g.C0[idx] = v;
-                g.C1[idx] = cmul(op_ikz(o), v);
+                g.C1[idx] = op_field(g.op, o, v);
             } else {
                 const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
                 float2 f = propagator_factor(o, pa, -1.f);

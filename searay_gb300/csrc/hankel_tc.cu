@@ -114,7 +114,7 @@ __device__ __forceinline__ void tc_load_tile(const TcArgs& g, uint8_t* st, uint3
             if (AMODE != TA_PLAIN) {
                 const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
                 v = cmul(propagator_factor(o, pa, 1.f), v);
-                if (AMODE == TA_QPHASE_IKZ) v = cmul(op_ikz(o), v);
+                if (AMODE == TA_QPHASE_IKZ) v = op_field(g.op, o, v);
             }
         }
         __nv_bfloat16 rh, rl, ih, il;
@@ -262,9 +262,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
         } else if (CMODE == TC_FINISH1) {
             const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
             if (g.C0) g.C0[idx] = v;
-            g.C1[idx] = cmul(op_ikz(o), v);
+            g.C1[idx] = op_field(g.op, o, v);
         } else {
-            const float cond = (w < 4) ? 0.f : 1.f;
+            const float cond = (w < g.op.ncond) ? 0.f : 1.f;
             const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
             const float2 f = propagator_factor(o, pa, -1.f);
             const float2 s = cscale(cmul_i(cmul(f, v)), 0.5f / o.kzr);

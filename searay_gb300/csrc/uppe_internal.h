@@ -111,6 +111,10 @@ cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepA
 // Cartesian first stage from k1 (adaptive step) fused with the inverse transform to E.
 cudaError_t launch_apply1_cart(UppeHandle* h, float Cs, float Ce, StepArgs z);
 cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1);
+// paraxial envelope time pass (envelope.cu)
+cudaError_t launch_time_env(UppeHandle* h, int mode, const float2* A, float2* out0, float2* out1);
+cudaError_t uppe_configure_env_kernel(size_t smem_bytes);
+size_t uppe_env_smem_bytes(const UppeHandle* h);
 cudaError_t launch_absmax(UppeHandle* h, const float2* q);
 cudaError_t launch_step_size(UppeHandle* h, const float2* q, const float2* k, double L, double dphi, double rel_amin);
 cudaError_t launch_apply_stage1(UppeHandle* h, float Cs, float Ce);

@@ -60,12 +60,32 @@ __global__ void k_build_operator(const double* __restrict__ w2n2, const double* 
     opKi[idx] = (float)zi;
 }
 
+// Paraxial envelope operator kz = (f(w) - kperp^2) / (2 k0(w)) (paraxial_kernel.py:79-88), FP64;
+// K holds Re kz (no Galilean term).
+__global__ void k_build_operator_env(const double* __restrict__ fw, const double* __restrict__ k0,
+                                     const double* __restrict__ kr2, float2* __restrict__ opK, float* __restrict__ opKi,
+                                     int N0, int S) {
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)N0 * S) return;
+    int iw = (int)(idx / S);
+    int s = (int)(idx - (size_t)iw * S);
+    const double r = 0.5 / k0[iw];
+    const double K = (fw[2 * iw] - kr2[s]) * r;
+    const float hi = (float)K;
+    opK[idx] = make_float2(hi, (float)(K - (double)hi));
+    opKi[idx] = (float)(fw[2 * iw + 1] * r);
+}
+
 cudaError_t launch_build_operator(UppeHandle* h) {
     size_t n = h->P;
     int threads = 256;
     unsigned blocks = (unsigned)((n + threads - 1) / threads);
     h->launches++;
-    k_build_operator<<<blocks, threads, 0, h->stream>>>(h->w2n2_d, h->kg_d, h->kr2_d, h->opK, h->opKi, h->N0, h->S);
+    if (h->cfg.envelope)
+        k_build_operator_env<<<blocks, threads, 0, h->stream>>>(h->w2n2_d, h->kg_d, h->kr2_d, h->opK, h->opKi, h->N0,
+                                                                h->S);
+    else
+        k_build_operator<<<blocks, threads, 0, h->stream>>>(h->w2n2_d, h->kg_d, h->kr2_d, h->opK, h->opKi, h->N0, h->S);
     return cudaGetLastError();
 }
 
@@ -73,7 +93,7 @@ __global__ void k_operator_bounds(const float2* __restrict__ opK, const float* _
     float mk = 0.f, mi = 0.f;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         mk = fmaxf(mk, fabsf(opK[i].x));
-        mi = fmaxf(mi, opKi[i]);
+        mi = fmaxf(mi, fabsf(opKi[i]));  // |Im kz|: the envelope operator has no sign guard
     }
     for (int o = 16; o > 0; o >>= 1) {
         mk = fmaxf(mk, __shfl_xor_sync(0xffffffffu, mk, o));
@@ -102,6 +122,8 @@ OpView uppe_op_view(const UppeHandle* h) {
     v.K = h->opK;
     v.ki = h->complex_medium ? h->opKi : nullptr;
     v.kg = h->kg2;
+    v.envelope = h->cfg.envelope;
+    v.ncond = h->cfg.envelope ? 0 : 4;
     return v;
 }
 
@@ -158,7 +180,7 @@ __global__ void __launch_bounds__(1024) k_real_cart(int mode, const float2* __re
     const int tid = threadIdx.x, nthr = blockDim.x;
     const PhaseArgs pa{z.zhi, z.zlo, z.plain};
     const float2 kgw = opv.kg[iw];
-    const float cond = (iw < 4) ? 0.f : 1.f;
+    const float cond = (iw < opv.ncond) ? 0.f : 1.f;
     if (mode != REAL_APPLY1) slice_load_async(sm, src + base, S, logN2, tid, nthr);
 #pragma unroll 4
     for (int e = tid; e < S; e += nthr) {
@@ -173,7 +195,7 @@ __global__ void __launch_bounds__(1024) k_real_cart(int mode, const float2* __re
             v = sm[pe];
         }
         v = cmul(propagator_factor(o, pa, 1.f), v);
-        if (mode != REAL_FINISH) v = cmul(op_ikz(o), v);
+        if (mode != REAL_FINISH) v = op_field(opv, o, v);
         sm[pe] = v;
     }
     __syncthreads();
@@ -187,7 +209,7 @@ __global__ void __launch_bounds__(1024) k_real_cart(int mode, const float2* __re
         } else {
             if (A_out) A_out[base + e] = v;
             const OpPoint o = op_at(opv, base + e, kgw);
-            E[base + e] = cmul(op_ikz(o), v);
+            E[base + e] = op_field(opv, o, v);
         }
     }
 }
@@ -204,7 +226,7 @@ __global__ void __launch_bounds__(1024) k_spec_cart(int mode, const float2* __re
     slice_load_async(sm, src + base, S, logN2, tid, nthr);
     slice_forward(sm, logN1, logN2, tw, twLog, tid, nthr);
     const PhaseArgs pa{z.zhi, z.zlo, z.plain};
-    const float cond = (iw < 4) ? 0.f : 1.f;
+    const float cond = (iw < opv.ncond) ? 0.f : 1.f;
     const float2 kgw = (mode == SPEC_LOAD) ? make_float2(0.f, 0.f) : opv.kg[iw];
 #pragma unroll 4
     for (int e = tid; e < S; e += nthr) {
@@ -241,7 +263,7 @@ __global__ void __launch_bounds__(1024) k_fused_cart(int mode, const float2* __r
     slice_forward(sm, logN1, logN2, tw, twLog, tid, nthr);
     const PhaseArgs pr{z_rhs.zhi, z_rhs.zlo, z_rhs.plain};
     const PhaseArgs pn{z_next.zhi, z_next.zlo, z_next.plain};
-    const float cond = (iw < 4) ? 0.f : 1.f;
+    const float cond = (iw < opv.ncond) ? 0.f : 1.f;
     const float2 kgw = opv.kg[iw];
     const bool last = (mode == SPEC_FINISH);
 #pragma unroll 2
@@ -250,7 +272,7 @@ __global__ void __launch_bounds__(1024) k_fused_cart(int mode, const float2* __r
         const int pe = slice_pad(e, logN2);
         const OpPoint o = op_at(opv, idx, kgw);
         const float2 qw = spec_update(mode, idx, sm[pe], o, cond, qi_out, qf, qi, Cs, Ce, pr, last);
-        sm[pe] = cmul(op_ikz(o), cmul(propagator_factor(o, pn, 1.f), qw));
+        sm[pe] = op_field(opv, o, cmul(propagator_factor(o, pn, 1.f), qw));
     }
     __syncthreads();
     slice_inverse(sm, logN1, logN2, tw, twLog, tid, nthr);
@@ -486,10 +508,10 @@ cudaError_t launch_step_size(UppeHandle* h, const float2* q, const float2* k, do
 
 // First RK stage once dz is known: q = cond(qi + Ce k1), qf = qi + Cs k1 (uppe.cl:22-39).
 __global__ void k_apply_stage1(const float2* __restrict__ qi, const float2* __restrict__ k1, float2* __restrict__ q,
-                               float2* __restrict__ qf, size_t n, int S, float Cs, float Ce) {
+                               float2* __restrict__ qf, size_t n, int S, float Cs, float Ce, int ncond) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         float2 a = qi[i], s = k1[i];
-        float cond = (i < (size_t)4 * S) ? 0.f : 1.f;
+        float cond = (i < (size_t)ncond * S) ? 0.f : 1.f;
         qf[i] = cadd(a, cscale(s, Cs));
         q[i] = cscale(cadd(a, cscale(s, Ce)), cond);
     }
@@ -497,7 +519,8 @@ __global__ void k_apply_stage1(const float2* __restrict__ qi, const float2* __re
 
 cudaError_t launch_apply_stage1(UppeHandle* h, float Cs, float Ce) {
     h->launches++;
-    k_apply_stage1<<<reduce_blocks(h->P) * 2, 256, 0, h->stream>>>(h->qi, h->k1, h->q, h->qf, h->P, h->S, Cs, Ce);
+    k_apply_stage1<<<reduce_blocks(h->P) * 2, 256, 0, h->stream>>>(h->qi, h->k1, h->q, h->qf, h->P, h->S, Cs, Ce,
+                                                                   h->cfg.envelope ? 0 : 4);
     return cudaGetLastError();
 }
 
@@ -505,7 +528,7 @@ cudaError_t launch_apply_stage1(UppeHandle* h, float Cs, float Ce) {
 __global__ void k_ikz(const float2* __restrict__ A, OpView opv, float2* __restrict__ E, size_t n, int S) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         const OpPoint o = op_at(opv, i, opv.kg[i / S]);
-        E[i] = cmul(op_ikz(o), A[i]);
+        E[i] = op_field(opv, o, A[i]);
     }
 }
 

@@ -34,15 +34,19 @@ def _check_grid(N):
 
 
 class DeviceGrid:
-    """A C handle for one volume grid plus its device field buffers (Source of uppe_kernel.py:92-129)."""
+    """A C handle for one volume grid plus its device field buffers (Source of uppe_kernel.py:92-129).
 
-    def __init__(self, grid, vol_dict, rates=None, precision="mixed", stream=None):
+    envelope=True makes it the paraxial envelope solver's (Source of paraxial_kernel.py:93-122): the
+    frequency axis goes to the device in FFT order, dt = 2 pi / bandwidth, no NL band."""
+
+    def __init__(self, grid, vol_dict, rates=None, precision="mixed", stream=None, envelope=False):
         lib = _native.lib()
         if not torch.cuda.is_available():
             raise RuntimeError("the GB300 UPPE propagator needs a CUDA device")
         self.grid = grid
         self.N = grid.N
-        nl = vol_dict["nonlinear band"]
+        self.envelope = bool(envelope)
+        nl = (0.0, (grid.N[0] + 1) * abs(grid.dw)) if envelope else vol_dict["nonlinear band"]
         cfg = _native.UppeConfig()
         cfg.n0, cfg.n1, cfg.n2 = grid.N[0], grid.N[1], grid.N[2]
         cfg.radial_modes = 0 if grid.cartesian else grid.Nk
@@ -54,6 +58,12 @@ class DeviceGrid:
         cfg.chi3_over_nref = vol_dict.get("chi3", 0.0) / vol_dict["density reference"]
         cfg.nl_cut_on = int(nl[0] / grid.dw)
         cfg.nl_cut_off = int(nl[1] / grid.dw)
+        if envelope:
+            N0 = grid.N[0]
+            bandwidth = 1.0 if N0 == 1 else (np.max(grid.w) - np.min(grid.w)) * (1 + 1 / (N0 - 1))
+            cfg.dt = 2 * np.pi / bandwidth  # paraxial_kernel.py:98-103
+            cfg.nl_cut_on, cfg.nl_cut_off = 0, N0
+            cfg.envelope = 1
         cfg.damping = 0.1
         cfg.window_cutoff = 4
         cfg.window_width = 64
@@ -79,7 +89,7 @@ class DeviceGrid:
         s = torch.cuda.current_stream() if stream is None else stream
         self.stream = s
         self._check(lib.uppe_set_stream(h, ctypes.c_void_p(s.cuda_stream)))
-        w = np.ascontiguousarray(grid.w, dtype=np.float64)
+        w = np.ascontiguousarray(np.fft.ifftshift(grid.w) if envelope else grid.w, dtype=np.float64)
         kr2 = np.ascontiguousarray(grid.kr2, dtype=np.float64)
         H = None if grid.H is None else np.ascontiguousarray(grid.H, dtype=np.float64)
         lam = None if grid.Lambda is None else np.ascontiguousarray(grid.Lambda, dtype=np.float64)

@@ -99,3 +99,42 @@ def test_rotator_matches_reference():
     j = np.arange(rot.wj.shape[0])
     assert np.sum((2 * j + 1) * rot.rho0jm) == pytest.approx(1.0, rel=1e-14)
     assert rot.Wj[0] == 0 and rot.Wj[1] == 0 and rot.Tj[0] == 0 and rot.Tj[1] == 0
+
+
+@pytest.mark.parametrize("name", replay.PARAXIAL_CASE_NAMES)
+def test_paraxial_material_tables_match_oracle(name):
+    """The envelope tables that paraxial.Material hands to the device (f(w), k0(w), the gas density;
+    paraxial_kernel.py:67-91) equal the oracle's, in FFT order."""
+    from oracle import paraxial_oracle as PO
+    from searay_gb300 import paraxial
+
+    class FakeDevice:
+        def set_material(self, fw, k0, ng):
+            self.tables = (fw, k0, ng)
+            return True
+
+    vd, _ = replay.load_case(name)
+    orc = PO.ParaxialOracle(vd)
+    g = grid.VolumeGrid(vd)
+    dev = FakeDevice()
+    chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+    mat = paraxial.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0), vd["density reference"],
+                            orc.w0, orc.ngrp, orc.n0, vd["density lambda"])
+    for z in (-3000.0, 0.0, 2500.0):
+        mat.UpdateMaterial(z)
+        orc.mat.update(z)
+        fw, k0, ng = dev.tables
+        np.testing.assert_array_equal(fw, orc.mat.fw)
+        np.testing.assert_array_equal(k0, orc.mat.k0)
+        np.testing.assert_array_equal(ng, orc.mat.ng)
+
+
+def test_paraxial_grid_checks():
+    """The ValueErrors of paraxial_kernel.py:393-398, raised before any device work."""
+    from searay_gb300 import paraxial
+    vd, _ = replay.load_case("par_cart_ion")
+    for N, msg in (((129, 16, 16, 2), "w-nodes"), ((128, 12, 16, 2), "x-nodes"), ((128, 16, 24, 2), "y-nodes")):
+        v = dict(vd)
+        v["wave grid"] = N
+        with pytest.raises(ValueError, match=msg):
+            paraxial.track(None, None, None, None, v)
