@@ -144,15 +144,25 @@ def working_set_mb(vd):
     return (6 * 8 + 8 + 4) * P / 1e6  # q, qi, qf, k1, E, J (complex64) + K (float2) + Im kz
 
 
+def is_paraxial(vd):
+    return vd.get("propagator", "uppe") == "paraxial"
+
+
 def build_device(vd, precision):
-    from searay_gb300 import grid, ionization, uppe
+    from searay_gb300 import grid, ionization, paraxial, uppe
     g = grid.VolumeGrid(vd)
     rates = ionization.RateCoefficients(vd["ionizer"]) if vd.get("ionizer") is not None else None
-    dev = uppe.DeviceGrid(g, vd, rates, precision)
+    env = is_paraxial(vd)
+    dev = uppe.DeviceGrid(g, vd, rates, precision, envelope=env)
     dev.set_rotator(vd.get("rotator"))
     chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
-    mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0), vd["density reference"],
-                        vd.get("window speed", 1.0), vd["density lambda"])
+    if env:  # envelope frame of paraxial_kernel.py:407-411
+        n = 1 / vd.get("window speed", 1.0)
+        mat = paraxial.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0),
+                                vd["density reference"], g.w[g.N[0] // 2], n, n, vd["density lambda"])
+    else:
+        mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0), vd["density reference"],
+                            vd.get("window speed", 1.0), vd["density lambda"])
     return g, dev, mat
 
 
@@ -164,6 +174,8 @@ def run_device(args, vd, ws, rank, local):
     nsteps_cfg = vd["subcycles"]
     dz = Lz / nsteps_cfg
     a = vd["incoming wave"](g.w, g.x1, g.x2)
+    if is_paraxial(vd):
+        a = np.fft.ifftshift(a, axes=0)  # the envelope solver keeps the frequency axis in FFT order
     a_dev = torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex64)).cuda()
     mat.UpdateMaterial(-Lz / 2 + 0.5 * dz)
     dev.load_field(a_dev)
@@ -200,7 +212,8 @@ def run_device(args, vd, ws, rank, local):
     # forward + adjoint: K_a vector-Jacobian products of the RK4 step (each recomputes its stage
     # states from the step's input, as the checkpointed backward pass does)
     adj = None
-    if args.adjoint_steps > 0 and vd.get("rotator") is None:  # the adjoint has no Raman response
+    # the adjoint has no Raman response and no envelope form
+    if args.adjoint_steps > 0 and vd.get("rotator") is None and not is_paraxial(vd):
         q = dev.empty_field()
         dev.get_field(q)
         gen = torch.Generator(device="cuda").manual_seed(0)
@@ -232,7 +245,8 @@ def run_device(args, vd, ws, rank, local):
 def run_e2e(args, vd):
     """K steps through track() with host input/outputs (one diagnostic interval)."""
     import torch
-    from searay_gb300 import uppe
+    from searay_gb300 import paraxial, uppe
+    solver = paraxial if is_paraxial(vd) else uppe
     Lz = vd["size"][2]
     dz = Lz / vd["subcycles"]
     v = dict(vd)
@@ -242,10 +256,10 @@ def run_e2e(args, vd):
     warm = dict(v)
     warm["size"] = (vd["size"][0], vd["size"][1], dz * 2)
     warm["subcycles"] = 2
-    uppe.track(None, None, None, None, warm)
+    solver.track(None, None, None, None, warm)
     torch.cuda.synchronize()
     t = time.perf_counter()
-    A, J, chi, ne, dom = uppe.track(None, None, None, None, v)
+    A, J, chi, ne, dom = solver.track(None, None, None, None, v)
     wall = time.perf_counter() - t
     N = v["wave grid"]
     P = int(np.prod(N[:3]))
@@ -263,6 +277,7 @@ def cpu_cores():
 
 def oracle_step_time(vd, n_perp=None):
     """Seconds for one FP64 oracle RK4 step (four RHS evaluations + stage arithmetic)."""
+    from oracle import paraxial_oracle as PO
     from oracle import uppe_oracle as O
     O.set_workers(cpu_cores())
     v = dict(vd)
@@ -271,23 +286,26 @@ def oracle_step_time(vd, n_perp=None):
         f = n_perp / N[1]
         v["wave grid"] = (N[0], n_perp, n_perp if N[2] > 1 else 1, N[3])
         v["size"] = (v["size"][0] * f, v["size"][1] * (f if N[2] > 1 else 1), v["size"][2])
-    orc = O.Oracle(v)
+    env = is_paraxial(v)
+    orc = PO.ParaxialOracle(v) if env else O.Oracle(v)
     g = orc.g
     orc.mat.update(0.0)
-    q = g.kspace(vd["incoming wave"](g.w, g.x1, g.x2))
+    a = vd["incoming wave"](g.w, g.x1, g.x2)
+    q = g.kspace(np.fft.ifftshift(a, axes=0) if env else a)
+    cond = 1.0 if env else orc.conditioner[:, None, None]
     dz = v["size"][2] / v["subcycles"]
     t = time.perf_counter()
     k1 = orc.load_source(q, 0.0)
     qf = q + dz / 6 * k1
-    qw = (q + dz / 2 * k1) * orc.conditioner[:, None, None]
+    qw = (q + dz / 2 * k1) * cond
     k2 = orc.load_source(qw, dz / 2)
     qf = qf + dz / 3 * k2
-    qw = (q + dz / 2 * k2) * orc.conditioner[:, None, None]
+    qw = (q + dz / 2 * k2) * cond
     k3 = orc.load_source(qw, dz / 2)
     qf = qf + dz / 3 * k3
-    qw = (q + dz * k3) * orc.conditioner[:, None, None]
+    qw = (q + dz * k3) * cond
     k4 = orc.load_source(qw, dz)
-    q = (qf + dz / 6 * k4) * orc.conditioner[:, None, None]
+    q = (qf + dz / 6 * k4) * cond
     return time.perf_counter() - t, int(np.prod(g.N[:3])), g.N
 
 
@@ -382,7 +400,8 @@ def main():
         # Im(cq u) into the sample's sum, 13); peak = 2 flops x 128 lanes x SMs x the median SM clock
         N = vd["wave grid"]
         ntr = int(np.count_nonzero(np.asarray(rot.Tj)[2:]))
-        flops = 17.0 * (2 * N[0] - 2) * N[1] * N[2] * ntr
+        Nt = N[0] if is_paraxial(vd) else 2 * N[0] - 2
+        flops = 17.0 * Nt * N[1] * N[2] * ntr
         sec = kernels["time_pass"]["avg_us"] / 1e6
         nsm = torch.cuda.get_device_properties(0).multi_processor_count
         fp32_peak = 2 * 128 * nsm * (clk.get("sm_mhz") or 1900) * 1e6 / 1e12
@@ -407,6 +426,7 @@ def main():
         "dtype": "f32 (float-float phase and density scan)" if args.precision == "mixed" else "f32",
         "data": "synthetic",
         "config": {"workload": args.workload, "grid": list(vd["wave grid"][:3]),
+                   "propagator": vd.get("propagator", "uppe"),
                    "precision": args.precision, "parallelism": "replicas" if ws > 1 else "single",
                    "l2": f"working set ({working_set_mb(vd):.0f} MB of fields and operator) vs the 129 MB L2"},
         "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk, "finite": finite,

@@ -213,6 +213,11 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
         if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess)
             h->num_sms = nsm;
         if (h->num_sms <= 0) h->num_sms = 152;
+        // small envelope grids: fewer transverse points per time-pass block while that leaves fewer
+        // blocks than multiprocessors, keeping at least one full warp per block
+        while (env && h->time_cols > 1 && h->S / h->time_cols < h->num_sms &&
+               h->Nt * (h->time_cols / 2) / 16 >= 32)
+            h->time_cols /= 2;
         int smsm = 0;
         if (cudaDeviceGetAttribute(&smsm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev) == cudaSuccess)
             h->smem_per_sm = smsm;

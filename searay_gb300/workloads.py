@@ -24,6 +24,8 @@ with N0 = 2^n + 1 frequency nodes):
   Ip = 9 eV (Z = 1 assumed) at 2.2e22 cm^-3, 100 RK4 steps over 1 cm.
 * ``cyl_raman_2049``: rotational Raman (N2, 32 states) with Kerr, cylindrical N0 = 2049 (band 0-8 w0),
   Nr = Nk = 256 over R = 1 mm, 800 nm 40 fs pulse at 4.5e13 W/cm^2, 100 RK4 steps over 0.441 cm.
+* ``cyl_raman_paraxial_256``: the same physics with the paraxial envelope propagator (``'propagator':
+  'paraxial'``): N0 = 256 over the band 0.5-1.5 w0, Nr = Nk = 256, 100 RK4 steps over 0.441 cm.
 """
 import numpy as np
 from scipy import constants as C
@@ -107,6 +109,24 @@ def gaussian_pulse(E0, tau, r0, cylindrical=False, screen=None, w0=1.0):
             tr = np.exp(-(x1[:, None] ** 2 + x2[None, :] ** 2) / r0 ** 2)
         if screen is not None:
             tr = tr * np.exp(1j * screen(x1, x2))
+        return spec[:, None, None] * tr[None, :, :]
+    return wave
+
+
+def envelope_pulse(E0, tau, r0, cylindrical=False, w0=1.0):
+    """Incoming wave for the paraxial (envelope) solver: the spectrum on the band's absolute
+    frequencies of the pulse E0 exp(-t^2/tau^2) around carrier w0, centred in the time window, so that
+    the envelope field ifft(i w A) (FFT order) has its crest near E0; Gaussian transverse profile."""
+    def wave(w, x1, x2):
+        dwn = w[1] - w[0]
+        N0 = w.shape[0]
+        dw = 2.0 / tau
+        amp = E0 * N0 * dwn / (np.sqrt(np.pi) * dw * w0)
+        spec = amp * np.exp(-(w - w0) ** 2 / dw ** 2) * np.exp(-1j * (w - w[N0 // 2]) * np.pi / dwn)
+        if cylindrical:
+            tr = np.exp(-(x1[:, None] ** 2) / r0 ** 2) * np.ones((1, x2.shape[0]))
+        else:
+            tr = np.exp(-(x1[:, None] ** 2 + x2[None, :] ** 2) / r0 ** 2)
         return spec[:, None, None] * tr[None, :, :]
     return wave
 
@@ -260,5 +280,23 @@ def cyl_raman_2049(steps=100):
     return vd
 
 
+def cyl_raman_paraxial_256(steps=100):
+    """Rotational Raman benchmark with the paraxial (envelope) propagator, SeaRay's default for that
+    example: N0 = 256 frequencies over the band 0.5-1.5 w0, cylindrical Nr = Nk = 256 over R = 1 mm,
+    the pulse, medium and N2 rotator of ``cyl_raman_2049``; fixed steps over 0.441 cm."""
+    vd = cyl_raman_2049(steps)
+    vd["propagator"] = "paraxial"
+    vd["wave grid"] = (256, 256, 1, 2)
+    vd["frequency band"] = (0.5, 1.5)
+    x1 = 0.8e-6 / (2 * np.pi)
+    u = Units(x1)
+    E0 = field_from_intensity(u, 4.5e13)
+    tau = u.fs(40.0) / np.sqrt(2 * np.log(2))
+    vd["incoming wave"] = envelope_pulse(E0, tau, u.um(150.0), cylindrical=True)
+    del vd["nonlinear band"]
+    return vd
+
+
 WORKLOADS = {"cyl_kerr_64": cyl_kerr_64, "cart_filament_128": cart_filament_128, "cart_filament_256": cart_filament_256,
-             "cyl_silica_512": cyl_silica_512, "cyl_adjoint_256": cyl_adjoint_256, "cyl_raman_2049": cyl_raman_2049}
+             "cyl_silica_512": cyl_silica_512, "cyl_adjoint_256": cyl_adjoint_256, "cyl_raman_2049": cyl_raman_2049,
+             "cyl_raman_paraxial_256": cyl_raman_paraxial_256}
