@@ -263,8 +263,10 @@ def run_e2e(args, vd):
     wall = time.perf_counter() - t
     N = v["wave grid"]
     P = int(np.prod(N[:3]))
-    h2d = P * 8 + (2 * N[0] + N[0]) * 8 + N[1] * N[2] * 8
-    d2h = 4 * P * 8
+    # the incoming plane (complex128) and the material tables in; the four complex128 result arrays
+    # (every diagnostic plane) out
+    h2d = P * 16 + (2 * N[0] + N[0]) * 8 + N[1] * N[2] * 8
+    d2h = 4 * P * N[3] * 16
     return P * args.steps / wall, h2d, d2h, bool(np.isfinite(A[..., -1]).all())
 
 

@@ -22,7 +22,7 @@ import torch
 from . import raywave
 from .grid import VolumeGrid, cell_centers, cell_walls
 from .ionization import RateCoefficients
-from .uppe import DeviceGrid
+from .uppe import DeviceGrid, TrackOutputs
 
 _POW2 = [2 ** i for i in range(32)]
 
@@ -124,10 +124,6 @@ def track(cl, xp, eikonal, vg, vol_dict):
     diagnostic_steps = N[3] - 1
     subcycles = vol_dict["subcycles"]
     steps = diagnostic_steps * subcycles
-    A = np.zeros(N).astype(np.cdouble)
-    J = np.zeros(N).astype(np.cdouble)
-    chiNL = np.zeros(N).astype(np.cdouble)
-    ne = np.zeros(N).astype(np.cdouble)
     _check_grid(N)
     window_speed = vol_dict.get("window speed", 1.0)
     chi3 = vol_dict.get("chi3", 0.0)
@@ -137,10 +133,10 @@ def track(cl, xp, eikonal, vg, vol_dict):
     if "incoming wave" not in vol_dict:
         logging.info("Start paraxial propagation using ray data.")
         logging.warning("Polarization information is lost upon entering paraxial region.")
-        A[..., 0] = raywave.boundary_fields(field_grid, xp[:, 0, :], eikonal, 1)
+        first = raywave.boundary_fields(field_grid, xp[:, 0, :], eikonal, 1)
     else:
         logging.info("Start paraxial propagation using wave data")
-        A[..., 0] = vol_dict["incoming wave"](grid.w, grid.x1, grid.x2)
+        first = vol_dict["incoming wave"](grid.w, grid.x1, grid.x2)
 
     # reference frame of the envelope (paraxial_kernel.py:407-411)
     w0 = grid.w[int(N[0] / 2)]
@@ -162,8 +158,9 @@ def track(cl, xp, eikonal, vg, vol_dict):
         diagnostic_walls = np.linspace(-size[3] / 2, size[3] / 2, N[3])
         dom4d = np.concatenate((grid.plot_ext, [field_walls[0], field_walls[-1]]))
 
-        shift = lambda t: torch.fft.fftshift(t, dim=0).cpu().numpy()
-        a_dev = torch.from_numpy(np.ascontiguousarray(np.fft.ifftshift(A[..., 0], axes=0), dtype=np.complex64)).to("cuda")
+        # the device keeps the frequency axis in FFT order; the outputs go back in ascending order
+        res = TrackOutputs(N, first, shift=lambda t: torch.fft.fftshift(t, dim=0))
+        a_dev = res.first_plane(order=lambda t: torch.fft.ifftshift(t, dim=0))
         outs = tuple(dev.empty_field() for _ in range(4))
         for k in range(diagnostic_steps):
             zi = diagnostic_walls[k]
@@ -171,11 +168,9 @@ def track(cl, xp, eikonal, vg, vol_dict):
             logging.info("Advancing to diagnostic plane %d", k + 1)
             A0, J0, c0, n0_, evals = propagator(dev, mat, a_dev, subcycles, zi, zf, outs)
             logging.info("%d evaluations of j(w,kx,ky)", evals)
-            A[..., k + 1] = shift(A0)
-            J[..., k + 1] = shift(J0)
-            chiNL[..., k + 1] = shift(c0)
-            ne[..., k + 1] = shift(n0_)
+            res.store(k + 1, A0, J0, c0, n0_)
             a_dev, outs = A0, (dev.empty_field(), J0, c0, n0_)
+        A, J, chiNL, ne = res.host()
     finally:
         dev.close()
     # relaunch the rays from the last plane (paraxial_kernel.py:438-442)

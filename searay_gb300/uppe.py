@@ -275,6 +275,35 @@ def propagator(dev, mat, a_dev, subcycles, zi, zf, dzmin, outputs=None):
     return A, J, chi, ne, 4 * iterations
 
 
+class TrackOutputs:
+    """The four arrays that ``track`` returns (A, J, chiNL, ne: complex128 of shape (N0, N1, N2, N3),
+    diagnostic planes last, as uppe_kernel.py:343-352 lays them out), assembled on the device plane
+    by plane and copied to the host once at the end.  The complex64 -> complex128 widening and the
+    strided plane writes run on the device; the host receives one contiguous copy per array.
+    ``shift`` reorders the frequency axis of each stored plane (the paraxial solver's fftshift)."""
+
+    def __init__(self, N, first_plane, shift=None):
+        self.arrays = [torch.empty(tuple(N), dtype=torch.complex128, device="cuda") for _ in range(4)]
+        self.arrays[0][..., 0] = torch.from_numpy(np.ascontiguousarray(first_plane, dtype=np.complex128)).to("cuda")
+        for x in self.arrays[1:]:
+            x[..., 0] = 0
+        self.shift = shift
+
+    def first_plane(self, order=None):
+        """The incoming plane as a contiguous complex64 device field (optionally reordered)."""
+        a = self.arrays[0][..., 0]
+        if order is not None:
+            a = order(a)
+        return a.to(torch.complex64).contiguous()
+
+    def store(self, k, A, J, chi, ne):
+        for dst, src in zip(self.arrays, (A, J, chi, ne)):
+            dst[..., k].copy_(self.shift(src) if self.shift is not None else src)
+
+    def host(self):
+        return tuple(x.cpu().numpy() for x in self.arrays)
+
+
 def track(cl, xp, eikonal, vg, vol_dict):
     """Propagate the UPPE volume's wave through its diagnostic planes (uppe_kernel.py:333-424).
 
@@ -292,10 +321,6 @@ def track(cl, xp, eikonal, vg, vol_dict):
     diagnostic_steps = N[3] - 1
     subcycles = vol_dict["subcycles"]
     steps = diagnostic_steps * subcycles
-    A = np.zeros(N).astype(np.cdouble)
-    J = np.zeros(N).astype(np.cdouble)
-    chiNL = np.zeros(N).astype(np.cdouble)
-    ne = np.zeros(N).astype(np.cdouble)
     _check_grid(N)
     window_speed = vol_dict.get("window speed", 1.0)
     chi3 = vol_dict.get("chi3", 0.0)
@@ -305,10 +330,10 @@ def track(cl, xp, eikonal, vg, vol_dict):
     if "incoming wave" not in vol_dict:
         logging.info("Start UPPE propagation using ray data.")
         logging.warning("Polarization information is lost upon entering UPPE region.")
-        A[..., 0] = raywave.boundary_fields(field_grid, xp[:, 0, :], eikonal, 1)
+        first = raywave.boundary_fields(field_grid, xp[:, 0, :], eikonal, 1)
     else:
         logging.info("Start UPPE propagation using wave data")
-        A[..., 0] = vol_dict["incoming wave"](grid.w, grid.x1, grid.x2)
+        first = vol_dict["incoming wave"](grid.w, grid.x1, grid.x2)
 
     chi = vol_dict["dispersion inside"].chi(grid.w).astype(np.cdouble)
     rates = None
@@ -326,7 +351,8 @@ def track(cl, xp, eikonal, vg, vol_dict):
         dzmin = vol_dict["minimum step"]
         dom4d = np.concatenate((grid.plot_ext, [field_walls[0], field_walls[-1]]))
 
-        a_dev = torch.from_numpy(np.ascontiguousarray(A[..., 0], dtype=np.complex64)).to("cuda")
+        res = TrackOutputs(N, first)
+        a_dev = res.first_plane()
         outs = tuple(dev.empty_field() for _ in range(4))
         for k in range(diagnostic_steps):
             zi = diagnostic_walls[k]
@@ -334,11 +360,9 @@ def track(cl, xp, eikonal, vg, vol_dict):
             logging.info("Advancing to diagnostic plane %d", k + 1)
             A0, J0, c0, n0, evals = propagator(dev, mat, a_dev, subcycles, zi, zf, dzmin, outs)
             logging.info("%d evaluations of j(w,kx,ky)", evals)
-            A[..., k + 1] = A0.cpu().numpy()
-            J[..., k + 1] = J0.cpu().numpy()
-            chiNL[..., k + 1] = c0.cpu().numpy()
-            ne[..., k + 1] = n0.cpu().numpy()
+            res.store(k + 1, A0, J0, c0, n0)
             a_dev, outs = A0, (dev.empty_field(), J0, c0, n0)
+        A, J, chiNL, ne = res.host()
     finally:
         dev.close()
     # relaunch the rays from the last plane (uppe_kernel.py:420-423)
