@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
     // ---- 2. sources, in place ----
     const int c = tid & (C - 1);
     const int seg = tid >> logC;
-    const int mps = tp.spt >> 1;  // packed pairs per thread
+    const int mps = CT ? 8 : (tp.spt >> 1);  // packed pairs per thread (16 samples with compile-time sizes)
     const int m0 = seg * mps;
     const int t1 = 2 * (m0 + mps);  // first sample of the next segment
     const float ngc = ng[col0 + c];
@@ -131,19 +131,25 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
     }
     float r_next = 0.f;
     ffloat part = {0.f, 0.f};
+    bool live = false;  // a nonzero rate in this segment (zero increments leave a float-float sum exactly as it is)
     if (ionize) {
         if (t1 <= Nt - 2) r_next = ion_rate(tp, Zp[(t1 >> 1) * C + c].x * inv);
         float rn = r_next;
+#pragma unroll(CT ? 8 : 1)
         for (int m = m0 + mps - 1; m >= m0; --m) {
             const float2 zv = Zp[m * C + c];
             const int t = 2 * m + 1;
             const float r1 = (t == Nt - 1) ? 0.f : ion_rate(tp, zv.y * inv);
-            if (t <= Nt - 2) acc_add(part, tp.hdt * (r1 + rn), tp.plain);
+            const float p1 = tp.hdt * (r1 + rn);
+            if (t <= Nt - 2 && p1 != 0.f) acc_add(part, p1, tp.plain);
             const float r0 = ion_rate(tp, zv.x * inv);
-            acc_add(part, tp.hdt * (r0 + r1), tp.plain);
+            const float p0 = tp.hdt * (r0 + r1);
+            if (p0 != 0.f) acc_add(part, p0, tp.plain);
+            live = live || r0 != 0.f || r1 != 0.f;
             rn = r0;
             Zj[m * C + c] = make_float2(r0, r1);  // this thread's own slot, reused below
         }
+        live = live || r_next != 0.f;
     }
     // Sum of the later segments of this column.  A warp holds 32/C consecutive segments of each of
     // the C columns (lanes C apart): a shuffle suffix scan gives the sums within the warp, and the
@@ -190,11 +196,14 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
     {
         float rn = r_next;
         const int wlo = tp.wcut + tp.wwid, whi = Nt - tp.wcut - tp.wwid - 1;  // window is 1 on [wlo, whi]
+        // no rate in this segment and none in the later ones: the density is zero throughout
+        const bool dens = ionize && (live || Sacc.hi != 0.f || Sacc.lo != 0.f);
+#pragma unroll(CT ? 8 : 1)
         for (int m = m0 + mps - 1; m >= m0; --m) {
             const float2 zv = Zp[m * C + c];
             const float e1 = zv.y * inv, e0 = zv.x * inv;
             float ne1 = 0.f, ne0 = 0.f;
-            if (ionize) {
+            if (dens) {
                 const float2 rr = Zj[m * C + c];
                 const int t = 2 * m + 1;
                 if (t <= Nt - 2) acc_add(Sacc, tp.hdt * (rr.y + rn), tp.plain);
