@@ -806,15 +806,13 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
     h->E_valid = 0;
     {
         const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz);
+        // each stage writes its estimate straight into the buffer the reverse sweep reads
         CUDA_TRY(h, eval_to_J(h, h->qi, z0));
-        PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE1, h->J, h->q, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z0));
-        CUDA_TRY(h, cudaMemcpyAsync(h->adj_q1, h->q, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
-        CUDA_TRY(h, eval_to_J(h, h->q, zh));
-        PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), zh));
-        CUDA_TRY(h, cudaMemcpyAsync(h->adj_q2, h->q, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
-        CUDA_TRY(h, eval_to_J(h, h->q, zh));
-        PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)dz, zh));
-        CUDA_TRY(h, cudaMemcpyAsync(h->adj_q3, h->q, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
+        PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE1, h->J, h->adj_q1, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z0));
+        CUDA_TRY(h, eval_to_J(h, h->adj_q1, zh));
+        PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE23, h->J, h->adj_q2, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), zh));
+        CUDA_TRY(h, eval_to_J(h, h->adj_q2, zh));
+        PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE23, h->J, h->adj_q3, h->qf, h->qi, (float)(dz / 3), (float)dz, zh));
     }
     // reverse sweep through the four stages
     CUDA_TRY(h, launch_adj_rk(h, 0, (const float2*)lam_out, nullptr, (float)(dz / 6), 0.f));

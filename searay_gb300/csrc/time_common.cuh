@@ -133,6 +133,45 @@ __device__ __forceinline__ V later_segments_sum(V part, V zero, V* tot, int C, i
     return acc;
 }
 
+template <class V>
+__device__ __forceinline__ V shfl_up_v(V v, int d) {
+    constexpr int N = sizeof(V) / sizeof(float);
+    V r;
+#pragma unroll
+    for (int i = 0; i < N; ++i)
+        reinterpret_cast<float*>(&r)[i] = __shfl_up_sync(0xffffffffu, reinterpret_cast<const float*>(&v)[i], d);
+    return r;
+}
+
+// Sum of `part` over the earlier segments (seg' < seg) of this thread's column: the prefix
+// counterpart of later_segments_sum, with the same layout, `tot` and barrier rules.
+template <class V, class Add>
+__device__ __forceinline__ V earlier_segments_sum(V part, V zero, V* tot, int C, int logC, int T, int tid, Add add,
+                                                  bool entry_sync = true) {
+    const int c = tid & (C - 1);
+    V acc = zero;
+    if (entry_sync || T < 32) __syncthreads();
+    if (T < 32) {
+        tot[tid] = part;
+        __syncthreads();
+        for (int s2 = 0; s2 < (tid >> logC); ++s2) acc = add(acc, tot[(s2 << logC) + c]);
+        return acc;
+    }
+    const int lane = tid & 31, warp = tid >> 5;
+    V incl = part;
+    for (int d = C; d < 32; d <<= 1) {
+        const V o = shfl_up_v(incl, d);
+        if (lane >= d) incl = add(o, incl);
+    }
+    const V prv = shfl_up_v(incl, C);
+    if (lane >= C) acc = prv;
+    if (lane >= 32 - C) tot[warp * C + (lane & (C - 1))] = incl;  // the warp's total of column `lane & (C-1)`
+    __syncthreads();
+    V before = zero;
+    for (int w2 = 0; w2 < warp; ++w2) before = add(before, tot[w2 * C + c]);
+    return add(before, acc);
+}
+
 // Two FP32 lanes in one 64-bit register for the packed f32x2 arithmetic of sm_100 and later.
 struct f2x {
     unsigned long long v;

@@ -459,7 +459,10 @@ __device__ __forceinline__ void pack_half_spectrum(float2* Z, int C, int logC, i
     }
 }
 
-__global__ void __launch_bounds__(256) k_time_adj(const float2* __restrict__ E, const float2* __restrict__ G,
+// 16 time samples per thread, ET complex FFT elements per thread (8: 512 threads for 2048 complex
+// elements per column block, the layout the launcher picks).
+template <int ET>
+__global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* __restrict__ E, const float2* __restrict__ G,
                                                   float2* __restrict__ gE, const float* __restrict__ ng,
                                                   const float* __restrict__ wv, const float* __restrict__ filt,
                                                   const float2* __restrict__ tw, int twLog, TimeParams tp,
@@ -474,7 +477,7 @@ __global__ void __launch_bounds__(256) k_time_adj(const float2* __restrict__ E, 
     float2* Zl = sa + 4 * R;   // gpl pairs
     float2* twl = sa + 5 * R;
     ffloat* tot = reinterpret_cast<ffloat*>(twl + (Nt >> 1));
-    __shared__ double red_sh[8];
+    __shared__ double red_sh[32];
     const int tid = threadIdx.x, T = blockDim.x;
     const size_t col0 = (size_t)blockIdx.x * C;
     const bool ionize = tp.rate_form != UPPE_RATE_NONE;
@@ -506,9 +509,9 @@ __global__ void __launch_bounds__(256) k_time_adj(const float2* __restrict__ E, 
             return cscale(cmul(Za[k * C + c], make_float2(tp.damping, -wk)), rden * wt * filt[k]);
         }, tid, T);
     __syncthreads();
-    fft_axis_tw<16>(Ze, tp.logM, logC, 1, C, tws, true, tid, T);
-    fft_axis_tw<16>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
-    if (ionize) fft_axis_tw<16>(Zl, tp.logM, logC, 1, C, tws, true, tid, T);
+    fft_axis_tw<ET>(Ze, tp.logM, logC, 1, C, tws, true, tid, T);
+    fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
+    if (ionize) fft_axis_tw<ET>(Zl, tp.logM, logC, 1, C, tws, true, tid, T);
 
     // ---- 2. forward sources along t (ne and ng w exp(-S)), as in k_time ----
     const int c = tid & (C - 1);
@@ -519,7 +522,11 @@ __global__ void __launch_bounds__(256) k_time_adj(const float2* __restrict__ E, 
     const float ngc = ng[col0 + c];
     const float kerr = ngc * tp.redchi3;
     const float inv = tp.inv_nt;
-    const int nseg = T >> logC;
+    const int plain = tp.plain;
+    const auto ffsum = [plain](ffloat x, ffloat y) {
+        if (plain) return ffloat{x.hi + y.hi, 0.f};
+        return ff_add(x, y);
+    };
     if (ionize) {
         float r_next = 0.f;
         if (t1 <= Nt - 2) r_next = ion_rate(tp, Ze[(t1 >> 1) * C + c].x * inv);
@@ -535,10 +542,7 @@ __global__ void __launch_bounds__(256) k_time_adj(const float2* __restrict__ E, 
             rn = r0;
             Zn[m * C + c] = make_float2(r0, r1);
         }
-        tot[tid] = part;
-        __syncthreads();
-        ffloat Sacc = {0.f, 0.f};
-        for (int s2 = seg + 1; s2 < nseg; ++s2) Sacc = ff_add(Sacc, tot[(s2 << logC) + c]);
+        ffloat Sacc = later_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
         rn = r_next;
         for (int m = m0 + mps - 1; m >= m0; --m) {
             const float2 rr = Zn[m * C + c];
@@ -565,9 +569,7 @@ __global__ void __launch_bounds__(256) k_time_adj(const float2* __restrict__ E, 
             acc_add(part, l2.x * e2.x * inv * a2.x, tp.plain);
             acc_add(part, l2.y * e2.y * inv * a2.y, tp.plain);
         }
-        tot[tid] = part;
-        __syncthreads();
-        for (int s2 = 0; s2 < seg; ++s2) carry = ff_add(carry, tot[(s2 << logC) + c]);
+        carry = earlier_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
     }
     // ---- 4. pointwise cotangent of e(t), written over the e pairs ----
     float dred_part = 0.f;
@@ -605,19 +607,24 @@ __global__ void __launch_bounds__(256) k_time_adj(const float2* __restrict__ E, 
             Ze[m * C + c] = make_float2(ge[0], ge[1]);
         }
     }
-    // block reduction of the chi3 derivative
+    // block reduction of the chi3 derivative (a block of fewer than 32 threads reduces through shared memory)
     double dsum = (double)dred_part;
-    for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
-    if ((tid & 31) == 0) red_sh[tid >> 5] = dsum;
+    if (T >= 32) {
+        for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+        if ((tid & 31) == 0) red_sh[tid >> 5] = dsum;
+    } else {
+        red_sh[tid] = dsum;
+    }
     __syncthreads();
     if (tid == 0) {
         double b = 0.0;
-        for (int i = 0; i < (T >> 5); ++i) b += red_sh[i];
+        const int nred = (T >= 32) ? (T >> 5) : T;
+        for (int i = 0; i < nred; ++i) b += red_sh[i];
         atomicAdd(dred, b);
     }
 
     // ---- 5. transpose of irfft: gE = (1/Nt) W2 rfft(ge) ----
-    fft_axis_tw<16>(Ze, tp.logM, logC, 1, C, tws, false, tid, T);
+    fft_axis_tw<ET>(Ze, tp.logM, logC, 1, C, tws, false, tid, T);
     for (int it = tid; it < (M + 1) * C; it += T) {
         const int cc = it & (C - 1);
         const int k = it >> logC;
@@ -629,15 +636,29 @@ __global__ void __launch_bounds__(256) k_time_adj(const float2* __restrict__ E, 
 }
 
 cudaError_t uppe_configure_time_adj_kernel(size_t smem_bytes) {
-    return cudaFuncSetAttribute(k_time_adj, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    return cudaFuncSetAttribute(k_time_adj<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+}
+
+// Columns per block of the adjoint time pass: five (M + 1)-point arrays per column in shared
+// memory, sized for two blocks per multiprocessor (2048 complex elements per block), 16 samples and
+// 8 FFT elements per thread.
+static int adjoint_cols(const UppeHandle* h) {
+    int c = 2048 / h->M;
+    if (c < 1) c = 1;
+    if (c > 16) c = 16;
+    if (c > h->S) c = h->S;
+    return c;
 }
 
 cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G, float2* gE, double* dred) {
     TimeParams tp = uppe_time_params(h);
-    const int T = h->Nt * h->time_cols / 32;
-    tp.spt = 32;
-    const size_t smem = ((size_t)(h->M + 1) * 5 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
+    const int Ca = adjoint_cols(h);
+    tp.C = Ca;
+    tp.logC = ilog2_exact(Ca);
+    tp.spt = 16;
+    const int T = h->Nt * Ca / 16;
+    const size_t smem = ((size_t)(h->M + 1) * 5 * Ca + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
     h->launches++;
-    k_time_adj<<<h->S / h->time_cols, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred);
+    k_time_adj<8><<<h->S / Ca, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred);
     return cudaGetLastError();
 }
