@@ -113,6 +113,7 @@ static void free_buffers(UppeHandle* h) {
     void* ptrs[] = {h->q,  h->qi,   h->qf,   h->k1,   h->E,     h->J,      h->scratch, h->opK,  h->opKi, h->kg2,
                     h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red, h->dev_err, h->Minv_tc, h->Mfwd_tc,
                     h->adj_q1, h->adj_q2, h->adj_q3, h->adj_lf, h->adj_acc, h->adj_lk, h->adj_mu, h->MfwdT, h->MinvT,
+                    h->adj_E[0], h->adj_E[1], h->adj_E[2],
                     h->dred_d, h->rot};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -769,7 +770,8 @@ static int ensure_adjoint(UppeHandle* h) {
     }
     if (h->adj_mu) return UPPE_OK;
     const size_t fb = h->P * sizeof(float2);
-    float2** bufs[] = {&h->adj_q1, &h->adj_q2, &h->adj_q3, &h->adj_lf, &h->adj_acc, &h->adj_lk, &h->adj_mu};
+    float2** bufs[] = {&h->adj_q1, &h->adj_q2, &h->adj_q3,   &h->adj_lf,   &h->adj_acc,
+                       &h->adj_lk, &h->adj_E[0], &h->adj_E[1], &h->adj_E[2], &h->adj_mu};  // adj_mu last: the "allocated" mark
     for (float2** b : bufs) CUDA_TRY(h, cudaMalloc((void**)b, fb));
     CUDA_TRY(h, cudaMalloc((void**)&h->dred_d, sizeof(double)));
     return UPPE_OK;
@@ -780,12 +782,16 @@ static cudaError_t adj_pass(UppeHandle* h, int mode, const float2* in, float2* o
 }
 
 // mu = S'(qs)^H lamk at z = zs (the right-hand side of load_source, uppe_kernel.py:188-216)
-static int vjp_rhs(UppeHandle* h, const float2* qs, double zs, const float2* lamk, float2* mu) {
+// Es: E of (qs, zs) when the recompute kept it, else formed here.
+static int vjp_rhs(UppeHandle* h, const float2* qs, double zs, const float2* lamk, float2* mu, const float2* Es) {
     const StepArgs z = split_z(h, zs);
     h->E_valid = 0;
-    PROF_TRY(h, UPPE_CLASS_OTHER, real_pass(h, REAL_E, qs, nullptr, z));
+    if (!Es) {
+        PROF_TRY(h, UPPE_CLASS_OTHER, real_pass(h, REAL_E, qs, nullptr, z));
+        Es = h->E;
+    }
     PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_S, lamk, h->J, z));
-    PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_adjoint(h, h->E, h->J, h->k1, h->dred_d));
+    PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_adjoint(h, Es, h->J, h->k1, h->dred_d));
     PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_E, h->k1, mu, z));
     return UPPE_OK;
 }
@@ -806,23 +812,34 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
     h->E_valid = 0;
     {
         const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz);
-        // each stage writes its estimate straight into the buffer the reverse sweep reads
-        CUDA_TRY(h, eval_to_J(h, h->qi, z0));
+        // each stage writes its estimate straight into the buffer the reverse sweep reads, and each
+        // evaluation keeps its E (the inverse pass writes into h->E, pointed at adj_E[s] meanwhile)
+        float2* const E_main = h->E;
+        h->E = h->adj_E[0];
+        cudaError_t e = eval_to_J(h, h->qi, z0);
+        h->E = E_main;
+        CUDA_TRY(h, e);
         PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE1, h->J, h->adj_q1, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z0));
-        CUDA_TRY(h, eval_to_J(h, h->adj_q1, zh));
+        h->E = h->adj_E[1];
+        e = eval_to_J(h, h->adj_q1, zh);
+        h->E = E_main;
+        CUDA_TRY(h, e);
         PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE23, h->J, h->adj_q2, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), zh));
-        CUDA_TRY(h, eval_to_J(h, h->adj_q2, zh));
+        h->E = h->adj_E[2];
+        e = eval_to_J(h, h->adj_q2, zh);
+        h->E = E_main;
+        CUDA_TRY(h, e);
         PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE23, h->J, h->adj_q3, h->qf, h->qi, (float)(dz / 3), (float)dz, zh));
     }
     // reverse sweep through the four stages
     CUDA_TRY(h, launch_adj_rk(h, 0, (const float2*)lam_out, nullptr, (float)(dz / 6), 0.f));
-    if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu))) return rc;
+    if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu, nullptr))) return rc;
     CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)dz));
-    if ((rc = vjp_rhs(h, h->adj_q2, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu))) return rc;
+    if ((rc = vjp_rhs(h, h->adj_q2, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu, h->adj_E[2]))) return rc;
     CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)(dz / 2)));
-    if ((rc = vjp_rhs(h, h->adj_q1, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu))) return rc;
+    if ((rc = vjp_rhs(h, h->adj_q1, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu, h->adj_E[1]))) return rc;
     CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 6), (float)(dz / 2)));
-    if ((rc = vjp_rhs(h, q0, z_phase, h->adj_lk, h->adj_mu))) return rc;
+    if ((rc = vjp_rhs(h, q0, z_phase, h->adj_lk, h->adj_mu, h->adj_E[0]))) return rc;
     CUDA_TRY(h, launch_adj_rk(h, 2, nullptr, (float2*)lam_in, 0.f, 0.f));
     if (dred_out) {
         double d = 0.0;
