@@ -193,11 +193,11 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
     } else {
         __syncthreads();  // pass 2 overwrites pairs that pass 1 of the previous segment read
     }
+    // no rate in this segment and none in the later ones: the density is zero throughout
+    const bool dens = ionize && (live || Sacc.hi != 0.f || Sacc.lo != 0.f);
     {
         float rn = r_next;
         const int wlo = tp.wcut + tp.wwid, whi = Nt - tp.wcut - tp.wwid - 1;  // window is 1 on [wlo, whi]
-        // no rate in this segment and none in the later ones: the density is zero throughout
-        const bool dens = ionize && (live || Sacc.hi != 0.f || Sacc.lo != 0.f);
 #pragma unroll(CT ? 8 : 1)
         for (int m = m0 + mps - 1; m >= m0; --m) {
             const float2 zv = Zp[m * C + c];
@@ -229,10 +229,11 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
             }
         }
     }
-    __syncthreads();
+    // a block whose density is zero everywhere has Jpl = 0: its transform is left out (exactly zero)
+    const bool any_ne = __syncthreads_or(dens ? 1 : 0) != 0;
 
     // ---- 3. forward FFTs (P, then Jpl) and the current ----
-    const bool two = ionize || mode == TIME_CHI_NE;
+    const bool two = any_ne || mode == TIME_CHI_NE;
     if constexpr (CT) {
         fft_axis_ct<ET, LOGM, LOGC, LOGM + 1>(Zp, TwHalfSharedCT<LOGM + 1>{twl}, false, tid);
         if (two) fft_axis_ct<ET, LOGM, LOGC, LOGM + 1>(Zj, TwHalfSharedCT<LOGM + 1>{twl}, false, tid);
@@ -251,7 +252,7 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
         if (mode == TIME_J) {
             const float wk = wv[k];
             float2 J = cmul_mi(cscale(P, wk));  // -i w P
-            if (ionize) {  // Jpl / (damping - i w) = Jpl (damping + i w) / (damping^2 + w^2)
+            if (two) {  // Jpl / (damping - i w) = Jpl (damping + i w) / (damping^2 + w^2)
                 const float rden = __frcp_rn(fmaf(wk, wk, tp.damping * tp.damping));
                 J = cadd(J, cscale(cmul(Q, make_float2(tp.damping, wk)), rden));
             }
@@ -511,7 +512,6 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
     __syncthreads();
     fft_axis_tw<ET>(Ze, tp.logM, logC, 1, C, tws, true, tid, T);
     fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
-    if (ionize) fft_axis_tw<ET>(Zl, tp.logM, logC, 1, C, tws, true, tid, T);
 
     // ---- 2. forward sources along t (ne and ng w exp(-S)), as in k_time ----
     const int c = tid & (C - 1);
@@ -527,11 +527,15 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
         if (plain) return ffloat{x.hi + y.hi, 0.f};
         return ff_add(x, y);
     };
+    // With no nonzero rate anywhere in the block the density, the plasma-current cotangent and the
+    // rate-derivative terms are all zero: `ion` leaves them out (and the inverse FFT of gpl).
+    bool ion = false;
+    float r_next = 0.f;
+    ffloat part = {0.f, 0.f};
     if (ionize) {
-        float r_next = 0.f;
         if (t1 <= Nt - 2) r_next = ion_rate(tp, Ze[(t1 >> 1) * C + c].x * inv);
-        ffloat part = {0.f, 0.f};
         float rn = r_next;
+        bool live = r_next != 0.f;
         for (int m = m0 + mps - 1; m >= m0; --m) {
             const float2 zv = Ze[m * C + c];
             const int t = 2 * m + 1;
@@ -539,11 +543,15 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
             if (t <= Nt - 2) acc_add(part, tp.hdt * (r1 + rn), tp.plain);
             const float r0 = ion_rate(tp, zv.x * inv);
             acc_add(part, tp.hdt * (r0 + r1), tp.plain);
+            live = live || r0 != 0.f || r1 != 0.f;
             rn = r0;
             Zn[m * C + c] = make_float2(r0, r1);
         }
+        ion = __syncthreads_or(live ? 1 : 0) != 0;
+    }
+    if (ion) {
         ffloat Sacc = later_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
-        rn = r_next;
+        float rn = r_next;
         for (int m = m0 + mps - 1; m >= m0; --m) {
             const float2 rr = Zn[m * C + c];
             const int t = 2 * m + 1;
@@ -558,11 +566,12 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
             Za[m * C + c] = make_float2(ngc * w0 * expf(-S0), ngc * w1 * expf(-S1));
         }
         __syncthreads();  // segment totals are reused below
+        fft_axis_tw<ET>(Zl, tp.logM, logC, 1, C, tws, true, tid, T);
     }
 
     // ---- 3. transposed scan: Pfx(j) = sum_{t <= j} gpl e a, two passes in increasing t ----
     ffloat carry = {0.f, 0.f};
-    if (ionize) {
+    if (ion) {
         ffloat part = {0.f, 0.f};
         for (int m = m0; m < m0 + mps; ++m) {
             const float2 e2 = Ze[m * C + c], l2 = Zl[m * C + c], a2 = Za[m * C + c];
@@ -587,7 +596,7 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
                 const float e = ev[h];
                 float g = 3.f * kerr * e * e * gp[h];
                 dred_part = fmaf(gp[h] * ngc * e * e, e, dred_part);
-                if (ionize) {
+                if (ion) {
                     const float2 l2 = Zl[m * C + c], n2 = Zn[m * C + c], a2 = Za[m * C + c];
                     const float gl = h ? l2.y : l2.x;
                     const float ne = h ? n2.y : n2.x;
