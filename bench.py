@@ -270,6 +270,18 @@ def run_e2e(args, vd):
     return P * args.steps / wall, h2d, d2h, bool(np.isfinite(A[..., -1]).all())
 
 
+def aggregate_replicas(ms, points, steps, ws, device):
+    """Whole-job rate of N independent replicas (one per rank, no collective on the data path): the
+    points*steps of all ranks over the slowest rank's time, taken as the MAX over ranks of ms.
+    Returns (rate, ms)."""
+    import torch
+    if ws > 1:
+        t = torch.tensor([ms], device=device, dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    return points * steps * ws / (ms / 1e3), ms
+
+
 def cpu_cores():
     try:
         return len(os.sched_getaffinity(0))
@@ -373,11 +385,7 @@ def main():
     else:
         torch.cuda.set_device(0)
     P, ms, launches, clk, prof, finite, adj_ms = run_device(args, vd, ws, rank, local)
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = P * args.steps * ws / (ms / 1e3)
+    value, ms = aggregate_replicas(ms, P, args.steps, ws, "cuda")
     peak, tpeak, peak_kind = measured_peaks()
     models = class_models(vd)
     tensor_path = vd["wave coordinates"] != "cartesian" and args.precision == "mixed"

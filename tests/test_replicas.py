@@ -1,0 +1,64 @@
+"""bench.py at N > 1: one independent replica per rank (the path does not shard), the job's rate
+taken over the slowest rank.  Two ranks over gloo on CPU, as torchrun starts them (RANK,
+WORLD_SIZE, MASTER_ADDR 127.0.0.1); the reference arm runs on rank 0 alone."""
+import multiprocessing as mp
+import os
+import socket
+import sys
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _replica(rank, ws, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(ws),
+                      LOCAL_RANK=str(rank))
+    sys.path.insert(0, ROOT)
+    import torch.distributed as dist
+    import bench
+    assert bench.dist_env() == (ws, rank, rank)
+    dist.init_process_group("gloo", rank=rank, world_size=ws)
+    ms = 10.0 + 2.5 * rank  # rank 1 is the slower replica
+    value, ms_max = bench.aggregate_replicas(ms, 1000, 4, ws, "cpu")
+    dist.destroy_process_group()
+    q.put((rank, value, ms_max))
+
+
+def test_two_replicas_report_the_slowest_rank():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_replica, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    for p in procs:
+        p.join(timeout=180)
+    assert all(p.exitcode == 0 for p in procs)
+    res = sorted(q.get(timeout=10) for _ in range(2))
+    for rank, value, ms_max in res:
+        assert ms_max == 12.5
+        assert value == 1000 * 4 * 2 / 12.5e-3
+
+
+def test_single_rank_needs_no_process_group():
+    sys.path.insert(0, ROOT)
+    import bench
+    value, ms = bench.aggregate_replicas(8.0, 500, 10, 1, "cpu")
+    assert ms == 8.0 and value == 500 * 10 / 8e-3
+
+
+def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
+    sys.path.insert(0, ROOT)
+    import bench
+    calls = []
+    monkeypatch.setattr(bench, "oracle_step_time", lambda *a, **k: calls.append(1) or (0.0, 1, (1, 1, 1)))
+
+    class Args:
+        steps, warmup, workload = 2, 3, "cart_filament_128"
+    bench.reference_arm(Args(), {}, 2, 1)
+    assert calls == [] and capsys.readouterr().out == ""
