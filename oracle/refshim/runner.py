@@ -134,3 +134,18 @@ def reference_paraxial(vol_dict, quiet=True):
     with contextlib.redirect_stdout(out) if quiet else contextlib.nullcontext():
         A, J, chi, ne, dom4d = m["paraxial_kernel"].track(_CL, xp, eikonal, vg, vd)
     return A, J, chi, ne, dom4d, out.getvalue()
+
+
+def reference_paraxial_rays(vol_dict, xp, eikonal, vg, quiet=True):
+    """Run ``paraxial_kernel.track`` on the given rays (no ``incoming wave``); returns its outputs and
+    the relaunched ray arrays (copies)."""
+    cl_refs()
+    m = modules()
+    vd = dict(vol_dict)
+    if "object" not in vd:
+        vd["object"] = DensityObject(vd)
+    xp, eikonal, vg = np.array(xp), np.array(eikonal), np.array(vg)
+    out = io.StringIO()
+    with contextlib.redirect_stdout(out) if quiet else contextlib.nullcontext():
+        A, J, chi, ne, dom4d = m["paraxial_kernel"].track(_CL, xp, eikonal, vg, vd)
+    return A, J, chi, ne, dom4d, xp, eikonal, vg

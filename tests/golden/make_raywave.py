@@ -4,7 +4,8 @@ For three field grids (Cartesian 33x16x16, cylindrical 33x32x1, cylindrical with
 33x16x4) it runs SeaRay's own ``caustic_tools`` field tools on seeded synthetic rays:
 ``GetBoundaryFields`` (component 1), ``RelaunchRays`` and ``RelaunchRays1``, and stores inputs and
 outputs.  It also runs the reference's whole ``uppe_kernel.track`` from rays (no ``incoming
-wave``) on a small Cartesian Kerr volume (``raywave_track_cart.npz``).
+wave``) on a small Cartesian Kerr volume (``raywave_track_cart.npz``), and its paraxial
+``paraxial_kernel.track`` on such a volume with an envelope band (``raywave_paraxial_cart.npz``).
 
 The reference's cylindrical ``RelaunchRays1`` calls ``scipy.integrate.cumtrapz``, which SciPy has
 since renamed ``cumulative_trapezoid`` (same trapezoid rule); the name is supplied before the call.
@@ -37,13 +38,13 @@ TOOLS = {
 }
 
 
-def make_rays(wn, cartesian, half_width, rng, per_bin=40):
-    """Bundles of 4 rays: primaries at every frequency node (the first node nudged above w = 0),
-    spread over the grid and a little beyond; satellites displaced by 0.5 in x, y, x+y."""
+def make_rays(wn, cartesian, half_width, rng, per_bin=40, nudge_first=True):
+    """Bundles of 4 rays: primaries at every frequency node (the first node nudged above w = 0 when
+    nudge_first), spread over the grid and a little beyond; satellites displaced by 0.5 in x, y, x+y."""
     dw = wn[1] - wn[0]
     prim = []
     for i, w in enumerate(wn):
-        wv = w if i > 0 else 0.25 * dw
+        wv = w if (i > 0 or not nudge_first) else 0.25 * dw
         if cartesian:
             r = 1.03 * half_width
             corners = np.array([[-r, -r], [-r, r], [r, -r], [r, r]])
@@ -131,16 +132,42 @@ def track_fixture(m, cl, rng):
     print("track from rays: max |A0|", np.abs(A[..., 0]).max(), "max |A|", np.abs(A[..., 1]).max())
 
 
-def main():
+def paraxial_fixture(m, cl, rng):
+    medium = m["dispersion"].SimpleAir(cases.MKS_LENGTH)
+    N = (64, 16, 16, 2)
+    band = (0.5, 1.5)
+    vd = {"wave grid": N, "wave coordinates": "cartesian", "frequency band": band,
+          "size": (1200.0, 1200.0, 4000.0), "subcycles": 2, "chi3": 0.6,
+          "density reference": 1.0, "window speed": 1.0, "dispersion inside": medium, "ionizer": None,
+          "density lambda": lambda x, y, z, r2: np.ones(x.shape), "full relaunch": False}
+    ft = m["caustic_tools"].FourierTool(N, band, (0, 0, 0), vd["size"], cl)
+    wn = ft.GetGridInfo()[0]
+    xp, eik, vg = make_rays(wn, True, 600.0, rng, per_bin=32, nudge_first=False)
+    eik[:, 1:3] *= 0.02
+    A, J, chi, ne, dom4d, xp2, eik2, vg2 = runner.reference_paraxial_rays(vd, xp, eik, vg)
+    wu = np.unique(xp[..., 4])
+    np.savez_compressed(HERE / "raywave_paraxial_cart.npz", N=np.array(N), band=np.array(band), xp=xp, eik=eik,
+                        vg=vg, chi_w=medium.chi(wn), A=A[..., 1:], J=J[..., 1:], chiNL=chi[..., 1:], ne=ne[..., 1:],
+                        A0=A[..., 0], dom4d=dom4d, xp_out=xp2, eik_out=eik2, vg_out=vg2, vg_w=wu,
+                        vg_v=medium.GroupVelocityMagnitude(wu))
+    print("paraxial track from rays: max |A0|", np.abs(A[..., 0]).max(), "max |A|", np.abs(A[..., 1]).max())
+
+
+def main(names=None):
     if not runner.available():
         raise SystemExit("reference tree not found")
     cl = runner.cl_refs()
     m = runner.modules()
     rng = np.random.default_rng(7)
+    if names:  # only the named fixtures ("paraxial"), with their own seed
+        if "paraxial" in names:
+            paraxial_fixture(m, cl, np.random.default_rng(11))
+        return
     for name in TOOLS:
         tool_fixture(name, m, cl, rng)
     track_fixture(m, cl, rng)
+    paraxial_fixture(m, cl, np.random.default_rng(11))
 
 
 if __name__ == "__main__":
-    main()
+    main(sys.argv[1:])

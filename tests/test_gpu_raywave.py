@@ -73,3 +73,35 @@ def test_track_from_rays_matches_reference(precision):
     assert np.allclose(xp, d["xp_out"], rtol=1e-12, atol=1e-12)
     assert np.allclose(vg, d["vg_out"], rtol=1e-12, atol=1e-12)
     assert np.max(np.abs(ne[..., 1:])) == 0
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp32"])
+def test_paraxial_track_from_rays_matches_reference(precision):
+    """The reference's ray-started paraxial volume (raywave_paraxial_cart.npz: envelope band
+    0.5-1.5, 64 x 16 x 16, Kerr) through searay_gb300.paraxial.track, same bounds as above."""
+    from searay_gb300 import grid, paraxial
+    d = np.load(GOLD / "raywave_paraxial_cart.npz")
+    N = tuple(int(n) for n in d["N"])
+    vd = {"wave grid": N, "wave coordinates": "cartesian", "frequency band": tuple(d["band"]),
+          "size": (1200.0, 1200.0, 4000.0), "subcycles": 2, "chi3": 0.6, "density reference": 1.0,
+          "window speed": 1.0, "ionizer": None, "density lambda": lambda x, y, z, r2: np.ones(x.shape),
+          "full relaunch": False, "precision": precision}
+    w = grid.VolumeGrid(vd).w
+    vd["dispersion inside"] = StoredMedium(w, d["chi_w"], d["vg_w"], d["vg_v"])
+    xp, eik, vg = d["xp"].copy(), d["eik"].copy(), d["vg"].copy()
+    A, J, chi, ne, dom4d = paraxial.track(None, xp, eik, vg, vd)
+    assert np.allclose(dom4d, d["dom4d"], rtol=1e-12)
+    errs = {"A0": rel(A[..., 0], d["A0"]), "A": rel(A[..., 1:], d["A"]), "J": rel(J[..., 1:], d["J"]),
+            "chi": rel(chi[..., 1:], d["chiNL"])}
+    amp_ref = d["eik_out"][:, 1]
+    errs["amp"] = np.max(np.abs(eik[:, 1] - amp_ref)) / np.max(np.abs(amp_ref))
+    strong = np.abs(amp_ref) > 0.01 * np.max(np.abs(amp_ref))
+    dphi = np.angle(np.exp(1j * (eik[strong, 0] - d["eik_out"][strong, 0])))
+    errs["phase"] = np.max(np.abs(dphi))
+    print("paraxial", precision, {k: f"{v:.2e}" for k, v in errs.items()})
+    assert errs["A0"] < 1e-10
+    assert errs["A"] < 2e-5 and errs["J"] < 1e-4 and errs["chi"] < 1e-4
+    assert errs["amp"] < 1e-5 and errs["phase"] < 1e-4
+    assert np.allclose(xp, d["xp_out"], rtol=1e-12, atol=1e-12)
+    assert np.allclose(vg, d["vg_out"], rtol=1e-12, atol=1e-12)
+    assert np.max(np.abs(ne[..., 1:])) == 0

@@ -85,3 +85,24 @@ def test_missing_frequency_bin_raises():
     keep = xps[:, 4] > 0.5  # no rays in the low bins
     with pytest.raises(ValueError, match="no rays found in frequency bin"):
         raywave.boundary_fields(fg, xps[keep], d["eik"][keep], 1)
+
+
+def _paraxial_grid(d):
+    vd = {"wave grid": tuple(int(n) for n in d["N"]), "wave coordinates": "cartesian",
+          "frequency band": tuple(d["band"]), "size": (1200.0, 1200.0, 4000.0)}
+    return raywave.FieldGrid(grid.VolumeGrid(vd))
+
+
+def test_paraxial_boundary_field_and_relaunch():
+    """The host ray <-> wave steps of the reference's ray-started paraxial volume (envelope band
+    0.5-1.5, raywave_paraxial_cart.npz): the first plane from the rays, and the relaunch from the
+    reference's own last plane."""
+    d = np.load(GOLD / "raywave_paraxial_cart.npz")
+    fg = _paraxial_grid(d)
+    bf = raywave.boundary_fields(fg, d["xp"][:, 0, :], d["eik"], 1)
+    assert close(bf, d["A0"], 1e-10)
+    xp, eik, vg = d["xp"].copy(), d["eik"].copy(), d["vg"].copy()
+    raywave.relaunch_rays(fg, xp, eik, vg, d["A"][..., -1], 4000.0, TableMedium(d["vg_w"], d["vg_v"]))
+    for got, ref in ((xp, d["xp_out"]), (eik, d["eik_out"]), (vg, d["vg_out"])):
+        assert np.array_equal(np.isnan(got), np.isnan(ref))
+        assert close(np.nan_to_num(got), np.nan_to_num(ref))
