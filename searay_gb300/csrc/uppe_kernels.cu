@@ -76,11 +76,44 @@ __global__ void k_build_operator_env(const double* __restrict__ fw, const double
     opKi[idx] = (float)(fw[2 * iw + 1] * r);
 }
 
+// The same operator for a real medium (Im w^2 (1 + chi0) = 0 at every w), mostly on the FP32 units:
+// a = w^2 n^2 - kperp^2 in FP64, kz = sqrt(a) as float-float (the FP32 root plus one Newton step from
+// the residual a - r^2 taken in FP64, about 2^-48 relative, the rounding of the FP64 form), K = kz + kg.
+// The reference's guards for a real argument: a <= 0 gives Re kz = 0, replaced by kz = 1
+// (uppe_kernel.py:83-84); Im kz = 0.
+__global__ void k_build_operator_real(const double* __restrict__ w2n2, const float2* __restrict__ kg2,
+                                      const double* __restrict__ kr2, float2* __restrict__ opK,
+                                      float* __restrict__ opKi, int N0, int S) {
+    size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (size_t)N0 * S) return;
+    int iw = (int)(idx / S);
+    int s = (int)(idx - (size_t)iw * S);
+    const double a = w2n2[2 * iw] - kr2[s];
+    ffloat kz;
+    if (a > 0.0) {
+        const float r = sqrtf((float)a);
+        // the residual a - r^2 in FP64 (r^2 of an FP32 r is exact in FP64), then one Newton step
+        const double res = a - (double)r * (double)r;
+        kz = ff_two_sum(r, (float)res / (2.f * r));
+    } else {
+        kz = ffloat{1.f, 0.f};
+    }
+    const float2 kg = kg2[iw];
+    const ffloat K = ff_add(kz, ffloat{kg.x, kg.y});
+    opK[idx] = make_float2(K.hi, K.lo);
+    opKi[idx] = 0.f;
+}
+
 cudaError_t launch_build_operator(UppeHandle* h) {
     size_t n = h->P;
     int threads = 256;
     unsigned blocks = (unsigned)((n + threads - 1) / threads);
     h->launches++;
+    if (!h->cfg.envelope && !h->complex_medium) {
+        k_build_operator_real<<<blocks, threads, 0, h->stream>>>(h->w2n2_d, h->kg2, h->kr2_d, h->opK, h->opKi, h->N0,
+                                                                  h->S);
+        return cudaGetLastError();
+    }
     if (h->cfg.envelope)
         k_build_operator_env<<<blocks, threads, 0, h->stream>>>(h->w2n2_d, h->kg_d, h->kr2_d, h->opK, h->opKi, h->N0,
                                                                 h->S);
