@@ -17,6 +17,7 @@
 #include "uppe_internal.h"
 
 void uppe_split_matrix_tiles(const float* B, int N2, int NI, int NK, std::vector<uint8_t>& out);
+size_t uppe_hankel_tc_atile_bytes(int N0, int N1, int N2);
 
 static char g_create_error[512] = "";
 
@@ -114,7 +115,7 @@ static void free_buffers(UppeHandle* h) {
                     h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red, h->dev_err, h->Minv_tc, h->Mfwd_tc,
                     h->adj_q1, h->adj_q2, h->adj_q3, h->adj_lf, h->adj_acc, h->adj_lk, h->adj_mu, h->MfwdT, h->MinvT,
                     h->adj_E[0], h->adj_E[1], h->adj_E[2],
-                    h->dred_d, h->rot};
+                    h->dred_d, h->rot, h->Atc};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -356,6 +357,10 @@ extern "C" int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, 
             uppe_split_matrix_tiles(Mfwd.data(), Nm, Nr, Nr, t);
             if (!h->Mfwd_tc) CUDA_TRY(h, cudaMalloc((void**)&h->Mfwd_tc, t.size()));
             CUDA_TRY(h, cudaMemcpy(h->Mfwd_tc, t.data(), t.size(), cudaMemcpyHostToDevice));
+            if (!h->Atc) {
+                h->Atc_bytes = uppe_hankel_tc_atile_bytes(h->N0, Nr, Nm);
+                CUDA_TRY(h, cudaMalloc((void**)&h->Atc, h->Atc_bytes));
+            }
         }
     }
     h->have_grid = 1;

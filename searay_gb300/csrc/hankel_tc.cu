@@ -7,7 +7,10 @@
 //     A_hi B_hi + A_hi B_lo + A_lo B_hi in FP32 (the dropped A_lo B_lo is ~2^-18 of the product);
 //   * one elected thread issues tcgen05.mma (M=128, N=128, K=16) from shared-memory operands in the
 //     no-swizzle K-major core-matrix layout; the accumulator lives in tensor memory (TMEM) and is
-//     read back with tcgen05.ld for the fused epilogue (store, finish, or ODE RHS + RK stage).
+//     read back with tcgen05.ld for the fused epilogue (store, finish, or ODE RHS + RK stage);
+//   * the A operand (the field with its propagator phase and i kz where the mode asks) is formed and
+//     split once per transform by k_hankel_tc_prep into tiles in that same layout, so every output
+//     tile fills its stages with 16-byte asynchronous copies, as it does for B.
 // Every wait on an mbarrier is bounded; on expiry the kernel records an error flag and skips ahead.
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -26,13 +29,14 @@
 #define TC_STAGE_LD (TC_N + 1)              // padded row of the epilogue staging tile (float2)
 #define TC_WAIT_LIMIT (1 << 24)
 
-enum { TA_PLAIN = 0, TA_QPHASE_IKZ = 1, TA_QPHASE = 2 };
+enum { TA_PLAIN = 0, TA_QPHASE_IKZ = 1, TA_QPHASE = 2, TA_PRESPLIT = 3 };
 enum { TC_STORE = 0, TC_FINISH1 = 1, TC_SPEC = 2 };
 
 struct TcArgs {
     const float2* A;
     const uint8_t* Btc;  // split matrix tiles [N2][nit][nkt][hi 16 KB | lo 16 KB]
-    int nit, nkt;
+    const uint8_t* Atc;  // split field tiles [N2][nwt][nkt][hi 16 KB | lo 16 KB] (TA_PRESPLIT)
+    int nit, nkt, nwt;
     OpView op;
     float2* C0;
     float2* C1;
@@ -102,6 +106,15 @@ __device__ __forceinline__ void tc_load_tile(const TcArgs& g, uint8_t* st, uint3
                                              int w0, int k0, int m, const PhaseArgs& pa, int tid) {
     for (int c = tid; c < 2 * TC_TILE_BYTES / 16; c += TC_THREADS)
         cp_async16(st_a + 2 * TC_TILE_BYTES + 16 * c, Btile + 16 * c);
+    if constexpr (AMODE == TA_PRESPLIT) {
+        const uint8_t* Atile =
+            g.Atc + (((size_t)m * g.nwt + w0 / TC_W) * g.nkt + k0 / TC_K) * (size_t)(2 * TC_TILE_BYTES);
+        for (int c = tid; c < 2 * TC_TILE_BYTES / 16; c += TC_THREADS) cp_async16(st_a + 16 * c, Atile + 16 * c);
+        asm volatile("cp.async.commit_group;\n" ::);
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+        return;
+    }
     asm volatile("cp.async.commit_group;\n" ::);
 #pragma unroll 4
     for (int e = tid; e < TC_W * TC_K; e += TC_THREADS) {
@@ -156,6 +169,40 @@ __device__ __forceinline__ void tc_issue(uint32_t tmem_d, uint32_t st_a, uint32_
     }
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
                  : "memory");
+}
+
+// The A operand tiles of one transform: element (w, k) of azimuthal mode m, with the propagator phase
+// and i kz as AMODE asks (the arithmetic of tc_load_tile), split into bf16 hi/lo at rows 2(w - w0)
+// and 2(w - w0) + 1 of its tile, zero outside [N0) x [NK).  One thread per element of the padded
+// [nwt * 64][nkt * 64] grid; consecutive threads take consecutive k.
+template <int AMODE>
+__global__ void __launch_bounds__(256) k_hankel_tc_prep(TcArgs g, uint8_t* __restrict__ Atc) {
+    const int m = blockIdx.y;
+    const int KP = g.nkt * TC_K;
+    const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (size_t)g.nwt * TC_W * KP) return;
+    const int k = (int)(e % KP), w = (int)(e / KP);
+    const PhaseArgs pa{g.z.zhi, g.z.zlo, g.z.plain};
+    float2 v = make_float2(0.f, 0.f);
+    if (w < g.N0 && k < g.NK) {
+        const size_t idx = ((size_t)w * g.N1 + k) * g.N2 + m;
+        v = g.A[idx];
+        if (AMODE != TA_PLAIN) {
+            const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
+            v = cmul(propagator_factor(o, pa, 1.f), v);
+            if (AMODE == TA_QPHASE_IKZ) v = op_field(g.op, o, v);
+        }
+    }
+    __nv_bfloat16 rh, rl, ih, il;
+    split_bf16(v.x, rh, rl);
+    split_bf16(v.y, ih, il);
+    const int wl = w % TC_W, kk = k % TC_K;
+    uint8_t* tile = Atc + (((size_t)m * g.nwt + w / TC_W) * g.nkt + k / TC_K) * (size_t)(2 * TC_TILE_BYTES);
+    const uint32_t ore = core_off(2 * wl, kk), oim = core_off(2 * wl + 1, kk);
+    *reinterpret_cast<__nv_bfloat16*>(tile + ore) = rh;
+    *reinterpret_cast<__nv_bfloat16*>(tile + oim) = ih;
+    *reinterpret_cast<__nv_bfloat16*>(tile + TC_TILE_BYTES + ore) = rl;
+    *reinterpret_cast<__nv_bfloat16*>(tile + TC_TILE_BYTES + oim) = il;
 }
 
 template <int AMODE, int CMODE>
@@ -338,12 +385,33 @@ cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* 
     a.Ce = Ce;
     a.z = z;
     a.err = h->dev_err;
-    if (amode == TA_PLAIN && cmode == TC_STORE) return run_tc<TA_PLAIN, TC_STORE>(h, a);
-    if (amode == TA_PLAIN && cmode == TC_SPEC) return run_tc<TA_PLAIN, TC_SPEC>(h, a);
-    if (amode == TA_QPHASE_IKZ && cmode == TC_STORE) return run_tc<TA_QPHASE_IKZ, TC_STORE>(h, a);
-    if (amode == TA_QPHASE && cmode == TC_STORE) return run_tc<TA_QPHASE, TC_STORE>(h, a);
-    if (amode == TA_QPHASE && cmode == TC_FINISH1) return run_tc<TA_QPHASE, TC_FINISH1>(h, a);
+    a.nwt = (h->N0 + TC_W - 1) / TC_W;
+    a.Atc = h->Atc;
+    // the A operand once per transform (k_hankel_tc_prep), then the GEMM on pre-split tiles
+    if (!h->Atc || (size_t)h->N2 * a.nwt * a.nkt * 2 * TC_TILE_BYTES > h->Atc_bytes) return cudaErrorInvalidValue;
+    {
+        const size_t n = (size_t)a.nwt * TC_W * a.nkt * TC_K;
+        dim3 grid((unsigned)((n + 255) / 256), h->N2);
+        h->launches++;
+        if (amode == TA_PLAIN)
+            k_hankel_tc_prep<TA_PLAIN><<<grid, 256, 0, h->stream>>>(a, h->Atc);
+        else if (amode == TA_QPHASE_IKZ)
+            k_hankel_tc_prep<TA_QPHASE_IKZ><<<grid, 256, 0, h->stream>>>(a, h->Atc);
+        else
+            k_hankel_tc_prep<TA_QPHASE><<<grid, 256, 0, h->stream>>>(a, h->Atc);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (cmode == TC_STORE) return run_tc<TA_PRESPLIT, TC_STORE>(h, a);
+    if (cmode == TC_SPEC) return run_tc<TA_PRESPLIT, TC_SPEC>(h, a);
+    if (cmode == TC_FINISH1) return run_tc<TA_PRESPLIT, TC_FINISH1>(h, a);
     return cudaErrorInvalidValue;
+}
+
+// Bytes of the pre-split A tiles for the transforms of a handle (reduction length up to N1).
+size_t uppe_hankel_tc_atile_bytes(int N0, int N1, int N2) {
+    const size_t nwt = (N0 + TC_W - 1) / TC_W, nkt = (N1 + TC_K - 1) / TC_K;
+    return (size_t)N2 * nwt * nkt * 2 * TC_TILE_BYTES;
 }
 
 // Host: round to the nearest bf16 (ties to even) and back, for the split of the matrices.
