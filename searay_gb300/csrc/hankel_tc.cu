@@ -92,7 +92,7 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
     lo = __float2bfloat16_rn(x - __bfloat162float(hi));
 }
 
-#define TC_THREADS 256
+#define TC_THREADS 512  // 16 warps: the copies and the fused epilogue are spread over more threads
 #define TC_STAGE_BYTES (4 * TC_TILE_BYTES)  // A_hi | A_lo | B_hi | B_lo
 
 __device__ __forceinline__ void cp_async16(uint32_t smem_addr, const void* g) {
@@ -269,13 +269,14 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
     __syncthreads();
 
     // ---- epilogue: TMEM -> registers -> padded staging tile [64][129] complex ----
-    // warps w and w+4 read the same 32 accumulator lanes (lane quarter w % 4), different columns
+    // warp w reads accumulator lanes 32 (w % 4) .. + 31 (the lane quarter a warp may access); the
+    // warps of one quarter take different 32-column chunks
     const int quarter = warp & 3;
     const int row = quarter * 32 + lane;  // accumulator lane = MMA row
     const int wl = row >> 1;
     const int part = row & 1;
 #pragma unroll 1
-    for (int c0 = (warp >> 2) * 32; c0 < TC_N; c0 += 64) {
+    for (int c0 = (warp >> 2) * 32; c0 < TC_N; c0 += (TC_THREADS / 128) * 32) {
         uint32_t r[32];
         const uint32_t taddr = tmem_d + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
         asm volatile(
