@@ -608,10 +608,10 @@ template <int LN1, int LN2>
 __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     k_real_reg(int mode, const float2* __restrict__ src, OpView opv, float2* __restrict__ E,
                float2* __restrict__ A_out, const float2* __restrict__ k1, float2* __restrict__ qf, float Cs, float Ce,
-               const float2* __restrict__ tw, int twLog, StepArgs z) {
+               const float2* __restrict__ tw, int twLog, StepArgs z, int iw0) {
     using RS = RegSlice<LN1, LN2>;
     extern __shared__ float2 sm[];
-    const int tid = threadIdx.x, iw = blockIdx.x;
+    const int tid = threadIdx.x, iw = blockIdx.x + iw0;
     const size_t base = (size_t)iw * RS::S;
     const TwGlobal twg{tw, twLog};
     const RegCoords<RS> c(sm, tid, false);
@@ -628,6 +628,11 @@ __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
             const float2 a = src[idx], s = k1[idx];
             qf[idx] = cadd(a, cscale(s, Cs));
             val = cscale(cadd(a, cscale(s, Ce)), cond);
+        } else if (mode >= REAL_ZS1) {  // src: qi (stages 1-3) or qf (finish); qf: the array written
+            const float2 a = src[idx];
+            val = cscale(a, cond);
+            if (mode == REAL_ZS1) qf[idx] = a;
+            if (mode == REAL_ZSF) qf[idx] = val;
         } else {
             val = src[idx];
         }

@@ -7,11 +7,11 @@ struct FusedReg {
         return cudaFuncSetAttribute(k_fused_reg<LN1, LN2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     FusedPlan<LN1, LN2>::SMEM);
     }
-    static cudaError_t run(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
+    static cudaError_t run(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next, int n) {
         using RS = RegSlice<LN1, LN2>;
-        const int grid = h->N0 < h->num_sms ? h->N0 : h->num_sms;  // persistent: one CTA per multiprocessor
+        const int grid = n < h->num_sms ? n : h->num_sms;  // persistent: one CTA per multiprocessor
         k_fused_reg<LN1, LN2><<<grid, RS::T, FusedPlan<LN1, LN2>::SMEM, h->stream>>>(
-            mode, h->J, uppe_op_view(h), h->qi, h->qf, h->qi, h->E, Cs, Ce, h->tw, h->twLog, z_rhs, z_next, h->N0);
+            mode, h->J, uppe_op_view(h), h->qi, h->qf, h->qi, h->E, Cs, Ce, h->tw, h->twLog, z_rhs, z_next, n);
         return cudaGetLastError();
     }
 };
@@ -25,6 +25,8 @@ cudaError_t configure_fused_reg() {
     return e;
 }
 
-cudaError_t launch_fused_reg(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
-    return reg_dispatch<FusedReg>(h, mode, Cs, Ce, z_rhs, z_next);
+// The fused pass over the slices [0, nslices).
+cudaError_t launch_fused_reg(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next,
+                             int nslices) {
+    return reg_dispatch<FusedReg>(h, mode, Cs, Ce, z_rhs, z_next, nslices);
 }

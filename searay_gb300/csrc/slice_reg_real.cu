@@ -8,10 +8,10 @@ struct RealReg {
                                     RegSlice<LN1, LN2>::SMEM);
     }
     static cudaError_t run(UppeHandle* h, int mode, const float2* src, float2* A_out, const float2* k1, float2* qf,
-                           float Cs, float Ce, StepArgs z) {
+                           float Cs, float Ce, StepArgs z, int iw0, int count) {
         using RS = RegSlice<LN1, LN2>;
-        k_real_reg<LN1, LN2><<<h->N0, RS::T, RS::SMEM, h->stream>>>(mode, src, uppe_op_view(h), h->E, A_out, k1, qf,
-                                                                    Cs, Ce, h->tw, h->twLog, z);
+        k_real_reg<LN1, LN2><<<count, RS::T, RS::SMEM, h->stream>>>(mode, src, uppe_op_view(h), h->E, A_out, k1, qf,
+                                                                    Cs, Ce, h->tw, h->twLog, z, iw0);
         return cudaGetLastError();
     }
 };
@@ -27,5 +27,10 @@ cudaError_t configure_real_reg() {
 
 cudaError_t launch_real_reg(UppeHandle* h, int mode, const float2* src, float2* A_out, const float2* k1, float2* qf,
                             float Cs, float Ce, StepArgs z) {
-    return reg_dispatch<RealReg>(h, mode, src, A_out, k1, qf, Cs, Ce, z);
+    return reg_dispatch<RealReg>(h, mode, src, A_out, k1, qf, Cs, Ce, z, 0, h->N0);
+}
+
+cudaError_t launch_real_reg_range(UppeHandle* h, int mode, const float2* src, float2* A_out, const float2* k1,
+                                  float2* qf, float Cs, float Ce, StepArgs z, int iw0, int count) {
+    return reg_dispatch<RealReg>(h, mode, src, A_out, k1, qf, Cs, Ce, z, iw0, count);
 }

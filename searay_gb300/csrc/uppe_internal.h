@@ -21,6 +21,11 @@ enum UppeRealMode {
     REAL_E = 0,       // E <- T^-1( i kz exp(i(kz+kg)z) q )
     REAL_FINISH = 1,  // A <- T^-1( exp(i(kz+kg)z) q ) and E <- i kz A   (uppe_kernel.py:250-253)
     REAL_APPLY1 = 2,  // first RK stage from k1 (q <- qi + Ce k1, qf <- qi + Cs k1), then E from q
+    // an RK stage on a slice without current (S = 0, the NL filter), then E at the next z from the
+    // stage estimate: the fused pass's arithmetic there (rk_stage.cuh spec_update with S = 0)
+    REAL_ZS1 = 3,     // q <- cond qi, qf <- qi
+    REAL_ZS23 = 4,    // q <- cond qi (qf unchanged)
+    REAL_ZSF = 5,     // q <- cond qf, written as the step's result
 };
 
 // Modes of the time-axis pass.
@@ -131,7 +136,11 @@ cudaError_t configure_fused_reg();
 cudaError_t configure_real_reg();
 cudaError_t configure_spec_reg();
 cudaError_t configure_adj_reg();
-cudaError_t launch_fused_reg(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next);
+cudaError_t launch_fused_reg(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next,
+                             int nslices);
+// k_real_reg over the slices [iw0, iw0 + count)
+cudaError_t launch_real_reg_range(UppeHandle* h, int mode, const float2* src, float2* A_out, const float2* k1,
+                                  float2* qf, float Cs, float Ce, StepArgs z, int iw0, int count);
 cudaError_t launch_real_reg(UppeHandle* h, int mode, const float2* src, float2* A_out, const float2* k1, float2* qf,
                             float Cs, float Ce, StepArgs z);
 cudaError_t launch_spec_reg(UppeHandle* h, int mode, const float2* src, float2* q_out, float2* qf, const float2* qi,

@@ -451,7 +451,25 @@ cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, fl
 
 cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
     if (h->slice_big) return launch_fused_big(h, mode, Cs, Ce, z_rhs, z_next);
-    if (h->slice_reg) return launch_fused_reg(h, mode, Cs, Ce, z_rhs, z_next);
+    if (h->slice_reg) {
+        // The NL filter leaves the slices w >= nl_cut_off without current (J = 0, so S = 0): the fused
+        // pass walks the others, and one block per such slice applies the stage with S = 0 and forms
+        // E, so that no persistent block takes a fourth slice for them (513 slices on 152 blocks).
+        const int jhi = h->cfg.nl_cut_off;
+        if (!h->cfg.envelope && h->cfg.nl_cut_on <= 0 && jhi > 0 && jhi < h->N0) {
+            cudaError_t e = launch_fused_reg(h, mode, Cs, Ce, z_rhs, z_next, jhi);
+            if (e != cudaSuccess) return e;
+            if (mode == SPEC_STAGE1)
+                return launch_real_reg_range(h, REAL_ZS1, h->qi, nullptr, nullptr, h->qf, 0.f, 0.f, z_next, jhi,
+                                             h->N0 - jhi);
+            if (mode == SPEC_STAGE23)
+                return launch_real_reg_range(h, REAL_ZS23, h->qi, nullptr, nullptr, nullptr, 0.f, 0.f, z_next, jhi,
+                                             h->N0 - jhi);
+            return launch_real_reg_range(h, REAL_ZSF, h->qf, nullptr, nullptr, h->qi, 0.f, 0.f, z_next, jhi,
+                                         h->N0 - jhi);
+        }
+        return launch_fused_reg(h, mode, Cs, Ce, z_rhs, z_next, h->N0);
+    }
     int logN1 = ilog2_exact(h->N1), logN2 = ilog2_exact(h->N2);
     h->launches++;
     k_fused_cart<<<h->N0, slice_threads(h), slice_smem(h), h->stream>>>(mode, h->J, uppe_op_view(h), h->qi, h->qf,
