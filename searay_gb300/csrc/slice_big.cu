@@ -162,9 +162,11 @@ bool big_slice_supported(int N1, int N2) {
     return ok(N1) && ok(N2) && N1 * N2 > 16384;
 }
 
+// Row transforms of the slices [0, nslices) (every slice when nslices < 0).
 template <bool INV>
-static cudaError_t rows(UppeHandle* h, const float2* src, float2* dst, float scale, int finish, float2* A_out) {
-    const size_t nrows = (size_t)h->N0 * h->N1;
+static cudaError_t rows(UppeHandle* h, const float2* src, float2* dst, float scale, int finish, float2* A_out,
+                        int nslices = -1) {
+    const size_t nrows = (size_t)(nslices < 0 ? h->N0 : nslices) * h->N1;
     h->launches++;
     const OpView opv = uppe_op_view(h);
     if (h->N2 == 256) {
@@ -191,7 +193,11 @@ static cudaError_t cols(UppeHandle* h, const BigColArgs& a) {
 }
 
 cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
-    cudaError_t e = rows<false>(h, h->J, h->J, 1.f, 0, nullptr);
+    // The time pass's NL filter leaves J = 0 on the slices w >= nl_cut_off: their forward row
+    // transforms are left out (the column pass then reads those zeros, and S = 0 there exactly).
+    const int jhi = h->cfg.nl_cut_off;
+    const int nfwd = (!h->cfg.envelope && h->cfg.nl_cut_on <= 0 && jhi > 0 && jhi < h->N0) ? jhi : h->N0;
+    cudaError_t e = rows<false>(h, h->J, h->J, 1.f, 0, nullptr, nfwd);
     BigColArgs a{};
     a.kind = BC_FUSED;
     a.mode = mode;
