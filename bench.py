@@ -188,6 +188,9 @@ def run_device(args, vd, ws, rank, local):
 
     for _ in range(args.warmup):
         one_step()
+    # the timed steps are the workload's own steps 0 .. K-1: back to the incoming plane
+    dev.load_field(a_dev)
+    step[0] = 0
     torch.cuda.synchronize()
     if ws > 1:
         torch.distributed.barrier()
@@ -253,6 +256,7 @@ def run_e2e(args, vd):
     v["size"] = (vd["size"][0], vd["size"][1], dz * args.steps)
     v["subcycles"] = args.steps
     v["minimum step"] = dz
+    v["precision"] = args.precision
     warm = dict(v)
     warm["size"] = (vd["size"][0], vd["size"][1], dz * 2)
     warm["subcycles"] = 2

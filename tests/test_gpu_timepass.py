@@ -1,7 +1,9 @@
 """The time-axis pass at the frequency grids of the benchmark configurations (N0 = 257, 513, 1025,
-2049), where it runs with compile-time sizes (searay_gb300/csrc/timepass.cu): one fixed RK4 step and
-the finish against the FP64 oracle, on a 16 x 16 Cartesian grid with the filamentation medium and a
-pulse strong enough to ionize.  Bounds: the golden parity tolerances (field 2e-5; J, chi, ne 1e-4)."""
+2049), where it runs with compile-time sizes (searay_gb300/csrc/timepass.cu), and at the longest
+time axis the library accepts (N0 = 4097, Nt = 8192: one transverse point per block, the
+runtime-size kernel): one fixed RK4 step and the finish against the FP64 oracle, on a 16 x 16
+Cartesian grid with the filamentation medium and a pulse strong enough to ionize.  Bounds: the
+golden parity tolerances (field 2e-5; J, chi, ne 1e-4)."""
 import numpy as np
 import pytest
 
@@ -22,7 +24,7 @@ def rel_err(x, ref):
 
 
 @pytest.mark.parametrize("precision", ["mixed", "fp32"])
-@pytest.mark.parametrize("n0", [257, 513, 1025, 2049])
+@pytest.mark.parametrize("n0", [257, 513, 1025, 2049, 4097])
 def test_time_pass_rk4_step_vs_oracle(n0, precision):
     import torch
     from oracle import uppe_oracle as O
