@@ -77,18 +77,35 @@ struct TwHalfShared {
     }
 };
 
+// Row order of a transform in shared memory.  NoSwizzle: element e in row e.  RowSwizzle: element e
+// in row e ^ key(e), key(e) = bits [sh, sh + 3) of e & mask, a permutation within every aligned
+// group of 8 rows.  With rows of C batched transforms (batch-fast data), the rows 8 apart that a
+// warp touches in a radix-8 stage with p = 1 (and in a sweep over consecutive segments of 8 rows)
+// then fall on distinct banks: sh = 3 when C >= 2, sh = 4 when C = 1 (a warp then spans 16 such
+// rows).  mask = N - 1 leaves row N (the Nyquist row of a half spectrum) in place; mask = 0 is the
+// identity.  The time pass swizzles for C <= 4 (2- to 16-way conflicts without it); at C = 8 the
+// conflicts are 2-way and the extra address registers cost more than they save; at C >= 16 the
+// rows of a half-warp are conflict-free as they are.
+struct NoSwizzle {
+    UPPE_DEV int operator()(int e) const { return e; }
+};
+struct RowSwizzle {
+    int mask, sh;
+    UPPE_DEV int operator()(int e) const { return e ^ (((e & mask) >> sh) & 7); }
+};
+
 // One radix-R stage over all nb transforms; thread `tid` of `nthr` handles ITEMS butterflies.
 // batch_fast: consecutive threads take consecutive transforms (use when es != 1 so that the
 // accesses of a warp are contiguous in shared memory).
-template <int R, int ITEMS, class TW>
+template <int R, int ITEMS, class TW, class SW = NoSwizzle>
 UPPE_DEV void stockham_stage(float2* buf, int logN, int logp, int lognb, int bs, int es, const TW& tw, bool inv,
-                             bool batch_fast, int tid, int nthr) {
+                             bool batch_fast, int tid, int nthr, const SW& sw = SW{}) {
     constexpr int LOGR = (R == 2) ? 1 : (R == 4) ? 2 : 3;
     const int logq = logN - LOGR;
     const int nq = 1 << logq;
     const int p = 1 << logp;
     float2 u[ITEMS][R];
-    int dst[ITEMS];
+    int dst[ITEMS], b_of[ITEMS];
 #pragma unroll
     for (int it = 0; it < ITEMS; ++it) {
         const int g = tid + it * nthr;
@@ -103,7 +120,7 @@ UPPE_DEV void stockham_stage(float2* buf, int logN, int logp, int lognb, int bs,
         const int k = i & (p - 1);
         const float2* base = buf + b * bs;
 #pragma unroll
-        for (int r = 0; r < R; ++r) u[it][r] = base[(i + r * nq) * es];
+        for (int r = 0; r < R; ++r) u[it][r] = base[sw(i + r * nq) * es];
         if (logp > 0) {
             const int sh = tw.log - logp - LOGR;  // NT / (p R)
             if constexpr (R == 8) {
@@ -132,22 +149,23 @@ UPPE_DEV void stockham_stage(float2* buf, int logN, int logp, int lognb, int bs,
             }
         }
         dft_small<R>(u[it], inv);
-        dst[it] = b * bs + (((i - k) << LOGR) + k) * es;
+        dst[it] = ((i - k) << LOGR) + k;  // row of output r = 0; output r is p rows further
+        b_of[it] = b * bs;
     }
     __syncthreads();
 #pragma unroll
     for (int it = 0; it < ITEMS; ++it) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) buf[dst[it] + r * p * es] = u[it][r];
+        for (int r = 0; r < R; ++r) buf[b_of[it] + sw(dst[it] + r * p) * es] = u[it][r];
     }
     __syncthreads();
 }
 
 // Full transform along one axis.  ET = elements per thread = nb*N/nthr (compile time); radix 8
 // stages first, then one radix-4 or radix-2 stage for the remainder.
-template <int ET, class TW>
+template <int ET, class TW, class SW = NoSwizzle>
 UPPE_DEV void fft_axis_tw(float2* buf, int logN, int lognb, int bs, int es, const TW& tw, bool inv, int tid,
-                          int nthr, int batch_fast_mode = -1) {
+                          int nthr, int batch_fast_mode = -1, const SW& sw = SW{}) {
     // batch_fast_mode: -1 = automatic (batch-fast when es != 1), 0 = element-fast, 1 = batch-fast
     const bool batch_fast = (batch_fast_mode < 0) ? (es != 1) : (batch_fast_mode != 0);
     int logp = 0;
@@ -155,20 +173,20 @@ UPPE_DEV void fft_axis_tw(float2* buf, int logN, int lognb, int bs, int es, cons
         const int rem = logN - logp;
         if constexpr (ET >= 8) {
             if (rem >= 3) {
-                stockham_stage<8, ET / 8>(buf, logN, logp, lognb, bs, es, tw, inv, batch_fast, tid, nthr);
+                stockham_stage<8, ET / 8>(buf, logN, logp, lognb, bs, es, tw, inv, batch_fast, tid, nthr, sw);
                 logp += 3;
                 continue;
             }
         }
         if constexpr (ET >= 4) {
             if (rem >= 2) {
-                stockham_stage<4, ET / 4>(buf, logN, logp, lognb, bs, es, tw, inv, batch_fast, tid, nthr);
+                stockham_stage<4, ET / 4>(buf, logN, logp, lognb, bs, es, tw, inv, batch_fast, tid, nthr, sw);
                 logp += 2;
                 continue;
             }
         }
         if constexpr (ET >= 2) {
-            stockham_stage<2, ET / 2>(buf, logN, logp, lognb, bs, es, tw, inv, batch_fast, tid, nthr);
+            stockham_stage<2, ET / 2>(buf, logN, logp, lognb, bs, es, tw, inv, batch_fast, tid, nthr, sw);
             logp += 1;
         } else {
             break;  // unreachable for valid launches (ET >= 2 whenever logN >= 1)
@@ -184,10 +202,10 @@ UPPE_DEV void fft_axis(float2* buf, int logN, int lognb, int bs, int es, const f
 }
 
 // ---------------------------------------------------------------------------------------------
-// Compile-time form for batch-fast data (element e of transform b at buf[b + e * NB], NB = 2^LOGNB
-// transforms of 2^LOGN points, NB * N / ET threads): every stride, offset and twiddle shift is a
-// constant, so a stage is its loads, twiddles, butterfly and stores.  Twiddles from a shared
-// half table of 2^(TWLOG-1) entries of exp(-2 pi i j / 2^TWLOG).
+// Compile-time form for batch-fast data (element e of transform b at buf[b + sw(e) * NB], NB = 2^LOGNB
+// transforms of 2^LOGN points, NB * N / ET threads, sw the RowSwizzle of ct_row_swizzle): every
+// stride, offset and twiddle shift is a constant, so a stage is its loads, twiddles, butterfly and
+// stores.  Twiddles from a shared half table of 2^(TWLOG-1) entries of exp(-2 pi i j / 2^TWLOG).
 // ---------------------------------------------------------------------------------------------
 template <int TWLOG>
 struct TwHalfSharedCT {
@@ -199,23 +217,28 @@ struct TwHalfSharedCT {
     }
 };
 
+template <int LOGN, int LOGNB>
+UPPE_DEV constexpr RowSwizzle ct_row_swizzle() {
+    return RowSwizzle{LOGNB <= 2 ? (1 << LOGN) - 1 : 0, LOGNB == 0 ? 4 : 3};
+}
+
 template <int R, int ITEMS, int LOGN, int LOGP, int LOGNB, int TWLOG>
 UPPE_DEV void stockham_stage_ct(float2* buf, const TwHalfSharedCT<TWLOG>& tw, bool inv, int tid) {
     constexpr int LOGR = (R == 2) ? 1 : (R == 4) ? 2 : 3;
     constexpr int NQ = 1 << (LOGN - LOGR), P = 1 << LOGP, NB = 1 << LOGNB;
     constexpr int NTHR = (NB << LOGN) / (R * ITEMS);
     constexpr int SH = TWLOG - LOGP - LOGR;
+    constexpr RowSwizzle sw = ct_row_swizzle<LOGN, LOGNB>();
     float2 u[ITEMS][R];
-    int dst[ITEMS];
+    int dst[ITEMS], bs[ITEMS];
 #pragma unroll
     for (int it = 0; it < ITEMS; ++it) {
         const int g = tid + it * NTHR;
         const int b = g & (NB - 1);
         const int i = g >> LOGNB;
         const int k = i & (P - 1);
-        const float2* src = buf + b + i * NB;
 #pragma unroll
-        for (int r = 0; r < R; ++r) u[it][r] = src[r * NQ * NB];
+        for (int r = 0; r < R; ++r) u[it][r] = buf[b + sw(i + r * NQ) * NB];
         if constexpr (LOGP > 0) {
             if constexpr (R == 8) {
                 float2 w1 = tw.get(k << SH), w2 = tw.get((2 * k) << SH), w4 = tw.get((4 * k) << SH);
@@ -242,13 +265,14 @@ UPPE_DEV void stockham_stage_ct(float2* buf, const TwHalfSharedCT<TWLOG>& tw, bo
             }
         }
         dft_small<R>(u[it], inv);
-        dst[it] = b + (((i - k) << LOGR) + k) * NB;
+        dst[it] = ((i - k) << LOGR) + k;  // row of output r = 0; output r is P rows further
+        bs[it] = b;
     }
     __syncthreads();
 #pragma unroll
     for (int it = 0; it < ITEMS; ++it) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) buf[dst[it] + r * P * NB] = u[it][r];
+        for (int r = 0; r < R; ++r) buf[bs[it] + sw(dst[it] + r * P) * NB] = u[it][r];
     }
     __syncthreads();
 }

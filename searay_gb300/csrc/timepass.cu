@@ -61,6 +61,9 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
     const size_t col0 = (size_t)blockIdx.x * C;
     const bool ionize = tp.rate_form != UPPE_RATE_NONE;
     const TwHalfShared tws{twl, tp.logNt};
+    // rows of the transforms in the row-swizzled order of the shared-memory FFTs (RowSwizzle; on for
+    // blocks of at most 4 columns)
+    const RowSwizzle sw{logC <= 2 ? M - 1 : 0, logC == 0 ? 4 : 3};
 
     // ---- 1. stage the half spectrum X[k][c], k in [0, M], with asynchronous copies ----
     if (C >= 2) {
@@ -68,13 +71,13 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
         for (int it = tid; it < (M + 1) * hC; it += T) {
             const int c2 = it & (hC - 1);
             const int k = it >> (logC - 1);
-            cp_async16_time(&Zj[k * C + 2 * c2], &E[(size_t)k * S + col0 + 2 * c2]);
+            cp_async16_time(&Zj[sw(k) * C + 2 * c2], &E[(size_t)k * S + col0 + 2 * c2]);
         }
     } else {
         for (int it = tid; it < (M + 1) * C; it += T) {
             const int c = it & (C - 1);
             const int k = it >> logC;
-            cp_async8(&Zj[it], &E[(size_t)k * S + col0 + c]);
+            cp_async8(&Zj[sw(k) * C + c], &E[(size_t)k * S + col0 + c]);
         }
     }
     float2* Zr = reinterpret_cast<float2*>(tot + 2 * T);
@@ -90,26 +93,26 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
     for (int it = tid; it < npairs; it += T) {
         const int c = it & (C - 1);
         const int k = it >> logC;
-        float2 Xa = Zj[k * C + c];
-        float2 Xm = Zj[(M - k) * C + c];
+        float2 Xa = Zj[sw(k) * C + c];
+        float2 Xm = Zj[sw(M - k) * C + c];
         if (k == 0) {
             Xa.y = 0.f;
             Xm.y = 0.f;
         }
         const float2 t = cconj(tws.get(k));  // e^{+2 pi i k / Nt}
         const float2 b = cconj(Xm);
-        Zp[k * C + c] = cadd(cadd(Xa, b), cmul_i(cmul(t, csub(Xa, b))));
+        Zp[sw(k) * C + c] = cadd(cadd(Xa, b), cmul_i(cmul(t, csub(Xa, b))));
         if (k != 0 && 2 * k != M) {
             const float2 t2 = make_float2(-t.x, t.y);  // e^{2 pi i (M-k)/Nt}
             const float2 b2 = cconj(Xa);
-            Zp[(M - k) * C + c] = cadd(cadd(Xm, b2), cmul_i(cmul(t2, csub(Xm, b2))));
+            Zp[sw(M - k) * C + c] = cadd(cadd(Xm, b2), cmul_i(cmul(t2, csub(Xm, b2))));
         }
     }
     __syncthreads();
     if constexpr (CT)
         fft_axis_ct<ET, LOGM, LOGC, LOGM + 1>(Zp, TwHalfSharedCT<LOGM + 1>{twl}, true, tid);
     else
-        fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
+        fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, true, tid, T, -1, sw);
 
     // ---- 2. sources, in place ----
     const int c = tid & (C - 1);
@@ -124,20 +127,20 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
         raman_pass<16, RAMAN == 1>(
             tp, Rs, tot, C, logC, T, tid, seg, ngc,
             [&](int k) {
-                const float2 zv = Zp[(m0 + k) * C + c];
+                const float2 zv = Zp[sw(m0 + k) * C + c];
                 return make_float2(zv.x * zv.x, zv.y * zv.y);
             },
-            [&](int k, float chi0, float chi1) { Zr[(m0 + k) * C + c] = make_float2(chi0, chi1); });
+            [&](int k, float chi0, float chi1) { Zr[sw(m0 + k) * C + c] = make_float2(chi0, chi1); });
     }
     float r_next = 0.f;
     ffloat part = {0.f, 0.f};
     bool live = false;  // a nonzero rate in this segment (zero increments leave a float-float sum exactly as it is)
     if (ionize) {
-        if (t1 <= Nt - 2) r_next = ion_rate(tp, Zp[(t1 >> 1) * C + c].x * inv);
+        if (t1 <= Nt - 2) r_next = ion_rate(tp, Zp[sw(t1 >> 1) * C + c].x * inv);
         float rn = r_next;
 #pragma unroll(CT ? 8 : 1)
         for (int m = m0 + mps - 1; m >= m0; --m) {
-            const float2 zv = Zp[m * C + c];
+            const float2 zv = Zp[sw(m) * C + c];
             const int t = 2 * m + 1;
             const float r1 = (t == Nt - 1) ? 0.f : ion_rate(tp, zv.y * inv);
             const float p1 = tp.hdt * (r1 + rn);
@@ -147,7 +150,7 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
             if (p0 != 0.f) acc_add(part, p0, tp.plain);
             live = live || r0 != 0.f || r1 != 0.f;
             rn = r0;
-            Zj[m * C + c] = make_float2(r0, r1);  // this thread's own slot, reused below
+            Zj[sw(m) * C + c] = make_float2(r0, r1);  // this thread's own slot, reused below
         }
         live = live || r_next != 0.f;
     }
@@ -200,11 +203,11 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
         const int wlo = tp.wcut + tp.wwid, whi = Nt - tp.wcut - tp.wwid - 1;  // window is 1 on [wlo, whi]
 #pragma unroll(CT ? 8 : 1)
         for (int m = m0 + mps - 1; m >= m0; --m) {
-            const float2 zv = Zp[m * C + c];
+            const float2 zv = Zp[sw(m) * C + c];
             const float e1 = zv.y * inv, e0 = zv.x * inv;
             float ne1 = 0.f, ne0 = 0.f;
             if (dens) {
-                const float2 rr = Zj[m * C + c];
+                const float2 rr = Zj[sw(m) * C + c];
                 const int t = 2 * m + 1;
                 if (t <= Nt - 2) acc_add(Sacc, tp.hdt * (rr.y + rn), tp.plain);
                 ne1 = ngc * one_minus_exp_neg(ff_value(Sacc));
@@ -216,16 +219,16 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
             }
             float chi1 = kerr * e1 * e1, chi0 = kerr * e0 * e0;
             if constexpr (RAMAN != 0) {  // the Raman chi comes first in the reference's sum (uppe_kernel.py:173-179)
-                const float2 zr = Zr[m * C + c];
+                const float2 zr = Zr[sw(m) * C + c];
                 chi1 = zr.y + chi1;
                 chi0 = zr.x + chi0;
             }
             if (mode == TIME_J) {
-                Zp[m * C + c] = make_float2(chi0 * e0, chi1 * e1);
-                Zj[m * C + c] = make_float2(ne0 * e0, ne1 * e1);
+                Zp[sw(m) * C + c] = make_float2(chi0 * e0, chi1 * e1);
+                Zj[sw(m) * C + c] = make_float2(ne0 * e0, ne1 * e1);
             } else {
-                Zp[m * C + c] = make_float2(chi0, chi1);
-                Zj[m * C + c] = make_float2(ne0, ne1);
+                Zp[sw(m) * C + c] = make_float2(chi0, chi1);
+                Zj[sw(m) * C + c] = make_float2(ne0, ne1);
             }
         }
     }
@@ -238,16 +241,16 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
         fft_axis_ct<ET, LOGM, LOGC, LOGM + 1>(Zp, TwHalfSharedCT<LOGM + 1>{twl}, false, tid);
         if (two) fft_axis_ct<ET, LOGM, LOGC, LOGM + 1>(Zj, TwHalfSharedCT<LOGM + 1>{twl}, false, tid);
     } else {
-        fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, false, tid, T);
-        if (two) fft_axis_tw<ET>(Zj, tp.logM, logC, 1, C, tws, false, tid, T);
+        fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, false, tid, T, -1, sw);
+        if (two) fft_axis_tw<ET>(Zj, tp.logM, logC, 1, C, tws, false, tid, T, -1, sw);
     }
     for (int it = tid; it < (M + 1) * C; it += T) {
         const int cc = it & (C - 1);
         const int k = it >> logC;
         const int ka = k & (M - 1), kb = (M - k) & (M - 1);
         const float2 twk = tws.get(k);  // e^{-2 pi i k / Nt}
-        const float2 P = real_spectrum(Zp[ka * C + cc], Zp[kb * C + cc], twk);
-        const float2 Q = two ? real_spectrum(Zj[ka * C + cc], Zj[kb * C + cc], twk) : make_float2(0.f, 0.f);
+        const float2 P = real_spectrum(Zp[sw(ka) * C + cc], Zp[sw(kb) * C + cc], twk);
+        const float2 Q = two ? real_spectrum(Zj[sw(ka) * C + cc], Zj[sw(kb) * C + cc], twk) : make_float2(0.f, 0.f);
         const size_t o = (size_t)k * S + col0 + cc;
         if (mode == TIME_J) {
             const float wk = wv[k];
