@@ -114,7 +114,7 @@ static void free_buffers(UppeHandle* h) {
     void* ptrs[] = {h->q,  h->qi,   h->qf,   h->k1,   h->E,     h->J,      h->scratch, h->opK,  h->opKi, h->kg2,
                     h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red, h->dev_err, h->Minv_tc, h->Mfwd_tc,
                     h->adj_q1, h->adj_q2, h->adj_q3, h->adj_lf, h->adj_acc, h->adj_lk, h->adj_mu, h->MfwdT, h->MinvT,
-                    h->adj_E[0], h->adj_E[1], h->adj_E[2],
+                    h->adj_E[0], h->adj_E[1], h->adj_E[2], h->adj_E[3],
                     h->dred_d, h->rot, h->Atc};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -776,7 +776,8 @@ static int ensure_adjoint(UppeHandle* h) {
     if (h->adj_mu) return UPPE_OK;
     const size_t fb = h->P * sizeof(float2);
     float2** bufs[] = {&h->adj_q1, &h->adj_q2, &h->adj_q3,   &h->adj_lf,   &h->adj_acc,
-                       &h->adj_lk, &h->adj_E[0], &h->adj_E[1], &h->adj_E[2], &h->adj_mu};  // adj_mu last: the "allocated" mark
+                       &h->adj_lk, &h->adj_E[0], &h->adj_E[1], &h->adj_E[2], &h->adj_E[3],
+                       &h->adj_mu};  // adj_mu last: the "allocated" mark
     for (float2** b : bufs) CUDA_TRY(h, cudaMalloc((void**)b, fb));
     CUDA_TRY(h, cudaMalloc((void**)&h->dred_d, sizeof(double)));
     return UPPE_OK;
@@ -815,7 +816,37 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
     // recompute the stage estimates q1', q2', q3' of the forward step (uppe_kernel.py:305-322)
     CUDA_TRY(h, cudaMemcpyAsync(h->qi, q0, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
     h->E_valid = 0;
-    {
+    // register-resident Cartesian slices: the forward step's own kernels, the time pass and the fused
+    // slice pass per stage, with the fused pass also storing the stage estimate (stage_q) and its E
+    // going to the buffer the reverse sweep reads, so that E of q3' at z + dz is kept as well
+    const bool fused = !h->cfg.cylindrical && h->slice_reg && !h->slice_big;
+    if (fused) {
+        const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz), ze = split_z(h, z_phase + dz);
+        float2* const E_main = h->E;
+        float2* const qs[3] = {h->adj_q1, h->adj_q2, h->adj_q3};
+        const int modes[3] = {SPEC_STAGE1, SPEC_STAGE23, SPEC_STAGE23};
+        const float cs[3] = {(float)(dz / 6), (float)(dz / 3), (float)(dz / 3)};
+        const float ce[3] = {(float)(dz / 2), (float)(dz / 2), (float)dz};
+        const StepArgs zr[3] = {z0, zh, zh}, zn[3] = {zh, zh, ze};
+        h->E = h->adj_E[0];
+        cudaError_t e = eval_to_J(h, h->qi, z0);
+        for (int s = 0; s < 3 && e == cudaSuccess; ++s) {
+            h->E = h->adj_E[s + 1];
+            h->stage_q = qs[s];
+            {
+                ProfScope ps(h, UPPE_CLASS_OTHER);
+                e = launch_fused_cart(h, modes[s], cs[s], ce[s], zr[s], zn[s]);
+            }
+            h->stage_q = nullptr;
+            if (e == cudaSuccess && s < 2) {
+                ProfScope ps(h, UPPE_CLASS_TIME);
+                e = launch_time_pass(h, TIME_J, h->E, h->J, nullptr);
+            }
+        }
+        h->E = E_main;
+        h->stage_q = nullptr;
+        CUDA_TRY(h, e);
+    } else {
         const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz);
         // each stage writes its estimate straight into the buffer the reverse sweep reads, and each
         // evaluation keeps its E (the inverse pass writes into h->E, pointed at adj_E[s] meanwhile)
@@ -838,7 +869,7 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
     }
     // reverse sweep through the four stages
     CUDA_TRY(h, launch_adj_rk(h, 0, (const float2*)lam_out, nullptr, (float)(dz / 6), 0.f));
-    if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu, nullptr))) return rc;
+    if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu, fused ? h->adj_E[3] : nullptr))) return rc;
     CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)dz));
     if ((rc = vjp_rhs(h, h->adj_q2, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu, h->adj_E[2]))) return rc;
     CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)(dz / 2)));

@@ -480,7 +480,8 @@ template <int LN1, int LN2>
 __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     k_fused_reg(int mode, const float2* __restrict__ J, OpView opv, float2* __restrict__ qi_out,
                 float2* __restrict__ qf, const float2* __restrict__ qi, float2* __restrict__ E, float Cs, float Ce,
-                const float2* __restrict__ tw, int twLog, StepArgs z_rhs, StepArgs z_next, int n0) {
+                const float2* __restrict__ tw, int twLog, StepArgs z_rhs, StepArgs z_next, int n0,
+                float2* __restrict__ q_store) {
     using RS = RegSlice<LN1, LN2>;
     using FP = FusedPlan<LN1, LN2>;
     extern __shared__ __align__(16) float2 sm[];
@@ -572,9 +573,11 @@ __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
                 if (mode == SPEC_STAGE1) {
                     qf[idx] = cadd(qiv, cscale(sv, Cs));
                     qw = cscale(cadd(qiv, cscale(sv, Ce)), cond);
+                    if (q_store) q_store[idx] = qw;
                 } else if (mode == SPEC_STAGE23) {
                     qf[idx] = cadd(qfv, cscale(sv, Cs));
                     qw = cscale(cadd(qiv, cscale(sv, Ce)), cond);
+                    if (q_store) q_store[idx] = qw;
                 } else {
                     qw = cscale(cadd(qfv, cscale(sv, Cs)), cond);
                     qi_out[idx] = qw;
@@ -608,7 +611,7 @@ template <int LN1, int LN2>
 __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     k_real_reg(int mode, const float2* __restrict__ src, OpView opv, float2* __restrict__ E,
                float2* __restrict__ A_out, const float2* __restrict__ k1, float2* __restrict__ qf, float Cs, float Ce,
-               const float2* __restrict__ tw, int twLog, StepArgs z, int iw0) {
+               const float2* __restrict__ tw, int twLog, StepArgs z, int iw0, float2* __restrict__ q_store) {
     using RS = RegSlice<LN1, LN2>;
     extern __shared__ float2 sm[];
     const int tid = threadIdx.x, iw = blockIdx.x + iw0;
@@ -633,6 +636,7 @@ __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
             val = cscale(a, cond);
             if (mode == REAL_ZS1) qf[idx] = a;
             if (mode == REAL_ZSF) qf[idx] = val;
+            if (mode != REAL_ZSF && q_store) q_store[idx] = val;
         } else {
             val = src[idx];
         }

@@ -11,7 +11,8 @@ struct FusedReg {
         using RS = RegSlice<LN1, LN2>;
         const int grid = n < h->num_sms ? n : h->num_sms;  // persistent: one CTA per multiprocessor
         k_fused_reg<LN1, LN2><<<grid, RS::T, FusedPlan<LN1, LN2>::SMEM, h->stream>>>(
-            mode, h->J, uppe_op_view(h), h->qi, h->qf, h->qi, h->E, Cs, Ce, h->tw, h->twLog, z_rhs, z_next, n);
+            mode, h->J, uppe_op_view(h), h->qi, h->qf, h->qi, h->E, Cs, Ce, h->tw, h->twLog, z_rhs, z_next, n,
+            h->stage_q);
         return cudaGetLastError();
     }
 };

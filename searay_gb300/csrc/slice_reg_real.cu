@@ -11,7 +11,8 @@ struct RealReg {
                            float Cs, float Ce, StepArgs z, int iw0, int count) {
         using RS = RegSlice<LN1, LN2>;
         k_real_reg<LN1, LN2><<<count, RS::T, RS::SMEM, h->stream>>>(mode, src, uppe_op_view(h), h->E, A_out, k1, qf,
-                                                                    Cs, Ce, h->tw, h->twLog, z, iw0);
+                                                                    Cs, Ce, h->tw, h->twLog, z, iw0,
+                                                                    mode >= REAL_ZS1 ? h->stage_q : nullptr);
         return cudaGetLastError();
     }
 };

@@ -439,10 +439,12 @@ __device__ __forceinline__ float ion_rate_deriv(const TimeParams& tp, float e, f
     return r * dl * tp.fconv * sg;
 }
 
-// even/odd packing of a half spectrum X(k) = f(k) into z for the M-point inverse FFT
+// even/odd packing of a half spectrum X(k) = f(k) into z for the M-point inverse FFT (rows of Z in
+// the order sw).  Every thread reads the pair X(k), X(M-k) and writes only rows k and M-k of Z, so Z
+// may hold X itself (packing in place).
 template <class F>
 __device__ __forceinline__ void pack_half_spectrum(float2* Z, int C, int logC, int M, const TwHalfShared& tws, F X,
-                                                   int tid, int T) {
+                                                   int tid, int T, const RowSwizzle& sw) {
     const int npairs = (M / 2 + 1) * C;
     for (int it = tid; it < npairs; it += T) {
         const int c = it & (C - 1);
@@ -454,74 +456,96 @@ __device__ __forceinline__ void pack_half_spectrum(float2* Z, int C, int logC, i
         }
         const float2 t = cconj(tws.get(k));
         const float2 b = cconj(Xm);
-        Z[k * C + c] = cadd(cadd(Xa, b), cmul_i(cmul(t, csub(Xa, b))));
+        const float2 zk = cadd(cadd(Xa, b), cmul_i(cmul(t, csub(Xa, b))));
+        float2 zm = zk;
         if (k != 0 && 2 * k != M) {
             const float2 t2 = make_float2(-t.x, t.y);
             const float2 b2 = cconj(Xa);
-            Z[(M - k) * C + c] = cadd(cadd(Xm, b2), cmul_i(cmul(t2, csub(Xm, b2))));
+            zm = cadd(cadd(Xm, b2), cmul_i(cmul(t2, csub(Xm, b2))));
         }
+        Z[sw(k) * C + c] = zk;
+        if (k != 0 && 2 * k != M) Z[sw(M - k) * C + c] = zm;
     }
 }
 
-// 16 time samples per thread, ET complex FFT elements per thread (8: 512 threads for 2048 complex
-// elements per column block, the layout the launcher picks).
-template <int ET>
-__global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* __restrict__ E, const float2* __restrict__ G,
-                                                  float2* __restrict__ gE, const float* __restrict__ ng,
-                                                  const float* __restrict__ wv, const float* __restrict__ filt,
-                                                  const float2* __restrict__ tw, int twLog, TimeParams tp,
-                                                  double* dred) {
+// 16 time samples per thread, 8 complex FFT elements per thread.  LOGM > 0: compile-time sizes
+// M = 2^LOGM, C = 2^LOGC (the compile-time Stockham transforms, unrolled segment loops); LOGM = 0:
+// sizes from the parameters.
+//
+// Shared layout: Ze [M+1][C] (e pairs, then ge pairs), Zn [M+1][C] (the raw E, then the rate pairs,
+// then the pairs of the density exponent S), Zp [M+1][C] (gp pairs), Zl [M+1][C] (the raw G, then
+// the gpl pairs), the half twiddle table, one float-float segment total per thread.  ne and
+// ng w exp(-S) are formed from S where they are used.  Rows in the order of RowSwizzle.
+template <int LOGM = 0, int LOGC = -1>
+__global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time_adj(const float2* __restrict__ E,
+                                                                   const float2* __restrict__ G,
+                                                                   float2* __restrict__ gE,
+                                                                   const float* __restrict__ ng,
+                                                                   const float* __restrict__ wv,
+                                                                   const float* __restrict__ filt,
+                                                                   const float2* __restrict__ tw, int twLog,
+                                                                   TimeParams tp, double* dred) {
     extern __shared__ float2 sa[];
-    const int C = tp.C, logC = tp.logC, Nt = tp.Nt, M = tp.M, S = tp.S;
+    constexpr bool CT = LOGM > 0;
+    const int C = CT ? (1 << LOGC) : tp.C, logC = CT ? LOGC : tp.logC;
+    const int Nt = CT ? (2 << LOGM) : tp.Nt, M = CT ? (1 << LOGM) : tp.M, S = tp.S;
     const int R = (M + 1) * C;
-    float2* Ze = sa;           // e pairs, then ge pairs
-    float2* Zn = sa + R;       // raw E / rates / ne pairs
-    float2* Za = sa + 2 * R;   // raw G / ng w exp(-S) pairs
-    float2* Zp = sa + 3 * R;   // gp pairs
-    float2* Zl = sa + 4 * R;   // gpl pairs
-    float2* twl = sa + 5 * R;
+    float2* Ze = sa;
+    float2* Zn = sa + R;
+    float2* Zp = sa + 2 * R;
+    float2* Zl = sa + 3 * R;
+    float2* twl = sa + 4 * R;
     ffloat* tot = reinterpret_cast<ffloat*>(twl + (Nt >> 1));
     __shared__ double red_sh[32];
-    const int tid = threadIdx.x, T = blockDim.x;
+    const int tid = threadIdx.x, T = CT ? ((2 << LOGM) << LOGC) / 16 : (int)blockDim.x;
     const size_t col0 = (size_t)blockIdx.x * C;
     const bool ionize = tp.rate_form != UPPE_RATE_NONE;
     const TwHalfShared tws{twl, tp.logNt};
+    const RowSwizzle sw{logC <= 2 ? M - 1 : 0, logC == 0 ? 4 : 3};
+    const auto inv_fft = [&](float2* Z) {
+        if constexpr (CT)
+            fft_axis_ct<8, LOGM, LOGC, LOGM + 1>(Z, TwHalfSharedCT<LOGM + 1>{twl}, true, tid);
+        else
+            fft_axis_tw<8>(Z, tp.logM, logC, 1, C, tws, true, tid, T, -1, sw);
+    };
 
     // ---- 1. stage E and G, recompute e(t), form the transposed-rfft inputs ----
     for (int it = tid; it < R; it += T) {
         const int c = it & (C - 1);
         const int k = it >> logC;
-        cp_async8(&Zn[it], &E[(size_t)k * S + col0 + c]);
-        cp_async8(&Za[it], &G[(size_t)k * S + col0 + c]);
+        cp_async8(&Zn[sw(k) * C + c], &E[(size_t)k * S + col0 + c]);
+        cp_async8(&Zl[sw(k) * C + c], &G[(size_t)k * S + col0 + c]);
     }
     asm volatile("cp.async.commit_group;\n" ::);
     for (int j = tid; j < (Nt >> 1); j += T) twl[j] = __ldg(&tw[j << (twLog - tp.logNt)]);
     asm volatile("cp.async.wait_group 0;\n" ::);
     __syncthreads();
-    pack_half_spectrum(Ze, C, logC, M, tws, [&](int k, int c) { return Zn[k * C + c]; }, tid, T);
+    pack_half_spectrum(Ze, C, logC, M, tws, [&](int k, int c) { return Zn[sw(k) * C + c]; }, tid, T, sw);
     // Gp_k = W_k filt_k (i w_k) G_k ; Gl_k = W_k filt_k G_k / (0.1 + i w_k), W = 1/2 inside the band
     pack_half_spectrum(Zp, C, logC, M, tws, [&](int k, int c) {
         const float wk = wv[k];
         const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
-        return cscale(cmul_i(Za[k * C + c]), wk * wt * filt[k]);
-    }, tid, T);
-    if (ionize)
+        return cscale(cmul_i(Zl[sw(k) * C + c]), wk * wt * filt[k]);
+    }, tid, T, sw);
+    if (ionize) {
+        __syncthreads();  // every read of G for Gp precedes the packing of Gl over it
         pack_half_spectrum(Zl, C, logC, M, tws, [&](int k, int c) {
             const float wk = wv[k];
             const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
             const float rden = __frcp_rn(fmaf(wk, wk, tp.damping * tp.damping));
-            return cscale(cmul(Za[k * C + c], make_float2(tp.damping, -wk)), rden * wt * filt[k]);
-        }, tid, T);
+            return cscale(cmul(Zl[sw(k) * C + c], make_float2(tp.damping, -wk)), rden * wt * filt[k]);
+        }, tid, T, sw);
+    }
     __syncthreads();
-    fft_axis_tw<ET>(Ze, tp.logM, logC, 1, C, tws, true, tid, T);
-    fft_axis_tw<ET>(Zp, tp.logM, logC, 1, C, tws, true, tid, T);
+    inv_fft(Ze);
+    inv_fft(Zp);
 
-    // ---- 2. forward sources along t (ne and ng w exp(-S)), as in k_time ----
+    // ---- 2. forward sources along t (rates and the density exponent S), as in k_time ----
     const int c = tid & (C - 1);
     const int seg = tid >> logC;
-    const int mps = tp.spt >> 1;
-    const int m0 = seg * mps;
-    const int t1 = 2 * (m0 + mps);
+    constexpr int MPS = 8;  // packed pairs (16 samples) per thread
+    const int m0 = seg * MPS;
+    const int t1 = 2 * (m0 + MPS);
     const float ngc = ng[col0 + c];
     const float kerr = ngc * tp.redchi3;
     const float inv = tp.inv_nt;
@@ -536,11 +560,13 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
     float r_next = 0.f;
     ffloat part = {0.f, 0.f};
     if (ionize) {
-        if (t1 <= Nt - 2) r_next = ion_rate(tp, Ze[(t1 >> 1) * C + c].x * inv);
+        if (t1 <= Nt - 2) r_next = ion_rate(tp, Ze[sw(t1 >> 1) * C + c].x * inv);
         float rn = r_next;
         bool live = r_next != 0.f;
-        for (int m = m0 + mps - 1; m >= m0; --m) {
-            const float2 zv = Ze[m * C + c];
+#pragma unroll
+        for (int j = MPS - 1; j >= 0; --j) {
+            const int m = m0 + j;
+            const float2 zv = Ze[sw(m) * C + c];
             const int t = 2 * m + 1;
             const float r1 = (t == Nt - 1) ? 0.f : ion_rate(tp, zv.y * inv);
             if (t <= Nt - 2) acc_add(part, tp.hdt * (r1 + rn), tp.plain);
@@ -548,38 +574,40 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
             acc_add(part, tp.hdt * (r0 + r1), tp.plain);
             live = live || r0 != 0.f || r1 != 0.f;
             rn = r0;
-            Zn[m * C + c] = make_float2(r0, r1);
+            Zn[sw(m) * C + c] = make_float2(r0, r1);
         }
         ion = __syncthreads_or(live ? 1 : 0) != 0;
     }
     if (ion) {
         ffloat Sacc = later_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
         float rn = r_next;
-        for (int m = m0 + mps - 1; m >= m0; --m) {
-            const float2 rr = Zn[m * C + c];
+#pragma unroll
+        for (int j = MPS - 1; j >= 0; --j) {
+            const int m = m0 + j;
+            const float2 rr = Zn[sw(m) * C + c];
             const int t = 2 * m + 1;
             if (t <= Nt - 2) acc_add(Sacc, tp.hdt * (rr.y + rn), tp.plain);
-            const float w1 = soft_window(t, Nt, tp.wcut, tp.wwid);
             const float S1 = ff_value(Sacc);
             acc_add(Sacc, tp.hdt * (rr.x + rr.y), tp.plain);
             rn = rr.x;
-            const float w0 = soft_window(t - 1, Nt, tp.wcut, tp.wwid);
-            const float S0 = ff_value(Sacc);
-            Zn[m * C + c] = make_float2(ngc * one_minus_exp_neg(S0) * w0, ngc * one_minus_exp_neg(S1) * w1);
-            Za[m * C + c] = make_float2(ngc * w0 * expf(-S0), ngc * w1 * expf(-S1));
+            Zn[sw(m) * C + c] = make_float2(ff_value(Sacc), S1);
         }
         __syncthreads();  // segment totals are reused below
-        fft_axis_tw<ET>(Zl, tp.logM, logC, 1, C, tws, true, tid, T);
+        inv_fft(Zl);
     }
 
-    // ---- 3. transposed scan: Pfx(j) = sum_{t <= j} gpl e a, two passes in increasing t ----
+    // ---- 3. transposed scan: Pfx(j) = sum_{t <= j} gpl e a, a = ng w exp(-S), increasing t ----
     ffloat carry = {0.f, 0.f};
     if (ion) {
         ffloat part = {0.f, 0.f};
-        for (int m = m0; m < m0 + mps; ++m) {
-            const float2 e2 = Ze[m * C + c], l2 = Zl[m * C + c], a2 = Za[m * C + c];
-            acc_add(part, l2.x * e2.x * inv * a2.x, tp.plain);
-            acc_add(part, l2.y * e2.y * inv * a2.y, tp.plain);
+#pragma unroll
+        for (int j = 0; j < MPS; ++j) {
+            const int m = m0 + j;
+            const float2 e2 = Ze[sw(m) * C + c], l2 = Zl[sw(m) * C + c], s2 = Zn[sw(m) * C + c];
+            const float a0 = ngc * soft_window(2 * m, Nt, tp.wcut, tp.wwid) * expf(-s2.x);
+            const float a1 = ngc * soft_window(2 * m + 1, Nt, tp.wcut, tp.wwid) * expf(-s2.y);
+            acc_add(part, l2.x * e2.x * inv * a0, tp.plain);
+            acc_add(part, l2.y * e2.y * inv * a1, tp.plain);
         }
         carry = earlier_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
     }
@@ -587,12 +615,19 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
     float dred_part = 0.f;
     {
         ffloat Pprev = carry;  // Pfx(t - 1)
-        for (int m = m0; m < m0 + mps; ++m) {
-            const float2 e2 = Ze[m * C + c];
-            const float2 p2 = Zp[m * C + c];
+#pragma unroll
+        for (int j = 0; j < MPS; ++j) {
+            const int m = m0 + j;
+            const float2 e2 = Ze[sw(m) * C + c];
+            const float2 p2 = Zp[sw(m) * C + c];
             float ge[2];
             const float ev[2] = {e2.x * inv, e2.y * inv};
             const float gp[2] = {p2.x, p2.y};
+            float2 l2 = make_float2(0.f, 0.f), s2 = l2;
+            if (ion) {
+                l2 = Zl[sw(m) * C + c];
+                s2 = Zn[sw(m) * C + c];
+            }
 #pragma unroll
             for (int h = 0; h < 2; ++h) {
                 const int t = 2 * m + h;
@@ -600,10 +635,11 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
                 float g = 3.f * kerr * e * e * gp[h];
                 dred_part = fmaf(gp[h] * ngc * e * e, e, dred_part);
                 if (ion) {
-                    const float2 l2 = Zl[m * C + c], n2 = Zn[m * C + c], a2 = Za[m * C + c];
                     const float gl = h ? l2.y : l2.x;
-                    const float ne = h ? n2.y : n2.x;
-                    const float a = h ? a2.y : a2.x;
+                    const float Sv = h ? s2.y : s2.x;
+                    const float wv_t = soft_window(t, Nt, tp.wcut, tp.wwid);
+                    const float ne = ngc * one_minus_exp_neg(Sv) * wv_t;
+                    const float a = ngc * wv_t * expf(-Sv);
                     g = fmaf(ne, gl, g);
                     ffloat P = Pprev;
                     acc_add(P, gl * e * a, tp.plain);
@@ -616,7 +652,7 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
                 }
                 ge[h] = g;
             }
-            Ze[m * C + c] = make_float2(ge[0], ge[1]);
+            Ze[sw(m) * C + c] = make_float2(ge[0], ge[1]);
         }
     }
     // block reduction of the chi3 derivative (a block of fewer than 32 threads reduces through shared memory)
@@ -636,24 +672,36 @@ __global__ void __launch_bounds__(ET == 8 ? 512 : 256) k_time_adj(const float2* 
     }
 
     // ---- 5. transpose of irfft: gE = (1/Nt) W2 rfft(ge) ----
-    fft_axis_tw<ET>(Ze, tp.logM, logC, 1, C, tws, false, tid, T);
+    if constexpr (CT)
+        fft_axis_ct<8, LOGM, LOGC, LOGM + 1>(Ze, TwHalfSharedCT<LOGM + 1>{twl}, false, tid);
+    else
+        fft_axis_tw<8>(Ze, tp.logM, logC, 1, C, tws, false, tid, T, -1, sw);
     for (int it = tid; it < (M + 1) * C; it += T) {
         const int cc = it & (C - 1);
         const int k = it >> logC;
         const int ka = k & (M - 1), kb = (M - k) & (M - 1);
-        const float2 X = real_spectrum(Ze[ka * C + cc], Ze[kb * C + cc], tws.get(k));
+        const float2 X = real_spectrum(Ze[sw(ka) * C + cc], Ze[sw(kb) * C + cc], tws.get(k));
         const float wt = (k == 0 || k == M) ? inv : 2.f * inv;
         gE[(size_t)k * S + col0 + cc] = cscale(X, wt);
     }
 }
 
+// The adjoint time-pass shapes with compile-time sizes: 2048 complex elements per block (256 threads).
+#define UPPE_TIME_ADJ_CT(X) X(8, 3) X(9, 2) X(10, 1) X(11, 0)
+
 cudaError_t uppe_configure_time_adj_kernel(size_t smem_bytes) {
-    return cudaFuncSetAttribute(k_time_adj<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    cudaError_t e = cudaFuncSetAttribute(k_time_adj<>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+#define UPPE_TIME_ADJ_CONF(A_, B_)                                                                              \
+    if (e == cudaSuccess)                                                                                       \
+        e = cudaFuncSetAttribute(k_time_adj<A_, B_>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
+    UPPE_TIME_ADJ_CT(UPPE_TIME_ADJ_CONF)
+#undef UPPE_TIME_ADJ_CONF
+    return e;
 }
 
-// Columns per block of the adjoint time pass: five (M + 1)-point arrays per column in shared
-// memory, sized for two blocks per multiprocessor (2048 complex elements per block), 16 samples and
-// 8 FFT elements per thread.
+// Columns per block of the adjoint time pass: four (M + 1)-row arrays per column in shared memory,
+// sized for three blocks per multiprocessor (2048 complex elements per block), 16 samples and 8
+// FFT elements per thread.
 static int adjoint_cols(const UppeHandle* h) {
     int c = 2048 / h->M;
     if (c < 1) c = 1;
@@ -669,8 +717,16 @@ cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G,
     tp.logC = ilog2_exact(Ca);
     tp.spt = 16;
     const int T = h->Nt * Ca / 16;
-    const size_t smem = ((size_t)(h->M + 1) * 5 * Ca + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
+    const size_t smem = ((size_t)(h->M + 1) * 4 * Ca + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
+    const int nblk = h->S / Ca;
     h->launches++;
-    k_time_adj<8><<<h->S / Ca, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred);
+#define UPPE_TIME_ADJ_CASE(A_, B_)                                                                              \
+    if (tp.logM == A_ && tp.logC == B_) {                                                                       \
+        k_time_adj<A_, B_><<<nblk, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred); \
+        return cudaGetLastError();                                                                              \
+    }
+    UPPE_TIME_ADJ_CT(UPPE_TIME_ADJ_CASE)
+#undef UPPE_TIME_ADJ_CASE
+    k_time_adj<><<<nblk, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred);
     return cudaGetLastError();
 }

@@ -116,3 +116,52 @@ def test_gradient_matches_finite_differences(name):
     print(name, f"dtheta {theta.grad.item():.6e} fd {fd_t:.6e} ({et:.1e}); dchi3 {chi.grad.item():.6e} fd {fd_c:.6e} ({ec:.1e})")
     assert et < 2e-2 and ec < 2e-2
     dev.close()
+
+
+@pytest.mark.parametrize("n0", [513, 1025, 2049])
+def test_vjp_at_benchmark_time_axes(n0):
+    """The adjoint time pass with compile-time sizes (2048 complex elements per block: 4, 2 and 1
+    transverse points per block at N0 = 513, 1025, 2049) in one VJP of an RK4 step on a 16 x 16
+    Cartesian grid with the filamentation medium and an ionizing pulse, against the FP64 torch
+    autograd.  Bound: the VJP tolerance of the FP32 transforms, 2e-4."""
+    import torch
+    from oracle import uppe_oracle as O
+    from searay_gb300 import grid, ionization, uppe, workloads
+    from torch_reference import TorchStep
+    vd = workloads.cart_filament_128(steps=400, n_perp=16)
+    vd["wave grid"] = (n0, 16, 16, 2)
+    vd["frequency band"] = (0.0, 4.0 * (n0 - 1) / 512)
+    vd["nonlinear band"] = (0.0, 3.5 * (n0 - 1) / 512)
+    wave = vd["incoming wave"]
+    vd["incoming wave"] = lambda w, x1, x2: 3.0 * wave(w, x1, x2)
+    g = grid.VolumeGrid(vd)
+    dev = uppe.DeviceGrid(g, vd, ionization.RateCoefficients(vd["ionizer"]), "mixed")
+    chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+    mat = uppe.Material(dev, g, "cartesian", None, chi, vd["chi3"], vd["density reference"], vd["window speed"],
+                        vd["density lambda"])
+    zmat = 100.0
+    mat.UpdateMaterial(zmat)
+    orc = O.Oracle(vd)
+    orc.mat.update(zmat)
+    redchi3 = vd["chi3"] / vd["density reference"]
+    ts = TorchStep(orc)
+    q0 = orc.g.kspace(vd["incoming wave"](g.w, g.x1, g.x2))
+    rng = np.random.default_rng(11)
+    lam = (rng.standard_normal(q0.shape) + 1j * rng.standard_normal(q0.shape)) * (np.abs(q0) + 1e-3 * np.abs(q0).max())
+    z, dz = 50.0, vd["size"][2] / 400
+    x = torch.tensor(q0.real, requires_grad=True)
+    y = torch.tensor(q0.imag, requires_grad=True)
+    c3 = torch.tensor(redchi3, dtype=torch.float64, requires_grad=True)
+    q1 = ts.step(torch.complex(x, y), z, dz, c3)
+    L = (torch.as_tensor(lam).conj() * q1).real.sum()
+    L.backward()
+    g_ref = x.grad.numpy() + 1j * y.grad.numpy()
+    dred_ref = float(c3.grad)
+    out = dev.empty_field()
+    dred = dev.adjoint_step(torch.from_numpy(q0.astype(np.complex64)).cuda(),
+                            torch.from_numpy(lam.astype(np.complex64)).cuda(), out, z, dz)
+    e = rel_err(out.cpu().numpy(), g_ref)
+    ed = abs(dred - dred_ref) / abs(dred_ref)
+    print(n0, f"vjp {e:.2e} dchi3 {ed:.2e}")
+    assert e < 2e-4 and ed < 2e-4
+    dev.close()
