@@ -869,7 +869,33 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
     }
     // reverse sweep through the four stages
     CUDA_TRY(h, launch_adj_rk(h, 0, (const float2*)lam_out, nullptr, (float)(dz / 6), 0.f));
-    if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu, fused ? h->adj_E[3] : nullptr))) return rc;
+    if (fused) {
+        // per stage: the adjoint time pass, then one slice pass that finishes the stage (cotangent of
+        // q, RK bookkeeping) and forms the next stage's cotangent of J
+        const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz), ze = split_z(h, z_phase + dz);
+        const float2* const Es[4] = {h->adj_E[3], h->adj_E[2], h->adj_E[1], h->adj_E[0]};
+        const float af[3] = {(float)(dz / 3), (float)(dz / 3), (float)(dz / 6)};
+        const float am[3] = {(float)dz, (float)(dz / 2), (float)(dz / 2)};
+        const StepArgs ze_[4] = {ze, zh, zh, z0};
+        h->E_valid = 0;
+        PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_S, h->adj_lk, h->J, ze));
+        for (int s = 0; s < 4; ++s) {
+            PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_adjoint(h, Es[s], h->J, h->k1, h->dred_d));
+            if (s < 3) {
+                PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_reg(h, 1, h->k1, h->J, af[s], am[s], ze_[s], ze_[s + 1]));
+            } else {
+                PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_reg(h, 2, h->k1, (float2*)lam_in, 0.f, 0.f, z0, z0));
+            }
+        }
+        if (dred_out) {
+            double d = 0.0;
+            CUDA_TRY(h, cudaMemcpyAsync(&d, h->dred_d, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+            CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+            *dred_out += d;
+        }
+        return UPPE_OK;
+    }
+    if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu, nullptr))) return rc;
     CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)dz));
     if ((rc = vjp_rhs(h, h->adj_q2, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu, h->adj_E[2]))) return rc;
     CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)(dz / 2)));

@@ -732,6 +732,53 @@ __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     }
 }
 
+// The end of one stage of the reverse RK4 sweep fused with the start of the next (the kernels
+// k_adj_reg ADJ_E, k_adj_rk and k_adj_reg ADJ_S in one pass over a slice):
+//   mu = conj(D0) (1/N) F g  at z_e (the cotangent of q from the cotangent g of E),
+//   mode 1: cm = cond mu, acc += cm, lam_k = a_f lam_f + a_mu cm, out = F^H( conj(D2) lam_k ) at z_s
+//           (the cotangent of J for the next stage's time pass);
+//   mode 2: lam_in = acc + mu (the cotangent of the step's input, written to out).
+// mu and lam_k stay in registers.
+template <int LN1, int LN2>
+__global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
+    k_adj_fused_reg(int mode, const float2* __restrict__ g, OpView opv, const float2* __restrict__ lam_f,
+                    float2* __restrict__ acc, float2* __restrict__ out, float a_f, float a_mu,
+                    const float2* __restrict__ tw, int twLog, StepArgs z_e, StepArgs z_s) {
+    using RS = RegSlice<LN1, LN2>;
+    extern __shared__ float2 sm[];
+    const int tid = threadIdx.x, iw = blockIdx.x;
+    const size_t base = (size_t)iw * RS::S;
+    const TwGlobal twg{tw, twLog};
+    const RegCoords<RS> c(sm, tid, false);
+    const PhaseArgs pe{z_e.zhi, z_e.zlo, z_e.plain};
+    const PhaseArgs ps{z_s.zhi, z_s.zlo, z_s.plain};
+    const float2 kgw = opv.kg[iw];
+    const float cond = (iw < opv.ncond) ? 0.f : 1.f;
+    float2 w[16], v[16];
+    slice_fwd_from_global<RS, LN1, LN2, false>(g + base, w, sm, c, twg);
+    constexpr float scale = 1.0f / (float)RS::S;
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const size_t idx = base + col_elem(c, r);
+        const OpPoint o = op_at(opv, idx, kgw);
+        const float2 mu = cmul(cconj(op_ikz(o)), cmul(cconj(propagator_factor(o, pe, 1.f)), cscale(w[r], scale)));
+        if (mode == 2) {
+            out[idx] = cadd(acc[idx], mu);
+        } else {
+            const float2 cm = cscale(mu, cond);
+            acc[idx] = cadd(acc[idx], cm);
+            const float2 lk = cadd(cscale(lam_f[idx], a_f), cscale(cm, a_mu));
+            const float2 f = cconj(propagator_factor(o, ps, -1.f));
+            w[r] = cscale(cmul_mi(cmul(f, lk)), 0.5f / o.kzr);
+        }
+    }
+    if (mode == 2) return;
+    slice_inv_to_rows<RS, LN1, LN2, true>(w, v, sm, c, twg);
+    float2* dst = out + base + (size_t)c.x * RS::N2 + c.jr;
+#pragma unroll
+    for (int m = 0; m < 16; ++m) dst[RS::R2 * m] = v[m];
+}
+
 // Supported shapes (log2 N1, log2 N2).
 #define UPPE_REG_SHAPES(X) \
     X(4, 4) X(4, 5) X(4, 6) X(4, 7) X(5, 4) X(5, 5) X(5, 6) X(5, 7) X(6, 4) X(6, 5) X(6, 6) X(6, 7) X(7, 4) X(7, 5) X(7, 6) X(7, 7)
