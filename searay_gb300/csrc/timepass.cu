@@ -473,9 +473,17 @@ __device__ __forceinline__ void pack_half_spectrum(float2* Z, int C, int logC, i
 // sizes from the parameters.
 //
 // Shared layout: Ze [M+1][C] (e pairs, then ge pairs), Zn [M+1][C] (the raw E, then the rate pairs,
-// then the pairs of the density exponent S), Zp [M+1][C] (gp pairs), Zl [M+1][C] (the raw G, then
-// the gpl pairs), the half twiddle table, one float-float segment total per thread.  ne and
+// then the pairs of the density exponent S), Zp [M+1][C] (gp pairs), Zl [M+1][C] (the raw G, then,
+// in blocks with a nonzero rate, the gpl pairs), the half twiddle table, one float-float segment total per thread.  ne and
 // ng w exp(-S) are formed from S where they are used.  Rows in the order of RowSwizzle.
+// The three inverse transforms of the adjoint time pass share one out-of-line copy of the
+// compile-time Stockham transform (inlined three times, with the segment loops, the kernel's
+// code outgrew the instruction cache).
+template <int LOGM, int LOGC>
+__device__ __noinline__ void adj_inverse_fft_ct(float2* Z, const float2* twl, int tid) {
+    fft_axis_ct<8, LOGM, LOGC, LOGM + 1>(Z, TwHalfSharedCT<LOGM + 1>{twl}, true, tid);
+}
+
 template <int LOGM = 0, int LOGC = -1>
 __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time_adj(const float2* __restrict__ E,
                                                                    const float2* __restrict__ G,
@@ -504,7 +512,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
     const RowSwizzle sw{logC <= 2 ? M - 1 : 0, logC == 0 ? 4 : 3};
     const auto inv_fft = [&](float2* Z) {
         if constexpr (CT)
-            fft_axis_ct<8, LOGM, LOGC, LOGM + 1>(Z, TwHalfSharedCT<LOGM + 1>{twl}, true, tid);
+            adj_inverse_fft_ct<LOGM, LOGC>(Z, twl, tid);
         else
             fft_axis_tw<8>(Z, tp.logM, logC, 1, C, tws, true, tid, T, -1, sw);
     };
@@ -527,15 +535,6 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
         const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
         return cscale(cmul_i(Zl[sw(k) * C + c]), wk * wt * filt[k]);
     }, tid, T, sw);
-    if (ionize) {
-        __syncthreads();  // every read of G for Gp precedes the packing of Gl over it
-        pack_half_spectrum(Zl, C, logC, M, tws, [&](int k, int c) {
-            const float wk = wv[k];
-            const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
-            const float rden = __frcp_rn(fmaf(wk, wk, tp.damping * tp.damping));
-            return cscale(cmul(Zl[sw(k) * C + c], make_float2(tp.damping, -wk)), rden * wt * filt[k]);
-        }, tid, T, sw);
-    }
     __syncthreads();
     inv_fft(Ze);
     inv_fft(Zp);
@@ -563,7 +562,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
         if (t1 <= Nt - 2) r_next = ion_rate(tp, Ze[sw(t1 >> 1) * C + c].x * inv);
         float rn = r_next;
         bool live = r_next != 0.f;
-#pragma unroll
+#pragma unroll 1
         for (int j = MPS - 1; j >= 0; --j) {
             const int m = m0 + j;
             const float2 zv = Ze[sw(m) * C + c];
@@ -581,7 +580,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
     if (ion) {
         ffloat Sacc = later_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
         float rn = r_next;
-#pragma unroll
+#pragma unroll 1
         for (int j = MPS - 1; j >= 0; --j) {
             const int m = m0 + j;
             const float2 rr = Zn[sw(m) * C + c];
@@ -592,7 +591,14 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
             rn = rr.x;
             Zn[sw(m) * C + c] = make_float2(ff_value(Sacc), S1);
         }
-        __syncthreads();  // segment totals are reused below
+        // Gl over the raw G, which Zl has held since staging (its pack reads every G it overwrites)
+        pack_half_spectrum(Zl, C, logC, M, tws, [&](int k, int c) {
+            const float wk = wv[k];
+            const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
+            const float rden = __frcp_rn(fmaf(wk, wk, tp.damping * tp.damping));
+            return cscale(cmul(Zl[sw(k) * C + c], make_float2(tp.damping, -wk)), rden * wt * filt[k]);
+        }, tid, T, sw);
+        __syncthreads();  // the packed Gl is complete; the segment totals are reused below
         inv_fft(Zl);
     }
 
@@ -600,7 +606,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
     ffloat carry = {0.f, 0.f};
     if (ion) {
         ffloat part = {0.f, 0.f};
-#pragma unroll
+#pragma unroll 1
         for (int j = 0; j < MPS; ++j) {
             const int m = m0 + j;
             const float2 e2 = Ze[sw(m) * C + c], l2 = Zl[sw(m) * C + c], s2 = Zn[sw(m) * C + c];
@@ -615,7 +621,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
     float dred_part = 0.f;
     {
         ffloat Pprev = carry;  // Pfx(t - 1)
-#pragma unroll
+#pragma unroll 1
         for (int j = 0; j < MPS; ++j) {
             const int m = m0 + j;
             const float2 e2 = Ze[sw(m) * C + c];
