@@ -113,6 +113,7 @@ static StepArgs split_z(const UppeHandle* h, double z) {
 static void free_buffers(UppeHandle* h) {
     void* ptrs[] = {h->q,  h->qi,   h->qf,   h->k1,   h->E,     h->J,      h->scratch, h->opK,  h->opKi, h->kg2,
                     h->ng, h->tw,   h->w,    h->nlfilt, h->Minv, h->Mfwd, h->kr2_d, h->w2n2_d, h->kg_d, h->red, h->dev_err, h->Minv_tc, h->Mfwd_tc,
+                    h->MfwdT_tc, h->MinvT_tc,
                     h->adj_q1, h->adj_q2, h->adj_q3, h->adj_lf, h->adj_acc, h->adj_lk, h->adj_mu, h->MfwdT, h->MinvT,
                     h->adj_E[0], h->adj_E[1], h->adj_E[2], h->adj_E[3],
                     h->dred_d, h->rot, h->Atc};
@@ -348,6 +349,15 @@ extern "C" int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, 
             if (!h->MinvT) CUDA_TRY(h, cudaMalloc((void**)&h->MinvT, MiT.size() * sizeof(float)));
             CUDA_TRY(h, cudaMemcpy(h->MfwdT, MfT.data(), MfT.size() * sizeof(float), cudaMemcpyHostToDevice));
             CUDA_TRY(h, cudaMemcpy(h->MinvT, MiT.data(), MiT.size() * sizeof(float), cudaMemcpyHostToDevice));
+            if (c.precision == UPPE_PREC_MIXED) {  // the adjoint transforms on the tensor cores
+                std::vector<uint8_t> t;
+                uppe_split_matrix_tiles(MfT.data(), 1, Nr, Nr, t);
+                if (!h->MfwdT_tc) CUDA_TRY(h, cudaMalloc((void**)&h->MfwdT_tc, t.size()));
+                CUDA_TRY(h, cudaMemcpy(h->MfwdT_tc, t.data(), t.size(), cudaMemcpyHostToDevice));
+                uppe_split_matrix_tiles(MiT.data(), 1, Nr, Nr, t);
+                if (!h->MinvT_tc) CUDA_TRY(h, cudaMalloc((void**)&h->MinvT_tc, t.size()));
+                CUDA_TRY(h, cudaMemcpy(h->MinvT_tc, t.data(), t.size(), cudaMemcpyHostToDevice));
+            }
         }
         if (c.precision == UPPE_PREC_MIXED) {
             std::vector<uint8_t> t;

@@ -170,7 +170,7 @@ static cudaError_t launch_azimuth(UppeHandle* h, const float2* in, float2* out, 
     return cudaGetLastError();
 }
 
-cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* A, int inverse, float2* C0,
+cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* A, int which, float2* C0,
                              float2* C1, const float2* qi, int NI, int NK, int spec_mode, float Cs, float Ce,
                              StepArgs z);
 
@@ -252,10 +252,14 @@ cudaError_t launch_spec_cyl(UppeHandle* h, int mode, const float2* src_real, flo
     return run_gemm<A_PLAIN, C_SPEC>(h, g);
 }
 
-// Adjoint transverse transforms on cylindrical grids (one azimuthal node), FP32 SIMT GEMMs with the
-// transposed folded matrices: ADJ_S / ADJ_LOAD apply Mfwd^T, ADJ_E / ADJ_FIN apply Minv^T.
+// Adjoint transverse transforms on cylindrical grids (one azimuthal node) with the transposed folded
+// matrices: ADJ_S / ADJ_LOAD apply Mfwd^T, ADJ_E / ADJ_FIN apply Minv^T; the tensor-core GEMM in the
+// mixed-precision form, the FP32 SIMT GEMM in the plain form.
 template <int AMODE, int CMODE>
-static cudaError_t run_gemm_simt(UppeHandle* h, GemmArgs& g) {
+static cudaError_t run_gemm_adj(UppeHandle* h, GemmArgs& g) {
+    if (h->cfg.precision == UPPE_PREC_MIXED)
+        return launch_hankel_tc(h, AMODE, CMODE, g.A, g.B == h->MfwdT ? 2 : 3, g.C0, g.C1, g.qi, g.NI, g.NK,
+                                g.spec_mode, g.Cs, g.Ce, g.z);
     dim3 grid((g.NI + GBN - 1) / GBN, (g.N0 + GBM - 1) / GBM, g.N2);
     h->launches++;
     k_hankel_gemm<AMODE, CMODE><<<grid, 256, 0, h->stream>>>(g);
@@ -271,15 +275,15 @@ cudaError_t launch_adj_cyl(UppeHandle* h, int mode, const float2* in, float2* ou
     switch (mode) {
         case ADJ_S:
             g.B = h->MfwdT;
-            return run_gemm_simt<A_SADJ, C_STORE>(h, g);
+            return run_gemm_adj<A_SADJ, C_STORE>(h, g);
         case ADJ_LOAD:
             g.B = h->MfwdT;
-            return run_gemm_simt<A_PLAIN, C_STORE>(h, g);
+            return run_gemm_adj<A_PLAIN, C_STORE>(h, g);
         case ADJ_E:
             g.B = h->MinvT;
-            return run_gemm_simt<A_PLAIN, C_QADJ>(h, g);
+            return run_gemm_adj<A_PLAIN, C_QADJ>(h, g);
         default:
             g.B = h->MinvT;
-            return run_gemm_simt<A_PLAIN, C_FADJ>(h, g);
+            return run_gemm_adj<A_PLAIN, C_FADJ>(h, g);
     }
 }

@@ -29,8 +29,10 @@
 #define TC_STAGE_LD (TC_N + 1)              // padded row of the epilogue staging tile (float2)
 #define TC_WAIT_LIMIT (1 << 24)
 
-enum { TA_PLAIN = 0, TA_QPHASE_IKZ = 1, TA_QPHASE = 2, TA_PRESPLIT = 3 };
-enum { TC_STORE = 0, TC_FINISH1 = 1, TC_SPEC = 2 };
+// operand modes (TA_SADJ: the cotangent of S times conj(D2), the A operand of the adjoint ADJ_S)
+enum { TA_PLAIN = 0, TA_QPHASE_IKZ = 1, TA_QPHASE = 2, TA_PRESPLIT = 3, TA_SADJ = 4 };
+// epilogues (TC_QADJ / TC_FADJ: conj(D0) C and conj(exp(i(kz+kg)z)) C of the adjoint ADJ_E / ADJ_FIN)
+enum { TC_STORE = 0, TC_FINISH1 = 1, TC_SPEC = 2, TC_QADJ = 3, TC_FADJ = 4 };
 
 struct TcArgs {
     const float2* A;
@@ -187,7 +189,12 @@ __global__ void __launch_bounds__(256) k_hankel_tc_prep(TcArgs g, uint8_t* __res
     if (w < g.N0 && k < g.NK) {
         const size_t idx = ((size_t)w * g.N1 + k) * g.N2 + m;
         v = g.A[idx];
-        if (AMODE != TA_PLAIN) {
+        if (AMODE == TA_SADJ) {
+            // conj(D2) v, D2 = (i/2) exp(-i(kz+kg)z) / Re kz
+            const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
+            const float2 f = cconj(propagator_factor(o, pa, -1.f));
+            v = cscale(cmul_mi(cmul(f, v)), 0.5f / o.kzr);
+        } else if (AMODE != TA_PLAIN) {
             const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
             v = cmul(propagator_factor(o, pa, 1.f), v);
             if (AMODE == TA_QPHASE_IKZ) v = op_field(g.op, o, v);
@@ -307,6 +314,11 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
         const size_t idx = ((size_t)w * g.N1 + i) * g.N2 + m;
         if (CMODE == TC_STORE) {
             g.C0[idx] = v;
+        } else if (CMODE == TC_QADJ || CMODE == TC_FADJ) {
+            const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
+            float2 r = cmul(cconj(propagator_factor(o, pa, 1.f)), v);
+            if (CMODE == TC_QADJ) r = cmul(cconj(op_ikz(o)), r);
+            g.C0[idx] = r;
         } else if (CMODE == TC_FINISH1) {
             const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
             if (g.C0) g.C0[idx] = v;
@@ -362,14 +374,18 @@ static cudaError_t run_tc(UppeHandle* h, TcArgs& a) {
     return cudaGetLastError();
 }
 
-// Entry used by hankel.cu in the mixed-precision form.  amode/cmode follow hankel.cu's A_*/C_* codes;
-// `inverse` selects the split tiles of Minv (else Mfwd).
-cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* A, int inverse, float2* C0,
+// Entry used by hankel.cu in the mixed-precision form.  amode/cmode follow hankel.cu's A_*/C_* codes
+// (its A_SADJ = 3 is TA_SADJ here); `which` selects the split matrix tiles: 0 Mfwd, 1 Minv,
+// 2 Mfwd^T, 3 Minv^T (the last two for the adjoint transforms).
+cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* A, int which, float2* C0,
                              float2* C1, const float2* qi, int NI, int NK, int spec_mode, float Cs, float Ce,
                              StepArgs z) {
     TcArgs a{};
     a.A = A;
-    a.Btc = inverse ? h->Minv_tc : h->Mfwd_tc;
+    const uint8_t* const tiles[4] = {h->Mfwd_tc, h->Minv_tc, h->MfwdT_tc, h->MinvT_tc};
+    if (which < 0 || which > 3 || !tiles[which]) return cudaErrorInvalidValue;
+    if (amode == 3) amode = TA_SADJ;
+    a.Btc = tiles[which];
     a.nit = (NI + TC_N - 1) / TC_N;
     a.nkt = (NK + TC_K - 1) / TC_K;
     a.op = uppe_op_view(h);
@@ -398,6 +414,8 @@ cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* 
             k_hankel_tc_prep<TA_PLAIN><<<grid, 256, 0, h->stream>>>(a, h->Atc);
         else if (amode == TA_QPHASE_IKZ)
             k_hankel_tc_prep<TA_QPHASE_IKZ><<<grid, 256, 0, h->stream>>>(a, h->Atc);
+        else if (amode == TA_SADJ)
+            k_hankel_tc_prep<TA_SADJ><<<grid, 256, 0, h->stream>>>(a, h->Atc);
         else
             k_hankel_tc_prep<TA_QPHASE><<<grid, 256, 0, h->stream>>>(a, h->Atc);
         cudaError_t e = cudaGetLastError();
@@ -406,6 +424,8 @@ cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* 
     if (cmode == TC_STORE) return run_tc<TA_PRESPLIT, TC_STORE>(h, a);
     if (cmode == TC_SPEC) return run_tc<TA_PRESPLIT, TC_SPEC>(h, a);
     if (cmode == TC_FINISH1) return run_tc<TA_PRESPLIT, TC_FINISH1>(h, a);
+    if (cmode == TC_QADJ) return run_tc<TA_PRESPLIT, TC_QADJ>(h, a);
+    if (cmode == TC_FADJ) return run_tc<TA_PRESPLIT, TC_FADJ>(h, a);
     return cudaErrorInvalidValue;
 }
 

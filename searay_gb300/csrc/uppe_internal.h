@@ -72,6 +72,8 @@ struct UppeHandle {
     float* Mfwd;     // cylindrical: [N2][Nr][Nr] (rows >= Nk zero)
     uint8_t* Minv_tc; // the same, split into bf16 hi/lo tensor-core tiles (mixed form)
     uint8_t* Mfwd_tc;
+    uint8_t* MfwdT_tc; // the transposed matrices of the adjoint transforms, split the same way
+    uint8_t* MinvT_tc;
     uint8_t* Atc;     // pre-split A operand tiles of the tensor-core Hankel transform (mixed form)
     size_t Atc_bytes;
     double* kr2_d;   // [S] transverse eigenvalues (FP64)
