@@ -163,3 +163,44 @@ def test_nonfinite_input_is_flagged():
     dev.load_field(torch.from_numpy(a).cuda())
     assert dev.nonfinite()
     dev.close()
+
+
+def test_kerr_collapse_long_run():
+    """cyl_kerr_64 (the config-1 beam: about twice the critical power of air, Kerr only, 100 fixed
+    steps over 10 cm) through 80 steps, on the GPU in both forms and in the FP64 oracle: the fields
+    agree after 80 steps (the peak has grown by about 11 %), and carried on to step 100 both have
+    overflowed, the unarrested self-focusing collapse near the end of the 10 cm (about step 88 in
+    the oracle).  Bound after 80 steps: 2e-4 of the peak field (accumulated FP32 and split-BF16
+    transform error; measured 1.9e-5 mixed, 2e-6 plain FP32)."""
+    import torch
+    from oracle import uppe_oracle as O
+    from searay_gb300 import grid, uppe, workloads
+    vd = workloads.cyl_kerr_64(steps=100)
+    g = grid.VolumeGrid(vd)
+    L = vd["size"][2]
+    dz = L / 100
+    a = vd["incoming wave"](g.w, g.x1, g.x2)
+    orc = O.Oracle(vd)
+    A80, _, _, _, n80 = orc.propagator(a, 0.0, 80 * dz, 80, dz)
+    assert n80 == 80 and np.isfinite(A80).all()
+    with np.errstate(all="ignore"):
+        A100, _, _, _, _ = orc.propagator(A80, 80 * dz, 100 * dz, 20, dz)
+    assert not np.isfinite(A100).all()
+    for precision in ("mixed", "fp32"):
+        dev = uppe.DeviceGrid(g, vd, None, precision)
+        chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+        mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd["chi3"], vd["density reference"],
+                            vd["window speed"], vd["density lambda"])
+        A, _, _, _, ev = uppe.propagator(dev, mat, torch.from_numpy(a.astype(np.complex64)).cuda(), 80, 0.0,
+                                         80 * dz, dz)
+        assert ev == 4 * 80
+        A = A.cpu().numpy()
+        e = rel_err(A, A80)
+        B, _, _, _, _ = uppe.propagator(dev, mat, torch.from_numpy(A.astype(np.complex64)).cuda(), 20, 80 * dz,
+                                        100 * dz, dz)
+        finite100 = bool(np.isfinite(B.cpu().numpy()).all())
+        print(precision, f"80 steps {e:.2e}", "finite at 100:", finite100, "peak growth",
+              float(np.abs(A80).max() / np.abs(a).max()))
+        assert e < 2e-4
+        assert not finite100
+        dev.close()
