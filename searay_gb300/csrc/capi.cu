@@ -829,7 +829,7 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
     // register-resident Cartesian slices: the forward step's own kernels, the time pass and the fused
     // slice pass per stage, with the fused pass also storing the stage estimate (stage_q) and its E
     // going to the buffer the reverse sweep reads, so that E of q3' at z + dz is kept as well
-    const bool fused = !h->cfg.cylindrical && h->slice_reg && !h->slice_big;
+    const bool fused = !h->cfg.cylindrical && (h->slice_big || h->slice_reg);
     if (fused) {
         const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz), ze = split_z(h, z_phase + dz);
         float2* const E_main = h->E;
@@ -891,10 +891,14 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
         PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_S, h->adj_lk, h->J, ze));
         for (int s = 0; s < 4; ++s) {
             PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_adjoint(h, Es[s], h->J, h->k1, h->dred_d));
-            if (s < 3) {
-                PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_reg(h, 1, h->k1, h->J, af[s], am[s], ze_[s], ze_[s + 1]));
+            const int mode = (s < 3) ? 1 : 2;
+            float2* const out = (s < 3) ? h->J : (float2*)lam_in;
+            const float a_f = (s < 3) ? af[s] : 0.f, a_mu = (s < 3) ? am[s] : 0.f;
+            const StepArgs z_s = (s < 3) ? ze_[s + 1] : z0;
+            if (h->slice_big) {
+                PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_big(h, mode, h->k1, out, a_f, a_mu, ze_[s], z_s));
             } else {
-                PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_reg(h, 2, h->k1, (float2*)lam_in, 0.f, 0.f, z0, z0));
+                PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_reg(h, mode, h->k1, out, a_f, a_mu, ze_[s], z_s));
             }
         }
         if (dred_out) {

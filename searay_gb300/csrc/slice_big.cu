@@ -68,16 +68,19 @@ enum BigColKind {
     BC_REAL = 2,     // pointwise from q (REAL_* modes), inverse column FFT
     BC_ADJ_IN = 3,   // ADJ_S / ADJ_LOAD pointwise, inverse column FFT (unnormalised)
     BC_ADJ_FWD = 4,  // forward column FFT, ADJ_E / ADJ_FIN pointwise with 1/S
+    BC_ADJ_STAGE = 5,  // forward column FFT, ADJ_E, the reverse RK bookkeeping and (mode 1) ADJ_S at z1,
+                       // inverse column FFT (the column part of k_adj_fused_reg)
 };
 
 struct BigColArgs {
     int kind, mode;
     const float2* src;
     float2* dst;
-    float2 *q_out, *qf;
-    const float2 *qi, *k1;
-    float Cs, Ce;
+    float2 *q_out, *qf;  // BC_ADJ_STAGE: qf = the accumulated cotangent
+    const float2 *qi, *k1;  // BC_ADJ_STAGE: qi = lam_f
+    float Cs, Ce;           // BC_ADJ_STAGE: a_f, a_mu
     StepArgs z0, z1;
+    float2* q_store;  // BC_FUSED: also store each stage estimate here (when set)
 };
 
 template <int LN1, int LN2>
@@ -101,7 +104,7 @@ __global__ void __launch_bounds__(16 << (LN1 - 4)) k_cols_big(BigColArgs a, OpVi
     const int kind = a.kind, mode = a.mode;
     float2 v[16], w[16];
 
-    if (kind == BC_FUSED || kind == BC_SPEC || kind == BC_ADJ_FWD) {
+    if (kind == BC_FUSED || kind == BC_SPEC || kind == BC_ADJ_FWD || kind == BC_ADJ_STAGE) {
 #pragma unroll
         for (int m = 0; m < 16; ++m) v[m] = a.src[base + (size_t)(i + R1 * m) * N2 + ky];
         reg_n2m<R1, LN1, false>(v, w, ex, i, twg, sync);
@@ -114,7 +117,21 @@ __global__ void __launch_bounds__(16 << (LN1 - 4)) k_cols_big(BigColArgs a, OpVi
             const OpPoint o = op_at(opv, idx, kgw);
             const float2 qw = spec_update(mode, idx, w[r], o, cond, a.q_out, a.qf, a.qi, a.Cs, a.Ce, p0,
                                           mode == SPEC_FINISH);
+            if (a.q_store && mode != SPEC_FINISH) a.q_store[idx] = qw;
             w[r] = cmul(op_ikz(o), cmul(propagator_factor(o, p1, 1.f), qw));
+        } else if (kind == BC_ADJ_STAGE) {
+            const OpPoint o = op_at(opv, idx, kgw);
+            const float2 mu = cmul(cconj(op_ikz(o)), cmul(cconj(propagator_factor(o, p0, 1.f)),
+                                                          cscale(w[r], 1.0f / (float)(N1 * N2))));
+            if (mode == 2) {
+                a.dst[idx] = cadd(a.qf[idx], mu);
+            } else {
+                const float2 cm = cscale(mu, cond);
+                a.qf[idx] = cadd(a.qf[idx], cm);
+                const float2 lk = cadd(cscale(a.qi[idx], a.Cs), cscale(cm, a.Ce));
+                const float2 f = cconj(propagator_factor(o, p1, -1.f));
+                w[r] = cscale(cmul_mi(cmul(f, lk)), 0.5f / o.kzr);
+            }
         } else if (kind == BC_SPEC) {
             OpPoint o;
             if (mode != SPEC_LOAD) o = op_at(opv, idx, kgw);
@@ -147,7 +164,7 @@ __global__ void __launch_bounds__(16 << (LN1 - 4)) k_cols_big(BigColArgs a, OpVi
             a.dst[idx] = val;
         }
     }
-    if (kind == BC_FUSED || kind == BC_REAL || kind == BC_ADJ_IN) {
+    if (kind == BC_FUSED || kind == BC_REAL || kind == BC_ADJ_IN || (kind == BC_ADJ_STAGE && mode == 1)) {
         reg_m2n<R1, LN1, true>(w, v, ex, i, twg, sync);
 #pragma unroll
         for (int m = 0; m < 16; ++m) a.dst[base + (size_t)(i + R1 * m) * N2 + ky] = v[m];
@@ -210,8 +227,32 @@ cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepAr
     a.Ce = Ce;
     a.z0 = z_rhs;
     a.z1 = z_next;
+    a.q_store = h->stage_q;
     if (e == cudaSuccess) e = cols(h, a);
     if (e == cudaSuccess) e = rows<true>(h, h->J, h->E, 1.0f / (float)h->S, 0, nullptr);
+    return e;
+}
+
+// One stage boundary of the reverse RK4 sweep (the contract of k_adj_fused_reg): rows of the
+// cotangent g of E into J, the column pass, and (mode 1) the inverse rows into J; mode 2 writes the
+// cotangent of the step's input to out from the column pass.  J is free here (the adjoint time
+// pass has consumed it).
+cudaError_t launch_adj_fused_big(UppeHandle* h, int mode, const float2* g, float2* out, float a_f, float a_mu,
+                                 StepArgs z_e, StepArgs z_s) {
+    cudaError_t e = rows<false>(h, g, h->J, 1.f, 0, nullptr);
+    BigColArgs a{};
+    a.kind = BC_ADJ_STAGE;
+    a.mode = mode;
+    a.src = h->J;
+    a.dst = (mode == 2) ? out : h->J;
+    a.qf = h->adj_acc;
+    a.qi = h->adj_lf;
+    a.Cs = a_f;
+    a.Ce = a_mu;
+    a.z0 = z_e;
+    a.z1 = z_s;
+    if (e == cudaSuccess) e = cols(h, a);
+    if (mode == 1 && e == cudaSuccess) e = rows<true>(h, h->J, out, 1.f, 0, nullptr);
     return e;
 }
 

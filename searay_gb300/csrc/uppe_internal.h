@@ -151,6 +151,8 @@ cudaError_t launch_spec_reg(UppeHandle* h, int mode, const float2* src, float2* 
 cudaError_t launch_adj_reg(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z);
 cudaError_t launch_adj_fused_reg(UppeHandle* h, int mode, const float2* g, float2* out, float a_f, float a_mu,
                                  StepArgs z_e, StepArgs z_s);
+cudaError_t launch_adj_fused_big(UppeHandle* h, int mode, const float2* g, float2* out, float a_f, float a_mu,
+                                 StepArgs z_e, StepArgs z_s);
 
 // ---- Cartesian slices of 128 x 256, 256 x 128, 256 x 256 (slice_big.cu): row + column passes ----
 bool big_slice_supported(int N1, int N2);

@@ -76,10 +76,11 @@ def test_big_slice_vs_oracle(shape):
     dev.close()
 
 
-def test_big_slice_adjoints_match_torch_fp64():
+@pytest.mark.parametrize("shape", SHAPES, ids=lambda s: "x".join(map(str, s)))
+def test_big_slice_adjoints_match_torch_fp64(shape):
     import torch
     from torch_reference import TorchStep
-    vd, g, dev, mat, orc = _setup((33, 128, 256))
+    vd, g, dev, mat, orc = _setup(shape)
     zmat = 3000.0
     mat.UpdateMaterial(zmat)
     orc.mat.update(zmat)
