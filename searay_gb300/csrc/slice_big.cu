@@ -83,7 +83,11 @@ struct BigColArgs {
     float2* q_store;  // BC_FUSED: also store each stage estimate here (when set)
 };
 
-template <int LN1, int LN2>
+// The pass kind is a template parameter (one body per kind keeps each kernel's code small).  In the
+// kinds that update the RK or adjoint state (BC_FUSED, BC_ADJ_STAGE) the pointwise operands of eight
+// points are loaded before any store of those points: the stores could alias the loads as far as
+// the compiler knows, which otherwise serialises every point behind a full memory latency.
+template <int LN1, int LN2, int KIND>
 __global__ void __launch_bounds__(16 << (LN1 - 4)) k_cols_big(BigColArgs a, OpView opv, const float2* __restrict__ tw,
                                                               int twLog) {
     constexpr int N1 = 1 << LN1, N2 = 1 << LN2, R1 = N1 / 16, T = 16 * R1, TILES = N2 / 16;
@@ -101,70 +105,115 @@ __global__ void __launch_bounds__(16 << (LN1 - 4)) k_cols_big(BigColArgs a, OpVi
     const PhaseArgs p1{a.z1.zhi, a.z1.zlo, a.z1.plain};
     const float cond = (iw < 4) ? 0.f : 1.f;
     const float2 kgw = opv.kg[iw];
-    const int kind = a.kind, mode = a.mode;
+    const int mode = a.mode;
     float2 v[16], w[16];
+    const auto idx_of = [&](int r) {
+        const int kx = i + R1 * (r / R1) + 16 * (r % R1);
+        return base + (size_t)kx * N2 + ky;
+    };
 
-    if (kind == BC_FUSED || kind == BC_SPEC || kind == BC_ADJ_FWD || kind == BC_ADJ_STAGE) {
+    if constexpr (KIND == BC_FUSED || KIND == BC_SPEC || KIND == BC_ADJ_FWD || KIND == BC_ADJ_STAGE) {
 #pragma unroll
         for (int m = 0; m < 16; ++m) v[m] = a.src[base + (size_t)(i + R1 * m) * N2 + ky];
         reg_n2m<R1, LN1, false>(v, w, ex, i, twg, sync);
     }
+    if constexpr (KIND == BC_FUSED || KIND == BC_ADJ_STAGE) {
+        // BC_FUSED: S and the RK stage (spec_update), E of the next evaluation;
+        // BC_ADJ_STAGE: the cotangent of q, the reverse RK bookkeeping and conj(D2) (k_adj_fused_reg)
+        const bool need_a = (KIND == BC_ADJ_STAGE) || mode != SPEC_FINISH;   // qi (fused) / lam_f
+        const bool need_b = (KIND == BC_ADJ_STAGE) || mode != SPEC_STAGE1;   // qf (fused) / acc
 #pragma unroll
-    for (int r = 0; r < 16; ++r) {
-        const int kx = i + R1 * (r / R1) + 16 * (r % R1);
-        const size_t idx = base + (size_t)kx * N2 + ky;
-        if (kind == BC_FUSED) {
-            const OpPoint o = op_at(opv, idx, kgw);
-            const float2 qw = spec_update(mode, idx, w[r], o, cond, a.q_out, a.qf, a.qi, a.Cs, a.Ce, p0,
-                                          mode == SPEC_FINISH);
-            if (a.q_store && mode != SPEC_FINISH) a.q_store[idx] = qw;
-            w[r] = cmul(op_ikz(o), cmul(propagator_factor(o, p1, 1.f), qw));
-        } else if (kind == BC_ADJ_STAGE) {
-            const OpPoint o = op_at(opv, idx, kgw);
-            const float2 mu = cmul(cconj(op_ikz(o)), cmul(cconj(propagator_factor(o, p0, 1.f)),
-                                                          cscale(w[r], 1.0f / (float)(N1 * N2))));
-            if (mode == 2) {
-                a.dst[idx] = cadd(a.qf[idx], mu);
-            } else {
-                const float2 cm = cscale(mu, cond);
-                a.qf[idx] = cadd(a.qf[idx], cm);
-                const float2 lk = cadd(cscale(a.qi[idx], a.Cs), cscale(cm, a.Ce));
-                const float2 f = cconj(propagator_factor(o, p1, -1.f));
-                w[r] = cscale(cmul_mi(cmul(f, lk)), 0.5f / o.kzr);
+        for (int h8 = 0; h8 < 16; h8 += 8) {
+            float2 K8[8], A8[8], B8[8];
+            float ki8[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const size_t idx = idx_of(h8 + j);
+                K8[j] = opv.K[idx];
+                ki8[j] = opv.ki ? opv.ki[idx] : 0.f;
+                A8[j] = need_a ? a.qi[idx] : make_float2(0.f, 0.f);
+                B8[j] = need_b ? a.qf[idx] : make_float2(0.f, 0.f);
             }
-        } else if (kind == BC_SPEC) {
-            OpPoint o;
-            if (mode != SPEC_LOAD) o = op_at(opv, idx, kgw);
-            spec_update(mode, idx, w[r], o, cond, a.q_out, a.qf, a.qi, a.Cs, a.Ce, p0, true);
-        } else if (kind == BC_REAL) {
-            const OpPoint o = op_at(opv, idx, kgw);
-            float2 val;
-            if (mode == REAL_APPLY1) {
-                const float2 q0 = a.qi[idx], s = a.k1[idx];
-                a.qf[idx] = cadd(q0, cscale(s, a.Cs));
-                val = cscale(cadd(q0, cscale(s, a.Ce)), cond);
-            } else {
-                val = a.src[idx];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+                const int r = h8 + j;
+                const size_t idx = idx_of(r);
+                OpPoint o;
+                o.Khi = K8[j].x;
+                o.Klo = K8[j].y;
+                o.kzr = opv.envelope ? kgw.x : (K8[j].x - kgw.x) + (K8[j].y - kgw.y);
+                o.kzi = ki8[j];
+                if constexpr (KIND == BC_FUSED) {
+                    const float2 f = propagator_factor(o, p0, -1.f);
+                    const float2 sv = cscale(cmul_i(cmul(f, w[r])), 0.5f / o.kzr);
+                    float2 qw;
+                    if (mode == SPEC_STAGE1) {
+                        a.qf[idx] = cadd(A8[j], cscale(sv, a.Cs));
+                        qw = cscale(cadd(A8[j], cscale(sv, a.Ce)), cond);
+                    } else if (mode == SPEC_STAGE23) {
+                        a.qf[idx] = cadd(B8[j], cscale(sv, a.Cs));
+                        qw = cscale(cadd(A8[j], cscale(sv, a.Ce)), cond);
+                    } else {
+                        qw = cscale(cadd(B8[j], cscale(sv, a.Cs)), cond);
+                        a.q_out[idx] = qw;
+                    }
+                    if (a.q_store && mode != SPEC_FINISH) a.q_store[idx] = qw;
+                    w[r] = cmul(op_ikz(o), cmul(propagator_factor(o, p1, 1.f), qw));
+                } else {
+                    const float2 mu = cmul(cconj(op_ikz(o)), cmul(cconj(propagator_factor(o, p0, 1.f)),
+                                                                  cscale(w[r], 1.0f / (float)(N1 * N2))));
+                    if (mode == 2) {
+                        a.dst[idx] = cadd(B8[j], mu);
+                    } else {
+                        const float2 cm = cscale(mu, cond);
+                        a.qf[idx] = cadd(B8[j], cm);
+                        const float2 lk = cadd(cscale(A8[j], a.Cs), cscale(cm, a.Ce));
+                        const float2 f = cconj(propagator_factor(o, p1, -1.f));
+                        w[r] = cscale(cmul_mi(cmul(f, lk)), 0.5f / o.kzr);
+                    }
+                }
             }
-            val = cmul(propagator_factor(o, p0, 1.f), val);
-            if (mode != REAL_FINISH) val = cmul(op_ikz(o), val);
-            w[r] = val;
-        } else if (kind == BC_ADJ_IN) {
-            float2 val = a.src[idx];
-            if (mode == ADJ_S) {
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < 16; ++r) {
+            const size_t idx = idx_of(r);
+            if constexpr (KIND == BC_SPEC) {
+                OpPoint o;
+                if (mode != SPEC_LOAD) o = op_at(opv, idx, kgw);
+                spec_update(mode, idx, w[r], o, cond, a.q_out, a.qf, a.qi, a.Cs, a.Ce, p0, true);
+            } else if constexpr (KIND == BC_REAL) {
                 const OpPoint o = op_at(opv, idx, kgw);
-                const float2 f = cconj(propagator_factor(o, p0, -1.f));
-                val = cscale(cmul_mi(cmul(f, val)), 0.5f / o.kzr);
+                float2 val;
+                if (mode == REAL_APPLY1) {
+                    const float2 q0 = a.qi[idx], s = a.k1[idx];
+                    a.qf[idx] = cadd(q0, cscale(s, a.Cs));
+                    val = cscale(cadd(q0, cscale(s, a.Ce)), cond);
+                } else {
+                    val = a.src[idx];
+                }
+                val = cmul(propagator_factor(o, p0, 1.f), val);
+                if (mode != REAL_FINISH) val = cmul(op_ikz(o), val);
+                w[r] = val;
+            } else if constexpr (KIND == BC_ADJ_IN) {
+                float2 val = a.src[idx];
+                if (mode == ADJ_S) {
+                    const OpPoint o = op_at(opv, idx, kgw);
+                    const float2 f = cconj(propagator_factor(o, p0, -1.f));
+                    val = cscale(cmul_mi(cmul(f, val)), 0.5f / o.kzr);
+                }
+                w[r] = val;
+            } else {  // BC_ADJ_FWD
+                const OpPoint o = op_at(opv, idx, kgw);
+                float2 val = cmul(cconj(propagator_factor(o, p0, 1.f)), cscale(w[r], 1.0f / (float)(N1 * N2)));
+                if (mode == ADJ_E) val = cmul(cconj(op_ikz(o)), val);
+                a.dst[idx] = val;
             }
-            w[r] = val;
-        } else {  // BC_ADJ_FWD
-            const OpPoint o = op_at(opv, idx, kgw);
-            float2 val = cmul(cconj(propagator_factor(o, p0, 1.f)), cscale(w[r], 1.0f / (float)(N1 * N2)));
-            if (mode == ADJ_E) val = cmul(cconj(op_ikz(o)), val);
-            a.dst[idx] = val;
         }
     }
-    if (kind == BC_FUSED || kind == BC_REAL || kind == BC_ADJ_IN || (kind == BC_ADJ_STAGE && mode == 1)) {
+    const bool inverse = (KIND == BC_FUSED || KIND == BC_REAL || KIND == BC_ADJ_IN) ||
+                         (KIND == BC_ADJ_STAGE && mode == 1);
+    if (inverse) {
         reg_m2n<R1, LN1, true>(w, v, ex, i, twg, sync);
 #pragma unroll
         for (int m = 0; m < 16; ++m) a.dst[base + (size_t)(i + R1 * m) * N2 + ky] = v[m];
@@ -196,16 +245,29 @@ static cudaError_t rows(UppeHandle* h, const float2* src, float2* dst, float sca
     return cudaGetLastError();
 }
 
+template <int KIND>
+static void cols_kind(UppeHandle* h, const BigColArgs& a, const OpView& opv, unsigned grid) {
+    if (h->N1 == 256 && h->N2 == 256)
+        k_cols_big<8, 8, KIND><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+    else if (h->N1 == 256)
+        k_cols_big<8, 7, KIND><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+    else
+        k_cols_big<7, 8, KIND><<<grid, 128, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+}
+
 static cudaError_t cols(UppeHandle* h, const BigColArgs& a) {
     h->launches++;
     const OpView opv = uppe_op_view(h);
     const unsigned grid = (unsigned)(h->N0 * (h->N2 / 16));
-    if (h->N1 == 256 && h->N2 == 256)
-        k_cols_big<8, 8><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog);
-    else if (h->N1 == 256)
-        k_cols_big<8, 7><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog);
-    else
-        k_cols_big<7, 8><<<grid, 128, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+    switch (a.kind) {
+        case BC_FUSED: cols_kind<BC_FUSED>(h, a, opv, grid); break;
+        case BC_SPEC: cols_kind<BC_SPEC>(h, a, opv, grid); break;
+        case BC_REAL: cols_kind<BC_REAL>(h, a, opv, grid); break;
+        case BC_ADJ_IN: cols_kind<BC_ADJ_IN>(h, a, opv, grid); break;
+        case BC_ADJ_FWD: cols_kind<BC_ADJ_FWD>(h, a, opv, grid); break;
+        case BC_ADJ_STAGE: cols_kind<BC_ADJ_STAGE>(h, a, opv, grid); break;
+        default: return cudaErrorInvalidValue;
+    }
     return cudaGetLastError();
 }
 
