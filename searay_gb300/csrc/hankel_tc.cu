@@ -9,8 +9,9 @@
 //     no-swizzle K-major core-matrix layout; the accumulator lives in tensor memory (TMEM) and is
 //     read back with tcgen05.ld for the fused epilogue (store, finish, or ODE RHS + RK stage);
 //   * the A operand (the field with its propagator phase and i kz where the mode asks) is formed and
-//     split once per transform by k_hankel_tc_prep into tiles in that same layout, so every output
-//     tile fills its stages with 16-byte asynchronous copies, as it does for B.
+//     split once per transform by k_hankel_tc_prep into tiles in that same layout, so every K step
+//     of an output tile is two contiguous 32 KB blocks (A and B), fetched by bulk copies into a ring
+//     of three shared-memory stages.
 // Every wait on an mbarrier is bounded; on expiry the kernel records an error flag and skips ahead.
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -96,54 +97,14 @@ __device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bflo
 
 #define TC_THREADS 512  // 16 warps: the copies and the fused epilogue are spread over more threads
 #define TC_STAGE_BYTES (4 * TC_TILE_BYTES)  // A_hi | A_lo | B_hi | B_lo
+#define TC_NSTAGE 3                         // pipeline stages of the K loop (192 KB)
 
-__device__ __forceinline__ void cp_async16(uint32_t smem_addr, const void* g) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_addr), "l"(g));
-}
-
-// One K tile into a pipeline stage: the B tile (already split and laid out in global memory) by
-// asynchronous 16-byte copies, the A tile computed from the fields (phase, i kz) and split in place.
-template <int AMODE>
-__device__ __forceinline__ void tc_load_tile(const TcArgs& g, uint8_t* st, uint32_t st_a, const uint8_t* Btile,
-                                             int w0, int k0, int m, const PhaseArgs& pa, int tid) {
-    for (int c = tid; c < 2 * TC_TILE_BYTES / 16; c += TC_THREADS)
-        cp_async16(st_a + 2 * TC_TILE_BYTES + 16 * c, Btile + 16 * c);
-    if constexpr (AMODE == TA_PRESPLIT) {
-        const uint8_t* Atile =
-            g.Atc + (((size_t)m * g.nwt + w0 / TC_W) * g.nkt + k0 / TC_K) * (size_t)(2 * TC_TILE_BYTES);
-        for (int c = tid; c < 2 * TC_TILE_BYTES / 16; c += TC_THREADS) cp_async16(st_a + 16 * c, Atile + 16 * c);
-        asm volatile("cp.async.commit_group;\n" ::);
-        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-        return;
-    }
-    asm volatile("cp.async.commit_group;\n" ::);
-#pragma unroll 4
-    for (int e = tid; e < TC_W * TC_K; e += TC_THREADS) {
-        const int kk = e & (TC_K - 1), wl = e >> 6;
-        const int w = w0 + wl, k = k0 + kk;
-        float2 v = make_float2(0.f, 0.f);
-        if (w < g.N0 && k < g.NK) {
-            const size_t idx = ((size_t)w * g.N1 + k) * g.N2 + m;
-            v = g.A[idx];
-            if (AMODE != TA_PLAIN) {
-                const OpPoint o = op_at(g.op, idx, g.op.kg[w]);
-                v = cmul(propagator_factor(o, pa, 1.f), v);
-                if (AMODE == TA_QPHASE_IKZ) v = op_field(g.op, o, v);
-            }
-        }
-        __nv_bfloat16 rh, rl, ih, il;
-        split_bf16(v.x, rh, rl);
-        split_bf16(v.y, ih, il);
-        const uint32_t ore = core_off(2 * wl, kk), oim = core_off(2 * wl + 1, kk);
-        *reinterpret_cast<__nv_bfloat16*>(st + ore) = rh;
-        *reinterpret_cast<__nv_bfloat16*>(st + oim) = ih;
-        *reinterpret_cast<__nv_bfloat16*>(st + TC_TILE_BYTES + ore) = rl;
-        *reinterpret_cast<__nv_bfloat16*>(st + TC_TILE_BYTES + oim) = il;
-    }
-    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
-    // make the generic-proxy and cp.async writes visible to the tensor core (async proxy)
-    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+// One 16-byte-aligned block of global memory (a multiple of 16 bytes) into this CTA's shared memory
+// by the bulk-copy engine; completion is counted in transaction bytes on the mbarrier.
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t mbar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
 }
 
 __device__ __forceinline__ void tc_issue(uint32_t tmem_d, uint32_t st_a, uint32_t idesc, bool first, uint32_t mbar) {
@@ -174,7 +135,7 @@ __device__ __forceinline__ void tc_issue(uint32_t tmem_d, uint32_t st_a, uint32_
 }
 
 // The A operand tiles of one transform: element (w, k) of azimuthal mode m, with the propagator phase
-// and i kz as AMODE asks (the arithmetic of tc_load_tile), split into bf16 hi/lo at rows 2(w - w0)
+// and i kz as AMODE asks, split into bf16 hi/lo at rows 2(w - w0)
 // and 2(w - w0) + 1 of its tile, zero outside [N0) x [NK).  One thread per element of the padded
 // [nwt * 64][nkt * 64] grid; consecutive threads take consecutive k.
 template <int AMODE>
@@ -212,15 +173,21 @@ __global__ void __launch_bounds__(256) k_hankel_tc_prep(TcArgs g, uint8_t* __res
     *reinterpret_cast<__nv_bfloat16*>(tile + TC_TILE_BYTES + oim) = il;
 }
 
+// The GEMM of one output tile (64 frequencies x 128 columns) on pre-split operand tiles (AMODE =
+// TA_PRESPLIT).  Thread 0 drives a ring of TC_NSTAGE stages: it issues both 32 KB tiles of a K step
+// as bulk copies that complete on the stage's `full` mbarrier, waits for them, issues the MMAs of the
+// step (committed to the stage's `done` mbarrier), and refills the stage of the previous step once
+// its MMAs have completed, so the copies run TC_NSTAGE - 1 steps ahead of the tensor core.
 template <int AMODE, int CMODE>
 __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
+    static_assert(AMODE == TA_PRESPLIT, "the GEMM reads pre-split operand tiles");
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    // two pipeline stages of [A_hi | A_lo | B_hi | B_lo] (1024-byte aligned), reused afterwards as
-    // the epilogue staging tile
+    // TC_NSTAGE pipeline stages of [A_hi | A_lo | B_hi | B_lo] (1024-byte aligned), reused afterwards
+    // as the epilogue staging tile
     const uint32_t raw_a = (uint32_t)__cvta_generic_to_shared(smem_raw);
     uint8_t* tiles = smem_raw + (((raw_a + 1023u) & ~1023u) - raw_a);
     float2* stage = reinterpret_cast<float2*>(tiles);
-    __shared__ uint64_t mbar[2];
+    __shared__ uint64_t full[TC_NSTAGE], done[TC_NSTAGE];
     __shared__ uint32_t tmem_slot;
     __shared__ int aborted;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -230,12 +197,14 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
     const int i0 = it * TC_N;
     const PhaseArgs pa{g.z.zhi, g.z.zlo, g.z.plain};
     const uint32_t tiles_a = smem_u32(tiles);
-    const uint32_t mb0 = smem_u32(&mbar[0]);  // mbarrier of stage s at mb0 + 8 s
+    const uint32_t full0 = smem_u32(&full[0]), done0 = smem_u32(&done[0]);  // stage s at + 8 s
 
     if (tid == 0) {
         aborted = 0;
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb0));
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mb0 + 8u));
+        for (int s2 = 0; s2 < TC_NSTAGE; ++s2) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(full0 + 8u * s2));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(done0 + 8u * s2));
+        }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     if (warp == 0) {
@@ -250,27 +219,46 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
     const int nkt = g.nkt;
     const uint32_t idesc = instr_desc();
     const uint8_t* Bbase = g.Btc + ((size_t)(m * g.nit + it) * nkt) * (2 * TC_TILE_BYTES);
+    const uint8_t* Abase = g.Atc + ((size_t)m * g.nwt + w0 / TC_W) * nkt * (size_t)(2 * TC_TILE_BYTES);
 
-    tc_load_tile<AMODE>(g, tiles, tiles_a, Bbase, w0, 0, m, pa, tid);
-    __syncthreads();
-    for (int kt = 0; kt < nkt; ++kt) {
-        const int s = kt & 1;
-        if (tid == 0 && !aborted) tc_issue(tmem_d, tiles_a + s * TC_STAGE_BYTES, idesc, kt == 0, mb0 + 8u * s);
-        if (kt + 1 < nkt) {
-            // the other stage was read by the MMAs of tile kt-1: wait for them before refilling it
-            if (kt >= 1 && !mbar_wait(mb0 + 8u * (s ^ 1), (uint32_t)(((kt - 1) >> 1) & 1), g.err)) aborted = 1;
-            tc_load_tile<AMODE>(g, tiles + (s ^ 1) * TC_STAGE_BYTES, tiles_a + (s ^ 1) * TC_STAGE_BYTES,
-                                Bbase + (size_t)(kt + 1) * (2 * TC_TILE_BYTES), w0, (kt + 1) * TC_K, m, pa, tid);
+    if (tid == 0) {
+        const auto load = [&](int kt, int s2) {
+            const uint32_t st = tiles_a + (uint32_t)s2 * TC_STAGE_BYTES, fb = full0 + 8u * s2;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(4 * TC_TILE_BYTES)
+                         : "memory");
+            bulk_g2s(st, Abase + (size_t)kt * (2 * TC_TILE_BYTES), 2 * TC_TILE_BYTES, fb);
+            bulk_g2s(st + 2 * TC_TILE_BYTES, Bbase + (size_t)kt * (2 * TC_TILE_BYTES), 2 * TC_TILE_BYTES, fb);
+        };
+        int issued = 0;  // K steps whose copies are issued
+        int landed = 0;  // K steps whose copies have been waited for
+        int mmas = 0;    // K steps whose MMAs are issued
+        bool ok = true;
+        for (; issued < nkt && issued < TC_NSTAGE; ++issued) load(issued, issued);
+        for (int kt = 0; kt < nkt && ok; ++kt) {
+            const int s2 = kt % TC_NSTAGE;
+            ok = mbar_wait(full0 + 8u * s2, (uint32_t)((kt / TC_NSTAGE) & 1), g.err);
+            if (!ok) break;
+            landed = kt + 1;
+            tc_issue(tmem_d, tiles_a + (uint32_t)s2 * TC_STAGE_BYTES, idesc, kt == 0, done0 + 8u * s2);
+            mmas = kt + 1;
+            if (kt >= 1 && issued < nkt) {
+                const int sp = (kt - 1) % TC_NSTAGE;  // == issued % TC_NSTAGE
+                ok = mbar_wait(done0 + 8u * sp, (uint32_t)(((kt - 1) / TC_NSTAGE) & 1), g.err);
+                if (!ok) break;
+                load(issued, sp);
+                ++issued;
+            }
         }
-        __syncthreads();
-        if (aborted) break;
-    }
-    // all MMAs are complete once the last commit has arrived (commits track all earlier MMAs)
-    if (!aborted) {
-        const int kl = nkt - 1;
-        if (!mbar_wait(mb0 + 8u * (kl & 1), (uint32_t)((kl >> 1) & 1), g.err)) aborted = 1;
-    } else {
-        mbar_wait(mb0 + 8u * ((nkt - 1) & 1), (uint32_t)(((nkt - 1) >> 1) & 1), nullptr);
+        // all MMAs are complete once the last commit has arrived (commits track all earlier MMAs)
+        if (ok) ok = mbar_wait(done0 + 8u * ((nkt - 1) % TC_NSTAGE), (uint32_t)(((nkt - 1) / TC_NSTAGE) & 1), g.err);
+        if (!ok) {
+            // drain: the copies still in flight into this CTA's shared memory, then the issued MMAs
+            for (int t = landed; t < issued; ++t)
+                mbar_wait(full0 + 8u * (t % TC_NSTAGE), (uint32_t)((t / TC_NSTAGE) & 1), nullptr);
+            if (mmas > 0)
+                mbar_wait(done0 + 8u * ((mmas - 1) % TC_NSTAGE), (uint32_t)(((mmas - 1) / TC_NSTAGE) & 1), nullptr);
+            aborted = 1;
+        }
     }
     asm volatile("tcgen05.fence::after_thread_sync;\n");
     __syncthreads();
@@ -353,7 +341,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
 }
 
 static size_t tc_smem_bytes() {
-    const size_t ops = 2 * (size_t)TC_STAGE_BYTES;
+    const size_t ops = TC_NSTAGE * (size_t)TC_STAGE_BYTES;
     const size_t stage = (size_t)TC_W * TC_STAGE_LD * sizeof(float2);
     return (ops > stage ? ops : stage) + 1024;  // + alignment slack
 }
