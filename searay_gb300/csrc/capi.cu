@@ -531,11 +531,13 @@ static int rk4_step_cartesian(UppeHandle* h, double z_phase, double L, double z_
     }
     const StepArgs zh = split_z(h, z_phase + 0.5 * dz), ze = split_z(h, z_phase + dz);
     PROF_TRY(h, UPPE_CLASS_TIME, launch_time_pass(h, TIME_J, h->E, h->J, nullptr));
-    PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, launch_fused_cart(h, SPEC_STAGE23, (float)(dz / 3), (float)(dz / 2), zh, zh));
+    PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
+             launch_fused_cart(h, SPEC_STAGE23, (float)(dz / 3), (float)(dz / 2), zh, zh, /*zs_current=*/true));
     PROF_TRY(h, UPPE_CLASS_TIME, launch_time_pass(h, TIME_J, h->E, h->J, nullptr));
     PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, launch_fused_cart(h, SPEC_STAGE23, (float)(dz / 3), (float)dz, zh, ze));
     PROF_TRY(h, UPPE_CLASS_TIME, launch_time_pass(h, TIME_J, h->E, h->J, nullptr));
-    PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, launch_fused_cart(h, SPEC_FINISH, (float)(dz / 6), 0.f, ze, ze));
+    PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
+             launch_fused_cart(h, SPEC_FINISH, (float)(dz / 6), 0.f, ze, ze, /*zs_current=*/true));
     h->E_valid = 1;
     h->E_z = z_phase + dz;
     h->E_mat = h->mat_version;

@@ -118,7 +118,10 @@ cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, fl
                              const float2* qi, float Cs, float Ce, StepArgs z);
 // Cartesian fused pass: forward FFT of J, RHS, RK stage (SPEC_STAGE1/STAGE23/FINISH), then E at
 // z_next from the new stage estimate; writes qf / qi as the stage requires and E.
-cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next);
+// zs_current: the slices without current (w >= nl_cut_off) already hold this stage's q and E (stage 2,
+// whose E is at the same z as stage 1's, and the finish, whose E is at the same z as stage 3's)
+cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next,
+                              bool zs_current = false);
 // Cartesian first stage from k1 (adaptive step) fused with the inverse transform to E.
 cudaError_t launch_apply1_cart(UppeHandle* h, float Cs, float Ce, StepArgs z);
 cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1);

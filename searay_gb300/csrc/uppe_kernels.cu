@@ -449,7 +449,8 @@ cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, fl
     return cudaGetLastError();
 }
 
-cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
+cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next,
+                              bool zs_current) {
     if (h->slice_big) return launch_fused_big(h, mode, Cs, Ce, z_rhs, z_next);
     if (h->slice_reg) {
         // The NL filter leaves the slices w >= nl_cut_off without current (J = 0, so S = 0): the fused
@@ -459,6 +460,11 @@ cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepA
         if (!h->cfg.envelope && h->cfg.nl_cut_on <= 0 && jhi > 0 && jhi < h->N0) {
             cudaError_t e = launch_fused_reg(h, mode, Cs, Ce, z_rhs, z_next, jhi);
             if (e != cudaSuccess) return e;
+            // With S = 0 there, those slices keep q = cond qi through the step (qf = qi after stage 1),
+            // so stage 2 would rewrite stage 1's E and the finish stage 3's E, and the finish would
+            // write q = qi back (cond = 1 above the conditioned bins): both are left out, except
+            // when the stage estimates are being stored (stage_q)
+            if (zs_current && jhi >= 4 && !h->stage_q) return cudaSuccess;
             if (mode == SPEC_STAGE1)
                 return launch_real_reg_range(h, REAL_ZS1, h->qi, nullptr, nullptr, h->qf, 0.f, 0.f, z_next, jhi,
                                              h->N0 - jhi);
