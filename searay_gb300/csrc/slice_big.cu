@@ -255,10 +255,11 @@ static void cols_kind(UppeHandle* h, const BigColArgs& a, const OpView& opv, uns
         k_cols_big<7, 8, KIND><<<grid, 128, 0, h->stream>>>(a, opv, h->tw, h->twLog);
 }
 
-static cudaError_t cols(UppeHandle* h, const BigColArgs& a) {
+// Column passes of the slices [0, nslices) (every slice when nslices < 0).
+static cudaError_t cols(UppeHandle* h, const BigColArgs& a, int nslices = -1) {
     h->launches++;
     const OpView opv = uppe_op_view(h);
-    const unsigned grid = (unsigned)(h->N0 * (h->N2 / 16));
+    const unsigned grid = (unsigned)((nslices < 0 ? h->N0 : nslices) * (h->N2 / 16));
     switch (a.kind) {
         case BC_FUSED: cols_kind<BC_FUSED>(h, a, opv, grid); break;
         case BC_SPEC: cols_kind<BC_SPEC>(h, a, opv, grid); break;
@@ -271,11 +272,15 @@ static cudaError_t cols(UppeHandle* h, const BigColArgs& a) {
     return cudaGetLastError();
 }
 
-cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next) {
+cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next,
+                             bool zs_current) {
     // The time pass's NL filter leaves J = 0 on the slices w >= nl_cut_off: their forward row
     // transforms are left out (the column pass then reads those zeros, and S = 0 there exactly).
+    // In stage 2 and the finish those slices already hold their q and E (launch_fused_cart): the
+    // column and inverse row passes leave them out as well.
     const int jhi = h->cfg.nl_cut_off;
     const int nfwd = (!h->cfg.envelope && h->cfg.nl_cut_on <= 0 && jhi > 0 && jhi < h->N0) ? jhi : h->N0;
+    const int nall = (zs_current && nfwd < h->N0 && jhi >= 4 && !h->stage_q) ? nfwd : h->N0;
     cudaError_t e = rows<false>(h, h->J, h->J, 1.f, 0, nullptr, nfwd);
     BigColArgs a{};
     a.kind = BC_FUSED;
@@ -290,8 +295,8 @@ cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepAr
     a.z0 = z_rhs;
     a.z1 = z_next;
     a.q_store = h->stage_q;
-    if (e == cudaSuccess) e = cols(h, a);
-    if (e == cudaSuccess) e = rows<true>(h, h->J, h->E, 1.0f / (float)h->S, 0, nullptr);
+    if (e == cudaSuccess) e = cols(h, a, nall);
+    if (e == cudaSuccess) e = rows<true>(h, h->J, h->E, 1.0f / (float)h->S, 0, nullptr, nall);
     return e;
 }
 

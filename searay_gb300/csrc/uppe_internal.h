@@ -159,7 +159,8 @@ cudaError_t launch_adj_fused_big(UppeHandle* h, int mode, const float2* g, float
 
 // ---- Cartesian slices of 128 x 256, 256 x 128, 256 x 256 (slice_big.cu): row + column passes ----
 bool big_slice_supported(int N1, int N2);
-cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next);
+cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next,
+                             bool zs_current = false);
 cudaError_t launch_real_big(UppeHandle* h, int mode, const float2* src, float2* A_out, const float2* k1, float2* qf,
                             float Cs, float Ce, StepArgs z);
 cudaError_t launch_spec_big(UppeHandle* h, int mode, const float2* src, float2* q_out, float2* qf, const float2* qi,

@@ -451,7 +451,7 @@ cudaError_t launch_spec_cart(UppeHandle* h, int mode, const float2* src_real, fl
 
 cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next,
                               bool zs_current) {
-    if (h->slice_big) return launch_fused_big(h, mode, Cs, Ce, z_rhs, z_next);
+    if (h->slice_big) return launch_fused_big(h, mode, Cs, Ce, z_rhs, z_next, zs_current);
     if (h->slice_reg) {
         // The NL filter leaves the slices w >= nl_cut_off without current (J = 0, so S = 0): the fused
         // pass walks the others, and one block per such slice applies the stage with S = 0 and forms
