@@ -42,7 +42,10 @@ UNIT = "grid-pt*steps/s"
 #   transverse_inverse: read q, K; write E
 #   time_pass: read E; write J
 #   transverse_forward_rk (fused slice pass): read J, K, qi and/or qf; write qf or qi; write E for
-#   the next evaluation -- 40 / 48 / 48 / 40 bytes for the four RK stages
+#   the next evaluation -- 40 / 48 / 48 / 40 bytes for the four RK stages.  The slices at and above
+#   the nonlinear cut carry no current (S = 0): there stage 1 reads qi and K and writes qf and E
+#   (32 bytes), stage 3 reads qi and K and writes E (24 bytes), and stage 2 and the finish have
+#   nothing to do (their q and E are unchanged); see cart_forward_bytes.
 CART_BYTES = {
     "transverse_inverse": 8 + 8 + 8,
     "time_pass": 8 + 8,
@@ -58,12 +61,29 @@ CYL_BYTES = {
 }
 
 
+def cart_forward_bytes(vd):
+    """Average bytes per grid point of the Cartesian fused evaluation tail over the four RK stages,
+    with the slices without current (w >= nonlinear cut, the cut index of the library's
+    configuration) counted at what they need: 32 / 0 / 24 / 0 bytes."""
+    from searay_gb300.grid import VolumeGrid
+    N = vd["wave grid"]
+    nl = vd.get("nonlinear band", vd["frequency band"])
+    dw = VolumeGrid(vd).dw  # the cut indices of searay_gb300.uppe.DeviceGrid
+    jhi = int(nl[1] / dw)
+    if is_paraxial(vd) or int(nl[0] / dw) > 0 or not (4 <= jhi < N[0]):
+        return CART_BYTES["transverse_forward_rk"]
+    f = (N[0] - jhi) / N[0]
+    return (1 - f) * CART_BYTES["transverse_forward_rk"] + f * (32 + 0 + 24 + 0) / 4.0
+
+
 def class_models(vd):
     """{class: {"bytes": B per launch, "flops": F per launch (transverse GEMMs only)}}"""
     N = vd["wave grid"]
     P = N[0] * N[1] * N[2]
     if vd["wave coordinates"] == "cartesian":
-        return {k: {"bytes": b * P} for k, b in CART_BYTES.items()}
+        m = {k: {"bytes": b * P} for k, b in CART_BYTES.items()}
+        m["transverse_forward_rk"]["bytes"] = cart_forward_bytes(vd) * P
+        return m
     Nr, Nk = N[1], vd.get("radial modes", N[1])
     m = {k: {"bytes": b * P} for k, b in CYL_BYTES.items()}
     m["transverse_inverse"]["flops"] = 4.0 * N[0] * N[2] * Nr * Nk
