@@ -149,6 +149,17 @@ int uppe_set_field(UppeHandle* h, const void* q);
 int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0, const void* lam_out, void* lam_in, double z_phase,
                           double dz, double* dred);
 
+/* One fixed RK4 step of the held field (the step of uppe_rk4_step with dzmin = L - z_sub = dz) that
+ * keeps the E of its four stage states for uppe_adjoint_rk4_step_kept.  Cartesian grids with 16 ..
+ * 256 points per axis; UPPE_E_ARG otherwise.  Allocates the adjoint buffers on first use. */
+int uppe_rk4_step_keep(UppeHandle* h, double z_phase, double dz);
+
+/* VJP of the step last taken by uppe_rk4_step_keep: lam_in = (dq1/dq0)^H lam_out, without the
+ * recompute of uppe_adjoint_rk4_step.  UPPE_E_ARG when no such step is kept for the current
+ * material (uppe_rk4_step, uppe_adjoint_rk4_step and uppe_set_material end it).  Adds
+ * d(loss)/d(chi3/nref) to *dred (may be NULL). */
+int uppe_adjoint_rk4_step_kept(UppeHandle* h, const void* lam_out, void* lam_in, double* dred);
+
 /* VJP of uppe_load_field (q = T a): lam_a = T^H lam_q. */
 int uppe_adjoint_load(UppeHandle* h, const void* lam_q, void* lam_a);
 

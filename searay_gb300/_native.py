@@ -27,7 +27,8 @@ EXPORTS = ("uppe_create", "uppe_destroy", "uppe_set_stream", "uppe_set_grid", "u
            "uppe_load_field", "uppe_rk4_step", "uppe_finish", "uppe_eval_rhs", "uppe_get_field",
            "uppe_check_finite", "uppe_profile_enable", "uppe_profile_read", "uppe_launch_count",
            "uppe_class_name", "uppe_step_size_noalloc", "uppe_set_chi3", "uppe_set_rotator", "uppe_set_field",
-           "uppe_adjoint_rk4_step", "uppe_adjoint_load", "uppe_adjoint_finish", "uppe_last_error")
+           "uppe_adjoint_rk4_step", "uppe_rk4_step_keep", "uppe_adjoint_rk4_step_kept", "uppe_adjoint_load",
+           "uppe_adjoint_finish", "uppe_last_error")
 NOALLOC_MAX_POINTS = 1 << 27
 NCLASS = 6
 
@@ -89,6 +90,8 @@ def lib():
     L.uppe_set_rotator.argtypes = [vp, ctypes.c_int, _dp, _dp, ctypes.c_double, ctypes.c_double]
     L.uppe_set_field.argtypes = [vp, vp]
     L.uppe_adjoint_rk4_step.argtypes = [vp, vp, vp, vp, ctypes.c_double, ctypes.c_double, _dp]
+    L.uppe_rk4_step_keep.argtypes = [vp, ctypes.c_double, ctypes.c_double]
+    L.uppe_adjoint_rk4_step_kept.argtypes = [vp, vp, vp, _dp]
     L.uppe_adjoint_load.argtypes = [vp, vp, vp]
     L.uppe_adjoint_finish.argtypes = [vp, ctypes.c_double, vp, vp]
     L.uppe_last_error.argtypes = [vp]

@@ -594,6 +594,7 @@ extern "C" int uppe_rk4_step(UppeHandle* h, double z_phase, double L, double z_s
     const bool adaptive = !(dzmin >= L - z_sub);
     rc = check_range(h, z_phase + (L - z_sub));
     if (rc) return rc;
+    h->kept_valid = 0;
     double dz = 0.0;
     rc = h->cfg.cylindrical ? rk4_step_generic(h, z_phase, L, z_sub, dzmin, adaptive, &dz)
                             : rk4_step_cartesian(h, z_phase, L, z_sub, dzmin, adaptive, &dz);
@@ -814,6 +815,42 @@ static int vjp_rhs(UppeHandle* h, const float2* qs, double zs, const float2* lam
     return UPPE_OK;
 }
 
+// The reverse RK4 sweep on Cartesian grids (register-resident or big slices), from the E of the four
+// stage states in adj_E[0..3]: per stage the adjoint time pass, then one slice pass that finishes the
+// stage (cotangent of q, RK bookkeeping) and forms the next stage's cotangent of J.  dred_d is
+// accumulated from zero.
+static int reverse_sweep_fused(UppeHandle* h, const float2* lam_out, float2* lam_in, double z_phase, double dz,
+                               double* dred_out) {
+    CUDA_TRY(h, cudaMemsetAsync(h->dred_d, 0, sizeof(double), h->stream));
+    CUDA_TRY(h, launch_adj_rk(h, 0, lam_out, nullptr, (float)(dz / 6), 0.f));
+    const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz), ze = split_z(h, z_phase + dz);
+    const float2* const Es[4] = {h->adj_E[3], h->adj_E[2], h->adj_E[1], h->adj_E[0]};
+    const float af[3] = {(float)(dz / 3), (float)(dz / 3), (float)(dz / 6)};
+    const float am[3] = {(float)dz, (float)(dz / 2), (float)(dz / 2)};
+    const StepArgs ze_[4] = {ze, zh, zh, z0};
+    h->E_valid = 0;
+    PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_S, h->adj_lk, h->J, ze));
+    for (int s = 0; s < 4; ++s) {
+        PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_adjoint(h, Es[s], h->J, h->k1, h->dred_d));
+        const int mode = (s < 3) ? 1 : 2;
+        float2* const out = (s < 3) ? h->J : lam_in;
+        const float a_f = (s < 3) ? af[s] : 0.f, a_mu = (s < 3) ? am[s] : 0.f;
+        const StepArgs z_s = (s < 3) ? ze_[s + 1] : z0;
+        if (h->slice_big) {
+            PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_big(h, mode, h->k1, out, a_f, a_mu, ze_[s], z_s));
+        } else {
+            PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_reg(h, mode, h->k1, out, a_f, a_mu, ze_[s], z_s));
+        }
+    }
+    if (dred_out) {
+        double d = 0.0;
+        CUDA_TRY(h, cudaMemcpyAsync(&d, h->dred_d, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        *dred_out += d;
+    }
+    return UPPE_OK;
+}
+
 extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void* lam_out, void* lam_in, double z_phase,
                                      double dz, double* dred_out) {
     if (!h || !q0v || !lam_out || !lam_in) return UPPE_E_ARG;
@@ -824,6 +861,7 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
     rc = check_range(h, z_phase + dz);
     if (rc) return rc;
     const float2* q0 = (const float2*)q0v;
+    h->kept_valid = 0;  // the recompute below overwrites the kept stage fields
     CUDA_TRY(h, cudaMemsetAsync(h->dred_d, 0, sizeof(double), h->stream));
     // recompute the stage estimates q1', q2', q3' of the forward step (uppe_kernel.py:305-322)
     CUDA_TRY(h, cudaMemcpyAsync(h->qi, q0, h->P * sizeof(float2), cudaMemcpyDeviceToDevice, h->stream));
@@ -880,37 +918,8 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
         PROF_TRY(h, UPPE_CLASS_OTHER, spec_pass(h, SPEC_STAGE23, h->J, h->adj_q3, h->qf, h->qi, (float)(dz / 3), (float)dz, zh));
     }
     // reverse sweep through the four stages
+    if (fused) return reverse_sweep_fused(h, (const float2*)lam_out, (float2*)lam_in, z_phase, dz, dred_out);
     CUDA_TRY(h, launch_adj_rk(h, 0, (const float2*)lam_out, nullptr, (float)(dz / 6), 0.f));
-    if (fused) {
-        // per stage: the adjoint time pass, then one slice pass that finishes the stage (cotangent of
-        // q, RK bookkeeping) and forms the next stage's cotangent of J
-        const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz), ze = split_z(h, z_phase + dz);
-        const float2* const Es[4] = {h->adj_E[3], h->adj_E[2], h->adj_E[1], h->adj_E[0]};
-        const float af[3] = {(float)(dz / 3), (float)(dz / 3), (float)(dz / 6)};
-        const float am[3] = {(float)dz, (float)(dz / 2), (float)(dz / 2)};
-        const StepArgs ze_[4] = {ze, zh, zh, z0};
-        h->E_valid = 0;
-        PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_S, h->adj_lk, h->J, ze));
-        for (int s = 0; s < 4; ++s) {
-            PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_adjoint(h, Es[s], h->J, h->k1, h->dred_d));
-            const int mode = (s < 3) ? 1 : 2;
-            float2* const out = (s < 3) ? h->J : (float2*)lam_in;
-            const float a_f = (s < 3) ? af[s] : 0.f, a_mu = (s < 3) ? am[s] : 0.f;
-            const StepArgs z_s = (s < 3) ? ze_[s + 1] : z0;
-            if (h->slice_big) {
-                PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_big(h, mode, h->k1, out, a_f, a_mu, ze_[s], z_s));
-            } else {
-                PROF_TRY(h, UPPE_CLASS_OTHER, launch_adj_fused_reg(h, mode, h->k1, out, a_f, a_mu, ze_[s], z_s));
-            }
-        }
-        if (dred_out) {
-            double d = 0.0;
-            CUDA_TRY(h, cudaMemcpyAsync(&d, h->dred_d, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-            CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-            *dred_out += d;
-        }
-        return UPPE_OK;
-    }
     if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu, nullptr))) return rc;
     CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)dz));
     if ((rc = vjp_rhs(h, h->adj_q2, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu, h->adj_E[2]))) return rc;
@@ -926,6 +935,78 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
         *dred_out += d;
     }
     return UPPE_OK;
+}
+
+// One fixed RK4 step (as uppe_rk4_step with dzmin = L - z_sub) that keeps the E of its four stage
+// states in adj_E[0..3], for uppe_adjoint_rk4_step_kept.  Cartesian grids on the register-resident
+// or big-slice passes; the slices without current are processed in every stage (their E is kept).
+extern "C" int uppe_rk4_step_keep(UppeHandle* h, double z_phase, double dz) {
+    if (!h) return UPPE_E_ARG;
+    int rc = check_ready(h, true);
+    if (rc) return rc;
+    if (h->cfg.cylindrical || !(h->slice_reg || h->slice_big)) {
+        uppe_set_error(h, "uppe_rk4_step_keep: Cartesian grids with 16..256 points per axis only");
+        return UPPE_E_ARG;
+    }
+    if (!(dz > 0.0)) {
+        uppe_set_error(h, "step must be positive");
+        return UPPE_E_ARG;
+    }
+    rc = ensure_adjoint(h);
+    if (rc) return rc;
+    rc = check_range(h, z_phase + dz);
+    if (rc) return rc;
+    h->kept_valid = 0;
+    const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz), ze = split_z(h, z_phase + dz);
+    float2* const E_main = h->E;
+    // E of q0 at z0 into adj_E[0]: the E left by the previous step's finish when it is current
+    if (h->E_valid && h->E_mat == h->mat_version && same_z(h->E_z, z_phase)) {
+        h->E = h->adj_E[0];
+        h->adj_E[0] = E_main;
+    } else {
+        h->E = h->adj_E[0];
+        cudaError_t e = launch_real_cart(h, REAL_E, h->qi, nullptr, z0);
+        h->E = E_main;
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_INV, e);
+    }
+    float2* const E_next = h->E;  // the buffer that takes E of the step's result
+    h->E_valid = 0;
+    const int modes[4] = {SPEC_STAGE1, SPEC_STAGE23, SPEC_STAGE23, SPEC_FINISH};
+    const float cs[4] = {(float)(dz / 6), (float)(dz / 3), (float)(dz / 3), (float)(dz / 6)};
+    const float ce[4] = {(float)(dz / 2), (float)(dz / 2), (float)dz, 0.f};
+    const StepArgs zr[4] = {z0, zh, zh, ze}, zn[4] = {zh, zh, ze, ze};
+    cudaError_t e = cudaSuccess;
+    for (int s = 0; s < 4 && e == cudaSuccess; ++s) {
+        {
+            ProfScope ps(h, UPPE_CLASS_TIME);
+            e = launch_time_pass(h, TIME_J, h->adj_E[s], h->J, nullptr);
+        }
+        if (e != cudaSuccess) break;
+        h->E = (s < 3) ? h->adj_E[s + 1] : E_next;
+        ProfScope ps(h, UPPE_CLASS_TRANSVERSE_FWD);
+        e = launch_fused_cart(h, modes[s], cs[s], ce[s], zr[s], zn[s], /*zs_current=*/false);
+    }
+    h->E = E_next;
+    CUDA_TRY(h, e);
+    h->E_valid = 1;
+    h->E_z = z_phase + dz;
+    h->E_mat = h->mat_version;
+    h->kept_valid = 1;
+    h->kept_z = z_phase;
+    h->kept_dz = dz;
+    h->kept_mat = h->mat_version;
+    return UPPE_OK;
+}
+
+// The vector-Jacobian product of the step last taken by uppe_rk4_step_keep (lam_in = (dq1/dq0)^H
+// lam_out), from its kept stage fields: uppe_adjoint_rk4_step without the recompute.
+extern "C" int uppe_adjoint_rk4_step_kept(UppeHandle* h, const void* lam_out, void* lam_in, double* dred_out) {
+    if (!h || !lam_out || !lam_in) return UPPE_E_ARG;
+    if (!h->kept_valid || h->kept_mat != h->mat_version) {
+        uppe_set_error(h, "uppe_adjoint_rk4_step_kept: no step kept by uppe_rk4_step_keep for the current material");
+        return UPPE_E_ARG;
+    }
+    return reverse_sweep_fused(h, (const float2*)lam_out, (float2*)lam_in, h->kept_z, h->kept_dz, dred_out);
 }
 
 extern "C" int uppe_adjoint_load(UppeHandle* h, const void* lam_q, void* lam_a) {

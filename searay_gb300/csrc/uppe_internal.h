@@ -91,6 +91,9 @@ struct UppeHandle {
     float2 *adj_q1, *adj_q2, *adj_q3, *adj_lf, *adj_acc, *adj_lk, *adj_mu;
     float2* adj_E[4];      // E of the recomputed stage states q0, q1', q2', q3' (reused by the reverse sweep)
     float2* stage_q;       // when set, the Cartesian fused pass also stores each stage estimate here
+    int kept_valid;        // adj_E[0..3] hold the stage fields of the step taken by uppe_rk4_step_keep
+    double kept_z, kept_dz;
+    long long kept_mat;
     float* MfwdT;          // cylindrical adjoint: [Nr][Nr], MfwdT[r][k] = Mfwd[k][r]
     float* MinvT;          // [Nr][Nr], MinvT[k][r] = Minv[r][k] for k < Nk, 0 beyond
     double* dred_d;        // device accumulator of d(loss)/d(chi3/nref)

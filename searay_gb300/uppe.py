@@ -176,6 +176,19 @@ class DeviceGrid:
                                                    ctypes.byref(d) if want_dchi3 else None))
         return d.value if want_dchi3 else None
 
+    def rk4_step_keep(self, z_phase, dz):
+        """One fixed RK4 step of the held field that keeps its stage fields for adjoint_step_kept
+        (Cartesian grids; the result equals rk4_step's with dzmin = L - z_sub = dz)."""
+        self._check(self.lib.uppe_rk4_step_keep(self.h, z_phase, dz))
+
+    def adjoint_step_kept(self, lam_out_dev, lam_in_dev, want_dchi3=True):
+        """VJP of the step last taken by rk4_step_keep, without recomputing its stage states."""
+        d = ctypes.c_double(0.0)
+        self._check(self.lib.uppe_adjoint_rk4_step_kept(self.h, ctypes.c_void_p(lam_out_dev.data_ptr()),
+                                                        ctypes.c_void_p(lam_in_dev.data_ptr()),
+                                                        ctypes.byref(d) if want_dchi3 else None))
+        return d.value if want_dchi3 else None
+
     def adjoint_load(self, lam_q_dev, lam_a_dev):
         self._check(self.lib.uppe_adjoint_load(self.h, ctypes.c_void_p(lam_q_dev.data_ptr()),
                                                ctypes.c_void_p(lam_a_dev.data_ptr())))
