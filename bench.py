@@ -254,27 +254,26 @@ def run_device(args, vd, ws, rank, local):
         a1.record(stream)
         torch.cuda.synchronize()
         adj_ms = a0.elapsed_time(a1) / args.adjoint_steps
-        # Cartesian grids: a forward step that keeps its stage fields plus the VJP of that step from
-        # them, timed together (the pair a training step runs)
+        # a forward step that keeps its stage fields plus the VJP of that step from them, timed
+        # together (the pair a training step runs)
         pair_ms = None
-        if vd["wave coordinates"] == "cartesian":
-            dev.set_field(q)
-            try:
-                for i in range(2):
-                    dev.rk4_step_keep((step[0] + i) * dz, dz)
-                    dev.adjoint_step_kept(lam, out, want_dchi3=False)
-            except RuntimeError:
-                pass
-            else:
-                torch.cuda.synchronize()
-                a0.record(stream)
-                for i in range(args.adjoint_steps):
-                    dev.rk4_step_keep((step[0] + 2 + i) * dz, dz)
-                    dev.adjoint_step_kept(lam, out, want_dchi3=False)
-                    lam, out = out, lam
-                a1.record(stream)
-                torch.cuda.synchronize()
-                pair_ms = a0.elapsed_time(a1) / args.adjoint_steps
+        dev.set_field(q)
+        try:
+            for i in range(2):
+                dev.rk4_step_keep((step[0] + i) * dz, dz)
+                dev.adjoint_step_kept(lam, out, want_dchi3=False)
+        except RuntimeError:
+            pass
+        else:
+            torch.cuda.synchronize()
+            a0.record(stream)
+            for i in range(args.adjoint_steps):
+                dev.rk4_step_keep((step[0] + 2 + i) * dz, dz)
+                dev.adjoint_step_kept(lam, out, want_dchi3=False)
+                lam, out = out, lam
+            a1.record(stream)
+            torch.cuda.synchronize()
+            pair_ms = a0.elapsed_time(a1) / args.adjoint_steps
         adj = (adj_ms, pair_ms)
     # per-kernel-class timing (separate region; event records between launches)
     nprof = min(args.steps, 20)

@@ -150,8 +150,9 @@ int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0, const void* lam_out, vo
                           double dz, double* dred);
 
 /* One fixed RK4 step of the held field (the step of uppe_rk4_step with dzmin = L - z_sub = dz) that
- * keeps the E of its four stage states for uppe_adjoint_rk4_step_kept.  Cartesian grids with 16 ..
- * 256 points per axis; UPPE_E_ARG otherwise.  Allocates the adjoint buffers on first use. */
+ * keeps what the reverse sweep reads (the E of its four stage states, and with separate transverse
+ * passes the stage estimates) for uppe_adjoint_rk4_step_kept.  The grids the adjoint supports;
+ * UPPE_E_ARG otherwise.  Allocates the adjoint buffers on first use. */
 int uppe_rk4_step_keep(UppeHandle* h, double z_phase, double dz);
 
 /* VJP of the step last taken by uppe_rk4_step_keep: lam_in = (dq1/dq0)^H lam_out, without the

@@ -851,6 +851,32 @@ static int reverse_sweep_fused(UppeHandle* h, const float2* lam_out, float2* lam
     return UPPE_OK;
 }
 
+// The reverse RK4 sweep with separate transverse passes (cylindrical grids and the generic Cartesian
+// slices), from the stage estimates adj_q1..3 and the E of the stage states q0, q1', q2' in
+// adj_E[0..2].  E of q3' is formed here unless q0 is NULL, in which case adj_E[3] holds it (a kept
+// step).  dred_d is accumulated from zero.
+static int reverse_sweep_generic(UppeHandle* h, const float2* lam_out, float2* lam_in, double z_phase, double dz,
+                                 double* dred_out, const float2* q0) {
+    int rc;
+    CUDA_TRY(h, cudaMemsetAsync(h->dred_d, 0, sizeof(double), h->stream));
+    CUDA_TRY(h, launch_adj_rk(h, 0, lam_out, nullptr, (float)(dz / 6), 0.f));
+    if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu, q0 ? nullptr : h->adj_E[3]))) return rc;
+    CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)dz));
+    if ((rc = vjp_rhs(h, h->adj_q2, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu, h->adj_E[2]))) return rc;
+    CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)(dz / 2)));
+    if ((rc = vjp_rhs(h, h->adj_q1, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu, h->adj_E[1]))) return rc;
+    CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 6), (float)(dz / 2)));
+    if ((rc = vjp_rhs(h, q0, z_phase, h->adj_lk, h->adj_mu, h->adj_E[0]))) return rc;
+    CUDA_TRY(h, launch_adj_rk(h, 2, nullptr, lam_in, 0.f, 0.f));
+    if (dred_out) {
+        double d = 0.0;
+        CUDA_TRY(h, cudaMemcpyAsync(&d, h->dred_d, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
+        *dred_out += d;
+    }
+    return UPPE_OK;
+}
+
 extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void* lam_out, void* lam_in, double z_phase,
                                      double dz, double* dred_out) {
     if (!h || !q0v || !lam_out || !lam_in) return UPPE_E_ARG;
@@ -919,35 +945,17 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
     }
     // reverse sweep through the four stages
     if (fused) return reverse_sweep_fused(h, (const float2*)lam_out, (float2*)lam_in, z_phase, dz, dred_out);
-    CUDA_TRY(h, launch_adj_rk(h, 0, (const float2*)lam_out, nullptr, (float)(dz / 6), 0.f));
-    if ((rc = vjp_rhs(h, h->adj_q3, z_phase + dz, h->adj_lk, h->adj_mu, nullptr))) return rc;
-    CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)dz));
-    if ((rc = vjp_rhs(h, h->adj_q2, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu, h->adj_E[2]))) return rc;
-    CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 3), (float)(dz / 2)));
-    if ((rc = vjp_rhs(h, h->adj_q1, z_phase + 0.5 * dz, h->adj_lk, h->adj_mu, h->adj_E[1]))) return rc;
-    CUDA_TRY(h, launch_adj_rk(h, 1, nullptr, nullptr, (float)(dz / 6), (float)(dz / 2)));
-    if ((rc = vjp_rhs(h, q0, z_phase, h->adj_lk, h->adj_mu, h->adj_E[0]))) return rc;
-    CUDA_TRY(h, launch_adj_rk(h, 2, nullptr, (float2*)lam_in, 0.f, 0.f));
-    if (dred_out) {
-        double d = 0.0;
-        CUDA_TRY(h, cudaMemcpyAsync(&d, h->dred_d, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-        CUDA_TRY(h, cudaStreamSynchronize(h->stream));
-        *dred_out += d;
-    }
-    return UPPE_OK;
+    return reverse_sweep_generic(h, (const float2*)lam_out, (float2*)lam_in, z_phase, dz, dred_out, q0);
 }
 
 // One fixed RK4 step (as uppe_rk4_step with dzmin = L - z_sub) that keeps the E of its four stage
-// states in adj_E[0..3], for uppe_adjoint_rk4_step_kept.  Cartesian grids on the register-resident
-// or big-slice passes; the slices without current are processed in every stage (their E is kept).
+// states in adj_E[0..3] (and, with separate transverse passes, the stage estimates in adj_q1..3),
+// for uppe_adjoint_rk4_step_kept.  On the register-resident and big-slice passes the slices without
+// current are processed in every stage (their E is kept).
 extern "C" int uppe_rk4_step_keep(UppeHandle* h, double z_phase, double dz) {
     if (!h) return UPPE_E_ARG;
     int rc = check_ready(h, true);
     if (rc) return rc;
-    if (h->cfg.cylindrical || !(h->slice_reg || h->slice_big)) {
-        uppe_set_error(h, "uppe_rk4_step_keep: Cartesian grids with 16..256 points per axis only");
-        return UPPE_E_ARG;
-    }
     if (!(dz > 0.0)) {
         uppe_set_error(h, "step must be positive");
         return UPPE_E_ARG;
@@ -959,6 +967,32 @@ extern "C" int uppe_rk4_step_keep(UppeHandle* h, double z_phase, double dz) {
     h->kept_valid = 0;
     const StepArgs z0 = split_z(h, z_phase), zh = split_z(h, z_phase + 0.5 * dz), ze = split_z(h, z_phase + dz);
     float2* const E_main = h->E;
+    if (h->cfg.cylindrical || !(h->slice_reg || h->slice_big)) {
+        // separate passes per evaluation: each evaluation's E and each stage estimate kept
+        float2* const qs[3] = {h->adj_q1, h->adj_q2, h->adj_q3};
+        const float2* const qin[4] = {h->qi, h->adj_q1, h->adj_q2, h->adj_q3};
+        const int modes[4] = {SPEC_STAGE1, SPEC_STAGE23, SPEC_STAGE23, SPEC_FINISH};
+        const float cs[4] = {(float)(dz / 6), (float)(dz / 3), (float)(dz / 3), (float)(dz / 6)};
+        const float ce[4] = {(float)(dz / 2), (float)(dz / 2), (float)dz, 0.f};
+        const StepArgs zr[4] = {z0, zh, zh, ze};
+        h->E_valid = 0;
+        cudaError_t e = cudaSuccess;
+        for (int s = 0; s < 4 && e == cudaSuccess; ++s) {
+            h->E = h->adj_E[s];
+            e = eval_to_J(h, qin[s], zr[s]);
+            h->E = E_main;
+            if (e != cudaSuccess) break;
+            ProfScope ps(h, UPPE_CLASS_TRANSVERSE_FWD);
+            e = (s < 3) ? spec_pass(h, modes[s], h->J, qs[s], h->qf, h->qi, cs[s], ce[s], zr[s])
+                        : spec_pass(h, SPEC_FINISH, h->J, h->qi, h->qf, nullptr, cs[s], 0.f, zr[s]);
+        }
+        CUDA_TRY(h, e);
+        h->kept_valid = 1;
+        h->kept_z = z_phase;
+        h->kept_dz = dz;
+        h->kept_mat = h->mat_version;
+        return UPPE_OK;
+    }
     // E of q0 at z0 into adj_E[0]: the E left by the previous step's finish when it is current
     if (h->E_valid && h->E_mat == h->mat_version && same_z(h->E_z, z_phase)) {
         h->E = h->adj_E[0];
@@ -1006,6 +1040,9 @@ extern "C" int uppe_adjoint_rk4_step_kept(UppeHandle* h, const void* lam_out, vo
         uppe_set_error(h, "uppe_adjoint_rk4_step_kept: no step kept by uppe_rk4_step_keep for the current material");
         return UPPE_E_ARG;
     }
+    if (h->cfg.cylindrical || !(h->slice_reg || h->slice_big))
+        return reverse_sweep_generic(h, (const float2*)lam_out, (float2*)lam_in, h->kept_z, h->kept_dz, dred_out,
+                                     nullptr);
     return reverse_sweep_fused(h, (const float2*)lam_out, (float2*)lam_in, h->kept_z, h->kept_dz, dred_out);
 }
 

@@ -178,7 +178,7 @@ class DeviceGrid:
 
     def rk4_step_keep(self, z_phase, dz):
         """One fixed RK4 step of the held field that keeps its stage fields for adjoint_step_kept
-        (Cartesian grids; the result equals rk4_step's with dzmin = L - z_sub = dz)."""
+        (the result equals rk4_step's with dzmin = L - z_sub = dz)."""
         self._check(self.lib.uppe_rk4_step_keep(self.h, z_phase, dz))
 
     def adjoint_step_kept(self, lam_out_dev, lam_in_dev, want_dchi3=True):

@@ -167,32 +167,38 @@ def test_vjp_at_benchmark_time_axes(n0):
     dev.close()
 
 
-@pytest.mark.parametrize("shape", [(129, 16, 16), (33, 256, 128)], ids=lambda s: "x".join(map(str, s)))
-def test_kept_step_matches_recompute(shape):
+@pytest.mark.parametrize("case", ["129x16x16", "33x256x128", "cart_series", "cyl_kerr"])
+def test_kept_step_matches_recompute(case):
     """rk4_step_keep + adjoint_step_kept (the stage fields kept by the forward step) against rk4_step
     + adjoint_step (the stage states recomputed): the same step result and the same VJP, on the
-    register-resident (16 x 16) and big-slice (256 x 128) passes, with ionization and the slices
-    above the nonlinear cut.  Bound 1e-6 relative (the same kernels; only the order of launches
+    register-resident (16 x 16) and big-slice (256 x 128) passes with ionization and the slices above
+    the nonlinear cut, on the generic Cartesian slices (8 x 16) and on a cylindrical grid (the
+    tensor-core transforms).  Bound 1e-6 relative (the same kernels; only the order of launches
     differs)."""
     import torch
     from oracle import uppe_oracle as O
     from searay_gb300 import grid, ionization, uppe, workloads
-    vd = workloads.cart_filament_128(steps=400, n_perp=shape[1])
-    vd["wave grid"] = (shape[0], shape[1], shape[2], 2)
-    wave = vd["incoming wave"]
-    vd["incoming wave"] = lambda w, x1, x2: 3.0 * wave(w, x1, x2)
+    if "x" in case:
+        shape = tuple(int(v) for v in case.split("x"))
+        vd = workloads.cart_filament_128(steps=400, n_perp=shape[1])
+        vd["wave grid"] = (shape[0], shape[1], shape[2], 2)
+        wave = vd["incoming wave"]
+        vd["incoming wave"] = lambda w, x1, x2: 3.0 * wave(w, x1, x2)
+    else:
+        vd, _ = replay.load_case(case)
     g = grid.VolumeGrid(vd)
-    dev = uppe.DeviceGrid(g, vd, ionization.RateCoefficients(vd["ionizer"]), "mixed")
+    rates = ionization.RateCoefficients(vd["ionizer"]) if vd.get("ionizer") else None
+    dev = uppe.DeviceGrid(g, vd, rates, "mixed")
     chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
-    mat = uppe.Material(dev, g, "cartesian", None, chi, vd["chi3"], vd["density reference"], vd["window speed"],
-                        vd["density lambda"])
+    mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0), vd["density reference"],
+                        vd.get("window speed", 1.0), vd["density lambda"])
     mat.UpdateMaterial(100.0)
     q0 = O.Oracle(vd).g.kspace(vd["incoming wave"](g.w, g.x1, g.x2))
     rng = np.random.default_rng(5)
     lam = (rng.standard_normal(q0.shape) + 1j * rng.standard_normal(q0.shape)) * (np.abs(q0) + 1e-3 * np.abs(q0).max())
     q0d = torch.from_numpy(q0.astype(np.complex64)).cuda()
     lamd = torch.from_numpy(lam.astype(np.complex64)).cuda()
-    z, dz = 50.0, vd["size"][2] / 400
+    z, dz = 50.0, 1500.0
     dev.set_field(q0d)
     dev.rk4_step(z, dz, 0.0, dz)
     q1 = dev.empty_field()
@@ -208,7 +214,7 @@ def test_kept_step_matches_recompute(shape):
     eq = rel_err(q1k.cpu().numpy(), q1.cpu().numpy())
     eg = rel_err(g_kept.cpu().numpy(), g_rec.cpu().numpy())
     ed = abs(d_kept - d_rec) / abs(d_rec)
-    print(shape, f"step {eq:.1e} vjp {eg:.1e} dchi3 {ed:.1e}")
+    print(case, f"step {eq:.1e} vjp {eg:.1e} dchi3 {ed:.1e}")
     assert eq < 1e-6 and eg < 1e-6 and ed < 1e-6
     # the kept fields belong to one step: a plain step ends them
     dev.rk4_step(z + dz, dz, 0.0, dz)
