@@ -221,3 +221,65 @@ def test_kept_step_matches_recompute(case):
     with pytest.raises(RuntimeError):
         dev.adjoint_step_kept(lamd, g_kept)
     dev.close()
+
+
+def test_legendre_phase_gradient_1025x256():
+    """The gradient of the adjoint workload (config 4): 1025 x 256 cylindrical, the config-1 beam,
+    the on-axis spectral energy in the 700-750 nm band as the loss, 64 Legendre spectral-phase
+    coefficients ~ N(0, 0.1) rad (numpy default_rng(1)) and chi3 as the parameters, checkpoints
+    every 20 steps.  100 steps of 0.5 mm (5 cm: the beam of twice the critical power collapses near
+    8.7 cm, so 200 such steps overflow), in the plain FP32 form.  The FP32 loss carries rounding
+    noise of about 1e-6 of itself, and the loss moves little with any one coefficient (the largest
+    component of the gradient is about 6e-3 of the loss per radian), so the central differences take
+    h = 1e-2 rad (at h = 1e-4 they are noise: they grow as 1/h) on the two coefficients with the
+    largest gradient, and h = 1e-4 of chi3 for chi3; 3e-2 relative.  The gradient of the constant
+    (global-phase) coefficient, which the loss does not depend on, stays below 2e-2 of the largest
+    component (a cancellation over 1025 frequencies in FP32)."""
+    import torch
+    from numpy.polynomial import legendre
+    from searay_gb300 import adjoint, grid, uppe, workloads
+    vd = workloads.cyl_adjoint_256()
+    g = grid.VolumeGrid(vd)
+    dev = uppe.DeviceGrid(g, vd, None, "fp32")
+    chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+    mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd["chi3"], vd["density reference"],
+                        vd["window speed"], vd["density lambda"])
+    mat.UpdateMaterial(0.0)
+    redchi3 = vd["chi3"] / vd["density reference"]
+    dz = vd["size"][2] / vd["subcycles"]
+    nsteps = 100
+    xi = 2 * (g.w - g.w[0]) / (g.w[-1] - g.w[0]) - 1
+    Pl = torch.tensor(legendre.legvander(xi, 63))  # (N0, 64)
+    base = torch.tensor(vd["incoming wave"](g.w, g.x1, g.x2))
+    band = torch.as_tensor((g.w > 0.8 / 0.75) & (g.w < 0.8 / 0.70))
+    c0 = torch.tensor(np.random.default_rng(1).normal(0.0, 0.1, 64))
+
+    def loss(c, chi3):
+        phase = (Pl @ c)[:, None, None]
+        a0 = (base * torch.exp(1j * phase)).to(torch.complex64).cuda()
+        A = adjoint.propagate(dev, a0, chi3, dz, nsteps, checkpoint_every=20)
+        return (A[band, 0, 0].to(torch.complex128).abs() ** 2).sum()
+
+    c = c0.clone().requires_grad_(True)
+    x3 = torch.tensor(redchi3, dtype=torch.float64, requires_grad=True)
+    L = loss(c, x3)
+    L.backward()
+    gc, g3 = c.grad.numpy(), float(x3.grad)
+    top = [int(n) for n in np.argsort(-np.abs(gc[1:]))[:2] + 1]
+    h = 1e-2
+    errs = {}
+    with torch.no_grad():
+        for n in top:
+            e = torch.zeros(64, dtype=torch.float64)
+            e[n] = h
+            fd = (loss(c0 + e, x3.detach()) - loss(c0 - e, x3.detach())).item() / (2 * h)
+            errs[f"c{n}"] = (gc[n], fd)
+        hc = 1e-4 * redchi3
+        fd3 = (loss(c0, torch.tensor(redchi3 + hc)) - loss(c0, torch.tensor(redchi3 - hc))).item() / (2 * hc)
+        errs["chi3"] = (g3, fd3)
+    print(f"L {L.item():.4e}", {k: f"{a:.6e} fd {b:.6e}" for k, (a, b) in errs.items()},
+          f"|g0|/max {abs(gc[0]) / np.abs(gc).max():.1e}")
+    for k, (a, b) in errs.items():
+        assert abs(a - b) < 3e-2 * abs(b), (k, a, b)
+    assert abs(gc[0]) < 2e-2 * np.abs(gc).max()
+    dev.close()
