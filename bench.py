@@ -14,6 +14,10 @@ roofline: the kernel class with the largest share of the step, algorithmic bytes
        average event-timed duration, against the measured HBM copy bandwidth.
 cpu_baseline: the FP64 NumPy oracle (a restatement of the reference path) timed on the host cores
        for one RK4 step of the same grid.
+fwd_adjoint: a forward step that keeps its stage fields plus the vector-Jacobian product of that step
+       (uppe_rk4_step_keep + uppe_adjoint_rk4_step_kept), timed together; "recompute" beside it is a
+       plain forward step plus the VJP that recomputes the stage states.
+kernels: per-class event-timed averages over a replay of the timed steps from the incoming plane.
 --impl reference: the reference arm.  The reference (SeaRay) runs through PyOpenCL, which is not
        available on the GPU machine; its CPU path is timed as the oracle port, one bounded RK4 step
        per bench step.
