@@ -138,3 +138,28 @@ def test_paraxial_grid_checks():
         v["wave grid"] = N
         with pytest.raises(ValueError, match=msg):
             paraxial.track(None, None, None, None, v)
+
+
+def test_bench_byte_model_counts_zero_current_slices():
+    """bench.py's algorithmic bytes of the Cartesian fused evaluation tail: 44 B per point on the
+    slices with current (40 / 48 / 48 / 40 over the RK stages), 32 / 0 / 24 / 0 on the slices at and
+    above the nonlinear cut, whose stages 2 and 4 have nothing to do (65 of 513 slices on the
+    filament grid: 40.2 B per point); the full 44 B when the nonlinear band reaches the top of the
+    frequency band; and the cut index the library computes (int(nl_hi / dw) of the grid)."""
+    import sys
+    import pathlib
+    sys.path.insert(0, str(pathlib.Path(__file__).resolve().parents[1]))
+    import bench
+    from searay_gb300 import workloads
+    vd = workloads.cart_filament_128()
+    g = grid.VolumeGrid(vd)
+    jhi = int(vd["nonlinear band"][1] / g.dw)
+    assert jhi == 448
+    f = (513 - jhi) / 513
+    assert bench.cart_forward_bytes(vd) == pytest.approx((1 - f) * 44 + f * 14)
+    assert bench.cart_forward_bytes(vd) == pytest.approx(40.2, abs=0.05)
+    full = dict(vd)
+    full["nonlinear band"] = vd["frequency band"]
+    assert bench.cart_forward_bytes(full) == pytest.approx(44.0)
+    m = bench.class_models(vd)
+    assert m["time_pass"]["bytes"] == 16 * 513 * 128 * 128
