@@ -249,6 +249,14 @@ cudaError_t launch_spec_cyl(UppeHandle* h, int mode, const float2* src_real, flo
     g.Ce = Ce;
     g.spec_mode = mode;
     if (mode == SPEC_LOAD) return run_gemm<A_PLAIN, C_STORE>(h, g);
+    if (h->cfg.precision == UPPE_PREC_MIXED && g.A == h->J) {
+        // the tensor-core transform stores its product over J (its pre-pass has already read J into
+        // the operand tiles), then a separate pass applies S and the RK stage
+        g.C0 = h->J;
+        cudaError_t err = run_gemm<A_PLAIN, C_STORE>(h, g);
+        if (err != cudaSuccess) return err;
+        return launch_spec_point(h, mode, h->J, q_out, qf_io, qi, Cs, Ce, z);
+    }
     return run_gemm<A_PLAIN, C_SPEC>(h, g);
 }
 

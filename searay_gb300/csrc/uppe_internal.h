@@ -157,6 +157,8 @@ cudaError_t launch_spec_reg(UppeHandle* h, int mode, const float2* src, float2* 
 cudaError_t launch_adj_reg(UppeHandle* h, int mode, const float2* in, float2* out, StepArgs z);
 cudaError_t launch_adj_fused_reg(UppeHandle* h, int mode, const float2* g, float2* out, float a_f, float a_mu,
                                  StepArgs z_e, StepArgs z_s);
+cudaError_t launch_spec_point(UppeHandle* h, int mode, const float2* C, float2* q_out, float2* qf, const float2* qi,
+                              float Cs, float Ce, StepArgs z);
 cudaError_t launch_adj_fused_big(UppeHandle* h, int mode, const float2* g, float2* out, float a_f, float a_mu,
                                  StepArgs z_e, StepArgs z_s);
 

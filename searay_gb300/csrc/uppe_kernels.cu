@@ -390,6 +390,30 @@ __global__ void k_adj_rk(int mode, const float2* __restrict__ lam_out, float2* _
     }
 }
 
+// The spectral update of every point from the transformed current C (the ODE right-hand side and the
+// RK stage of spec_update), as a separate pass after a tensor-core transform that stored C: many
+// warps per multiprocessor hide the latency of its operand reads, which the GEMM's own epilogue,
+// with one block per multiprocessor, does not.
+__global__ void k_spec_point(int mode, const float2* __restrict__ C, OpView opv, float2* __restrict__ q_out,
+                             float2* __restrict__ qf, const float2* __restrict__ qi, float Cs, float Ce, StepArgs z,
+                             size_t n, int S) {
+    const PhaseArgs pa{z.zhi, z.zlo, z.plain};
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
+        const int w = (int)(idx / (size_t)S);
+        const float cond = (w < opv.ncond) ? 0.f : 1.f;
+        const OpPoint o = op_at(opv, idx, opv.kg[w]);
+        spec_update(mode, idx, C[idx], o, cond, q_out, qf, qi, Cs, Ce, pa, true);
+    }
+}
+
+cudaError_t launch_spec_point(UppeHandle* h, int mode, const float2* C, float2* q_out, float2* qf, const float2* qi,
+                              float Cs, float Ce, StepArgs z) {
+    h->launches++;
+    k_spec_point<<<reduce_blocks_host(h->P), 256, 0, h->stream>>>(mode, C, uppe_op_view(h), q_out, qf, qi, Cs, Ce, z,
+                                                                   h->P, h->S);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_adj_rk(UppeHandle* h, int mode, const float2* lam_out, float2* lam_in, float a_f, float a_mu) {
     h->launches++;
     k_adj_rk<<<reduce_blocks_host(h->P), 256, 0, h->stream>>>(mode, lam_out, h->adj_lf, h->adj_acc, h->adj_lk,
