@@ -163,3 +163,26 @@ def test_bench_byte_model_counts_zero_current_slices():
     assert bench.cart_forward_bytes(full) == pytest.approx(44.0)
     m = bench.class_models(vd)
     assert m["time_pass"]["bytes"] == 16 * 513 * 128 * 128
+
+
+@pytest.mark.parametrize("propagator,case", [("uppe", "cart_ion"), ("paraxial", replay.PARAXIAL_CASE_NAMES[0])])
+def test_report_writes_reference_wave_files(tmp_path, capsys, propagator, case):
+    """The wave-data files of a volume's report: names, contents and dtypes as modules/volume.py:626-641
+    writes them from track's five returns."""
+    from searay_gb300 import report
+    _, exp = replay.load_case(case)
+    outputs = tuple(exp[k] for k in ("A", "J", "chi", "ne", "dom4d"))
+    base = str(tmp_path / "run")
+    paths = report.write_wave_data(base, "vol0", outputs, propagator)
+    label = "UPPE" if propagator == "uppe" else "paraxial"
+    assert f"Write {label} wave data..." in capsys.readouterr().out
+    assert [p.rsplit("/", 1)[1] for p in paths] == [
+        f"run_vol0_{propagator}_{f}.npy" for f in ("wave", "j", "chi", "plasma", "plot_ext")]
+    for p, a in zip(paths, outputs):
+        b = np.load(p)
+        assert b.dtype == a.dtype and b.shape == a.shape
+        np.testing.assert_array_equal(b, a)
+    with pytest.raises(ValueError):
+        report.wave_data_paths(base, "vol0", "eikonal")
+    with pytest.raises(ValueError):
+        report.write_wave_data(base, "vol0", outputs[:4], propagator)
