@@ -787,12 +787,15 @@ static int ensure_adjoint(UppeHandle* h) {
         return UPPE_E_ARG;
     }
     if (h->adj_mu) return UPPE_OK;
+    // Only buffers still missing are allocated, so a call after a failed allocation neither leaks
+    // nor reallocates; adj_mu, the "allocated" mark, comes last, after the scalar dred_d.
+    if (!h->dred_d) CUDA_TRY(h, cudaMalloc((void**)&h->dred_d, sizeof(double)));
     const size_t fb = h->P * sizeof(float2);
     float2** bufs[] = {&h->adj_q1, &h->adj_q2, &h->adj_q3,   &h->adj_lf,   &h->adj_acc,
                        &h->adj_lk, &h->adj_E[0], &h->adj_E[1], &h->adj_E[2], &h->adj_E[3],
-                       &h->adj_mu};  // adj_mu last: the "allocated" mark
-    for (float2** b : bufs) CUDA_TRY(h, cudaMalloc((void**)b, fb));
-    CUDA_TRY(h, cudaMalloc((void**)&h->dred_d, sizeof(double)));
+                       &h->adj_mu};
+    for (float2** b : bufs)
+        if (!*b) CUDA_TRY(h, cudaMalloc((void**)b, fb));
     return UPPE_OK;
 }
 
