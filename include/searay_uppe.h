@@ -71,7 +71,10 @@ typedef struct UppeHandle UppeHandle;
 
 /* Allocate a propagator for one grid.  Replaces the buffer set-up of Source.__init__
  * (uppe_kernel.py:95-129), Material.__init__ (:35-66) and TransverseModeTool.AllocateDeviceMemory
- * (grid_tools.py:299-303). */
+ * (grid_tools.py:299-303).  The whole configuration is checked on the host before any CUDA call
+ * (UPPE_E_ARG, with the reference's ValueError wording for grids, uppe_kernel.py:354-360); then
+ * UPPE_E_NOMEM when device memory runs out, UPPE_E_CUDA for any other CUDA failure (no device, no
+ * driver).  *out is NULL on every error; uppe_last_error(NULL) holds the message. */
 int uppe_create(const UppeConfig* cfg, UppeHandle** out);
 
 /* Release a handle and its device buffers (grid_tools.py:304-307). */

@@ -259,7 +259,7 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
         uppe_set_error(nullptr, "device allocation failed: %s", cudaGetErrorString(e));
         free_buffers(h);
         delete h;
-        return UPPE_E_NOMEM;
+        return (e == cudaErrorMemoryAllocation) ? UPPE_E_NOMEM : UPPE_E_CUDA;  // no device, no driver, ...
     }
     // twiddle table tw[j] = exp(-2 pi i j / NT), computed in FP64
     const int NT = 1 << h->twLog;
@@ -1051,7 +1051,10 @@ extern "C" int uppe_adjoint_rk4_step_kept(UppeHandle* h, const void* lam_out, vo
 
 extern "C" int uppe_adjoint_load(UppeHandle* h, const void* lam_q, void* lam_a) {
     if (!h || !lam_q || !lam_a) return UPPE_E_ARG;
-    if (!h->have_grid) return UPPE_E_ARG;
+    if (!h->have_grid) {
+        uppe_set_error(h, "uppe_adjoint_load before uppe_set_grid");
+        return UPPE_E_ARG;
+    }
     int rc = ensure_adjoint(h);
     if (rc) return rc;
     CUDA_TRY(h, adj_pass(h, ADJ_LOAD, (const float2*)lam_q, (float2*)lam_a, split_z(h, 0.0)));
