@@ -229,7 +229,9 @@ cudaError_t launch_real_cyl(UppeHandle* h, int mode, const float2* src, float2* 
     return launch_ikz(h, A, h->E);
 }
 
-// Forward transform of J (or of the incoming field for SPEC_LOAD) with the spectral update fused.
+// Forward transform of J (or of the incoming field for SPEC_LOAD) and the spectral update: fused
+// into the GEMM's epilogue in the SIMT form and on azimuthal grids (N2 > 1, the operand is the
+// azimuthal DFT in scratch); a separate elementwise pass after the tensor-core GEMM otherwise.
 cudaError_t launch_spec_cyl(UppeHandle* h, int mode, const float2* src_real, float2* q_out, float2* qf_io,
                             const float2* qi, float Cs, float Ce, StepArgs z) {
     GemmArgs g = base_args(h, z);
