@@ -351,6 +351,8 @@ def oracle_step_time(vd, n_perp=None):
         f = n_perp / N[1]
         v["wave grid"] = (N[0], n_perp, n_perp if N[2] > 1 else 1, N[3])
         v["size"] = (v["size"][0] * f, v["size"][1] * (f if N[2] > 1 else 1), v["size"][2])
+        if v.get("radial modes") is not None:  # keep the same fraction of the radial nodes
+            v["radial modes"] = max(1, min(n_perp, int(round(v["radial modes"] * f))))
     env = is_paraxial(v)
     orc = PO.ParaxialOracle(v) if env else O.Oracle(v)
     g = orc.g
@@ -380,7 +382,10 @@ def reference_arm(args, vd, ws, rank):
     # size the per-step sample so the whole run stays within a few minutes
     budget = 150.0
     chosen = None
-    for n in (128, 64, 32, 16, 8):
+    # the full transverse grid where it has at most 128 points per axis, else sub-grids of it
+    n_full = vd["wave grid"][1]
+    sizes = ([n_full] if n_full <= 128 else []) + [n for n in (128, 64, 32, 16, 8) if n < n_full]
+    for n in sizes:
         t, P, N = oracle_step_time(vd, n)
         chosen = (n, t, P, N)
         if t * (args.steps + args.warmup) <= budget:

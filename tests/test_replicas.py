@@ -62,3 +62,36 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch, capsys):
         steps, warmup, workload = 2, 3, "cart_filament_128"
     bench.reference_arm(Args(), {}, 2, 1)
     assert calls == [] and capsys.readouterr().out == ""
+
+
+def test_reference_arm_line_keeps_the_bench_contract(capsys):
+    """The reference arm's JSON line on rank 0: the bench keys, a cpu_baseline describing the run, an
+    e2e with no host-device bytes, and a sample no larger than the workload's grid."""
+    sys.path.insert(0, ROOT)
+    import json
+    import bench
+    from searay_gb300 import workloads
+
+    class Args:
+        steps, warmup, workload = 3, 3, "cyl_kerr_64"
+    vd = workloads.WORKLOADS[Args.workload]()
+    bench.reference_arm(Args(), vd, 1, 0)
+    d = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for k in ("impl", "metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert k in d, k
+    assert d["impl"] == "reference" and d["steps"] == 3 and d["warmup"] == 3 and d["value"] > 0
+    assert d["config"]["workload"] == "cyl_kerr_64"
+    assert d["config"]["sample_grid"] == d["config"]["grid"] == [257, 64, 1]
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["unit"] == d["unit"]
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_reference_sample_scales_radial_modes():
+    """A cylindrical sample below the workload's radial size keeps the same fraction of radial modes."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from searay_gb300 import workloads
+    t, P, N = bench.oracle_step_time(workloads.WORKLOADS["cyl_silica_512"](), 16)
+    assert tuple(N[:3]) == (2049, 16, 1) and P == 2049 * 16 and t > 0
