@@ -95,3 +95,14 @@ def test_reference_sample_scales_radial_modes():
     from searay_gb300 import workloads
     t, P, N = bench.oracle_step_time(workloads.WORKLOADS["cyl_silica_512"](), 16)
     assert tuple(N[:3]) == (2049, 16, 1) and P == 2049 * 16 and t > 0
+
+
+def test_cpu_baseline_repeats_steps_to_its_time():
+    """The cpu_baseline leg repeats the oracle step until its time is reached and says so."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from searay_gb300 import workloads
+    cb = bench.cpu_baseline(workloads.WORKLOADS["cyl_kerr_64"](), min_seconds=0.5, max_steps=50)
+    assert cb["kind"] == "port" and cb["value"] > 0 and cb["unit"] == bench.UNIT
+    steps = int(cb["sample"].split()[0])
+    assert 1 < steps <= 50 and "on the full 257x64x1 grid" in cb["sample"]
