@@ -186,3 +186,18 @@ def test_report_writes_reference_wave_files(tmp_path, capsys, propagator, case):
         report.wave_data_paths(base, "vol0", "eikonal")
     with pytest.raises(ValueError):
         report.write_wave_data(base, "vol0", outputs[:4], propagator)
+
+
+def test_product_code_never_reaches_the_oracle():
+    """The package (Python host, CUDA sources, C header) imports, loads or names neither the oracle
+    nor scratch files: the oracle is test infrastructure and the product has no CPU fallback."""
+    import pathlib
+    import re
+    root = pathlib.Path(__file__).resolve().parent.parent
+    files = [p for p in (root / "searay_gb300").rglob("*") if p.suffix in (".py", ".cu", ".cuh", ".h")]
+    files += list((root / "include").glob("*.h"))
+    assert len(files) > 10
+    pat = re.compile(r"\boracle\b|\b_work\b|refshim")
+    hits = [f"{p.relative_to(root)}:{i + 1}" for p in files
+            for i, line in enumerate(p.read_text().splitlines()) if pat.search(line)]
+    assert hits == []
