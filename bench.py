@@ -1,11 +1,12 @@
-"""Benchmark of the GB300 UPPE z-step: grid-pt*steps/s on the Cartesian filament workload.
+"""Benchmark of the GB300 UPPE z-step: grid-pt*steps/s on the large Cartesian filament workload.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload cart_filament_128] [--precision mixed|fp32]
+                    [--workload cart_filament_256] [--precision mixed|fp32]
 
 A "step" is one classic RK4 z-step (four right-hand-side evaluations) over the whole grid.
-The default workload is the Cartesian 128 x 128 x 513 filament (Kerr + O2 tunneling ionization +
-plasma current, 400 fixed steps over 10 cm; searay_gb300/workloads.py).
+The default workload is the 1025 x 256 x 256 filament (256 x 256 over 3 mm, 800 nm 40 fs pulse at
+10 critical powers, Kerr + O2 tunneling ionization + plasma current, 1000 fixed steps over 10 cm;
+searay_gb300/workloads.py), the largest workload that fits one GPU.
 
 value: P * K / (device time of K steps), fields resident in HBM, CUDA events on the library's stream.
 e2e:   the same metric through the reference-facing call searay_gb300.track() with host (NumPy)
@@ -18,6 +19,13 @@ cpu_baseline: the FP64 NumPy oracle (a restatement of the reference path) timed 
 fwd_adjoint: a forward step that keeps its stage fields plus the vector-Jacobian product of that step
        (uppe_rk4_step_keep + uppe_adjoint_rk4_step_kept), timed together; "recompute" beside it is a
        plain forward step plus the VJP that recomputes the stage states.
+fp32:  the same forward and forward+adjoint rates in the plain FP32 form (FP32 phase and density
+       sum, SIMT Hankel transforms on cylindrical grids) beside the mixed form of the main line.
+err_vs_fp64: both forms' first RK4 step (with the finish: A, J, chi, n_e) against the FP64 oracle's
+       on the grid the cpu_baseline leg times (the full grid, or its 128 x 128 sub-grid for larger
+       Cartesian slices): max |x - x_ref| / max |x_ref| of the field, its fluence (sum over w of
+       |A|^2 per transverse point), its spectrum (sum over the transverse points of |A|^2 per w),
+       J, chi and n_e.
 kernels: per-class event-timed averages over a replay of the timed steps from the incoming plane.
 --impl reference: the reference arm.  The reference (SeaRay) runs through PyOpenCL, which is not
        available on the GPU machine; its CPU path is timed as the oracle port, one bounded RK4 step
@@ -191,9 +199,9 @@ def build_device(vd, precision):
     return g, dev, mat
 
 
-def run_device(args, vd, ws, rank, local):
+def run_device(args, vd, ws, rank, local, precision, per_class=True):
     import torch
-    g, dev, mat = build_device(vd, args.precision)
+    g, dev, mat = build_device(vd, precision)
     P = int(np.prod(g.N[:3]))
     Lz = vd["size"][2]
     nsteps_cfg = vd["subcycles"]
@@ -282,18 +290,20 @@ def run_device(args, vd, ws, rank, local):
         adj = (adj_ms, pair_ms)
     # per-kernel-class timing: the timed steps again from the incoming plane (separate region; event
     # records between launches), so that the per-class averages describe the same work
-    dev.load_field(a_dev)
-    step[0] = 0
-    dev.profile(True)
-    for _ in range(args.steps):
-        one_step()
-    prof = dev.profile_read()
-    dev.profile(False)
+    prof = None
+    if per_class:
+        dev.load_field(a_dev)
+        step[0] = 0
+        dev.profile(True)
+        for _ in range(args.steps):
+            one_step()
+        prof = dev.profile_read()
+        dev.profile(False)
     dev.close()
     return P, ms, launches, clk, prof, finite, adj
 
 
-def run_e2e(args, vd):
+def run_e2e(args, vd, precision):
     """K steps through track() with host input/outputs (one diagnostic interval)."""
     import torch
     from searay_gb300 import paraxial, uppe
@@ -304,7 +314,7 @@ def run_e2e(args, vd):
     v["size"] = (vd["size"][0], vd["size"][1], dz * args.steps)
     v["subcycles"] = args.steps
     v["minimum step"] = dz
-    v["precision"] = args.precision
+    v["precision"] = precision
     warm = dict(v)
     warm["size"] = (vd["size"][0], vd["size"][1], dz * 2)
     warm["subcycles"] = 2
@@ -343,18 +353,12 @@ def cpu_cores():
 
 def oracle_step_time(vd, n_perp=None):
     """Seconds for one FP64 oracle RK4 step (four RHS evaluations + stage arithmetic)."""
-    t, _, P, N = oracle_run(vd, n_perp)
+    t, _, P, N, _ = oracle_run(sample_volume(vd, n_perp))
     return t, P, N
 
 
-def oracle_run(vd, n_perp=None, min_seconds=0.0, max_steps=1):
-    """The FP64 oracle's first RK4 step from the incoming plane, repeated until ``min_seconds`` of step
-    time or ``max_steps`` steps; returns (seconds, steps, points, grid).  Set-up is not timed.  Every
-    repeat starts again from the incoming plane, so each does the same work and stays finite (a
-    collapsing beam overflows after some tens of steps)."""
-    from oracle import paraxial_oracle as PO
-    from oracle import uppe_oracle as O
-    O.set_workers(cpu_cores())
+def sample_volume(vd, n_perp=None):
+    """The volume itself, or its n_perp x n_perp (n_perp radial nodes) sub-grid with the box scaled."""
     v = dict(vd)
     if n_perp is not None and n_perp != v["wave grid"][1]:
         N = v["wave grid"]
@@ -363,15 +367,28 @@ def oracle_run(vd, n_perp=None, min_seconds=0.0, max_steps=1):
         v["size"] = (v["size"][0] * f, v["size"][1] * (f if N[2] > 1 else 1), v["size"][2])
         if v.get("radial modes") is not None:  # keep the same fraction of the radial nodes
             v["radial modes"] = max(1, min(n_perp, int(round(v["radial modes"] * f))))
+    return v
+
+
+def oracle_run(v, min_seconds=0.0, max_steps=1, outputs=False):
+    """The FP64 oracle's first RK4 step from the incoming plane on the volume ``v``, repeated until
+    ``min_seconds`` of step time or ``max_steps`` steps; returns (seconds, steps, points, grid,
+    outputs).  Set-up is not timed.  Every repeat starts again from the incoming plane, so each does
+    the same work and stays finite (a collapsing beam overflows after some tens of steps).  With
+    ``outputs`` the first step's finish (A, J, chi, n_e, as the oracle's propagator returns them for
+    one fixed step) is computed after the timed work; otherwise ``outputs`` is None."""
+    from oracle import paraxial_oracle as PO
+    from oracle import uppe_oracle as O
+    O.set_workers(cpu_cores())
     env = is_paraxial(v)
     orc = PO.ParaxialOracle(v) if env else O.Oracle(v)
     g = orc.g
-    orc.mat.update(0.0)
-    a = vd["incoming wave"](g.w, g.x1, g.x2)
+    dz = v["size"][2] / v["subcycles"]
+    orc.mat.update(0.5 * dz)  # the medium at the middle of the first subcycle, as the propagator samples it
+    a = v["incoming wave"](g.w, g.x1, g.x2)
     q = g.kspace(np.fft.ifftshift(a, axes=0) if env else a)
     cond = 1.0 if env else orc.conditioner[:, None, None]
-    dz = v["size"][2] / v["subcycles"]
-    tot, steps = 0.0, 0
+    tot, steps, q1 = 0.0, 0, None
     while steps < max(1, max_steps) and (steps == 0 or tot < min_seconds):
         t = time.perf_counter()
         k1 = orc.load_source(q, 0.0)
@@ -384,24 +401,81 @@ def oracle_run(vd, n_perp=None, min_seconds=0.0, max_steps=1):
         qf = qf + dz / 3 * k3
         qw = (q + dz * k3) * cond
         k4 = orc.load_source(qw, dz)
-        _ = (qf + dz / 6 * k4) * cond  # the step's result: computed for its time only
+        q = (qf + dz / 6 * k4) * cond  # the step's result
         tot += time.perf_counter() - t
         steps += 1
-    return tot, steps, int(np.prod(g.N[:3])), g.N
+        if q1 is None:
+            q1 = q
+    out = None
+    if outputs:
+        out = orc.finish(q1, dz)
+    return tot, steps, int(np.prod(g.N[:3])), g.N, out
 
 
-def cpu_baseline(vd, min_seconds=10.0, max_steps=200):
-    """The FP64 oracle's rate on a bounded sample of the workload: RK4 steps on the full grid, or on
-    its 128 x 128 sub-grid (same physics, box scaled) for larger Cartesian slices, repeated until
-    about ``min_seconds`` of CPU work."""
+def cpu_sample(vd):
+    """The volume the CPU baseline times: the full grid, or its 128 x 128 sub-grid (same physics, box
+    scaled) for larger Cartesian slices."""
     N = vd["wave grid"]
     n_perp = 128 if N[1] * N[2] > 128 * 128 and N[2] > 1 else None
-    t, steps, P, Ns = oracle_run(vd, n_perp, min_seconds, max_steps)
+    return sample_volume(vd, n_perp), n_perp is None
+
+
+def cpu_baseline(vd, min_seconds=10.0, max_steps=200, outputs=False):
+    """The FP64 oracle's rate on a bounded sample of the workload (cpu_sample), repeated until about
+    ``min_seconds`` of CPU work.  Returns (baseline entry, sample volume, first-step outputs)."""
+    N = vd["wave grid"]
+    v, full = cpu_sample(vd)
+    t, steps, P, Ns, out = oracle_run(v, min_seconds, max_steps, outputs)
     grid = f"{Ns[0]}x{Ns[1]}x{Ns[2]}"
-    where = (f"the full {grid} grid" if n_perp is None else
+    where = (f"the full {grid} grid" if full else
              f"a {grid} sub-grid (box scaled) of the {N[0]}x{N[1]}x{N[2]} grid")
-    return {"value": P * steps / t, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
-            "sample": f"{steps} FP64 oracle RK4 step(s) on {where} ({t:.1f} s)"}
+    return ({"value": P * steps / t, "unit": UNIT, "cores": cpu_cores(), "kind": "port",
+             "sample": f"{steps} FP64 oracle RK4 step(s) on {where} ({t:.1f} s)"}, v, out)
+
+
+def field_metrics(A, J, chi, ne, ref):
+    """Errors of one step's outputs against the oracle's: max |x - x_ref| / max |x_ref| of A, J, chi,
+    n_e, and of the fluence (sum over w of |A|^2) and the spectrum (sum over x, y of |A|^2)."""
+    def rel(x, r):
+        s = np.max(np.abs(r))
+        return float(np.max(np.abs(x - r)) / s) if s > 0 else float(np.max(np.abs(x)))
+
+    def power(x):
+        return x.real.astype(np.float64) ** 2 + x.imag.astype(np.float64) ** 2
+
+    A_ref, J_ref, chi_ref, ne_ref = ref
+    pA, pR = power(A), power(A_ref)
+    return {"field": rel(A, A_ref), "fluence": rel(pA.sum(axis=0), pR.sum(axis=0)),
+            "spectrum": rel(pA.sum(axis=(1, 2)), pR.sum(axis=(1, 2))), "J": rel(J, J_ref),
+            "chi": rel(chi, chi_ref), "ne": rel(ne, ne_ref)}
+
+
+def gpu_first_step_errors(v, ref, precision):
+    """One fixed RK4 step with the finish on the device, on the sample volume v, against ref."""
+    import torch
+    from searay_gb300 import paraxial, uppe
+    g, dev, mat = build_device(v, precision)
+    try:
+        dz = v["size"][2] / v["subcycles"]
+        a = v["incoming wave"](g.w, g.x1, g.x2)
+        if is_paraxial(v):
+            a_dev = torch.from_numpy(np.ascontiguousarray(np.fft.ifftshift(a, axes=0), dtype=np.complex64)).cuda()
+            out = paraxial.propagator(dev, mat, a_dev, 1, 0.0, dz)[:4]
+            host = [np.fft.fftshift(t.cpu().numpy(), axes=0) for t in out]
+        else:
+            a_dev = torch.from_numpy(np.ascontiguousarray(a, dtype=np.complex64)).cuda()
+            out = uppe.propagator(dev, mat, a_dev, 1, 0.0, dz, dz)[:4]
+            host = [t.cpu().numpy() for t in out]
+    finally:
+        dev.close()
+    return field_metrics(*host, ref)
+
+
+def config_of(args, vd, ws):
+    """The workload description shared by both arms' lines."""
+    return {"workload": args.workload, "grid": list(vd["wave grid"][:3]), "propagator": vd.get("propagator", "uppe"),
+            "parallelism": "replicas" if ws > 1 else "single",
+            "l2": f"working set ({working_set_mb(vd):.0f} MB of fields and operator) vs the 129 MB L2"}
 
 
 def reference_arm(args, vd, ws, rank):
@@ -427,12 +501,15 @@ def reference_arm(args, vd, ws, rank):
         tot += t
     value = P * args.steps / tot
     cores = cpu_cores()
-    sample = f"one FP64 RK4 step per bench step on a {N[0]}x{N[1]}x{N[2]} sub-grid of the workload (same physics, box scaled)"
+    full = list(N[:3]) == list(vd["wave grid"][:3])
+    sample = (f"one FP64 RK4 step per bench step on the full {N[0]}x{N[1]}x{N[2]} grid" if full else
+              f"one FP64 RK4 step per bench step on a {N[0]}x{N[1]}x{N[2]} sub-grid of the workload "
+              "(same physics, box scaled)")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": args.workload, "grid": list(vd["wave grid"][:3]), "sample_grid": list(N[:3])},
+        "config": config_of(args, vd, ws), "sample_grid": list(N[:3]),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "SeaRay's UPPE path needs PyOpenCL + an OpenCL runtime, absent on the GPU machine; its CPU path is "
@@ -441,16 +518,32 @@ def reference_arm(args, vd, ws, rank):
     print(json.dumps(line))
 
 
+def fwd_adjoint_entry(P, ws, fwd_ms, adj):
+    """The forward+adjoint rate: the kept-stage pair where it ran, else forward + recomputing VJP."""
+    adj_ms, pair_ms = adj
+    recompute = {"value": P * ws / ((fwd_ms + adj_ms) / 1e3), "unit": UNIT, "adjoint_ms_per_step": adj_ms,
+                 "forward_ms_per_step": fwd_ms,
+                 "note": "one forward step plus one vector-Jacobian product of the step; the VJP "
+                         "recomputes the step's stage states (checkpointed backward pass)"}
+    if pair_ms is None:
+        return recompute
+    return {"value": P * ws / (pair_ms / 1e3), "unit": UNIT, "ms_per_step": pair_ms,
+            "note": "one forward step that keeps its stage fields (rk4_step_keep) and the "
+                    "vector-Jacobian product of that step from them (adjoint_step_kept), timed together",
+            "recompute": recompute}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="cart_filament_128")
+    ap.add_argument("--workload", default="cart_filament_256")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-fp32", action="store_true", help="skip the plain FP32 companion rates")
     ap.add_argument("--adjoint-steps", type=int, default=20,
                     help="adjoint (VJP) steps timed for the forward+adjoint rate; 0 to skip")
     args = ap.parse_args()
@@ -468,7 +561,7 @@ def main():
         torch.distributed.init_process_group("nccl")
     else:
         torch.cuda.set_device(0)
-    P, ms, launches, clk, prof, finite, adj_ms = run_device(args, vd, ws, rank, local)
+    P, ms, launches, clk, prof, finite, adj = run_device(args, vd, ws, rank, local, args.precision)
     value, ms = aggregate_replicas(ms, P, args.steps, ws, "cuda")
     peak, tpeak, peak_kind = measured_peaks()
     models = class_models(vd)
@@ -504,48 +597,56 @@ def main():
                                          "fp32_frac": flops / sec / 1e12 / fp32_peak,
                                          "note": "FP32 peak from the SM count and the median SM clock under load"}
     dom = max((k for k in kernels if k in models), key=lambda k: kernels[k]["total_ms"])
-    traffic = ncu_traffic(args.workload).get(dom)
+    traffic_rec = ncu_traffic(args.workload)
+    traffic = traffic_rec.get(dom)
+    traffic_source = (f"profiles/traffic_{args.workload}.json: {traffic_rec.get('source', 'ncu capture')}"
+                      if traffic is not None else None)
     share = kernels[dom]["total_ms"] / sum(v["total_ms"] for v in kernels.values())
     if tensor_path and "achieved_TFLOPs" in kernels[dom]:
         roof = {"bound": "tensor", "kernel": dom, "achieved": kernels[dom]["achieved_TFLOPs"], "peak": tpeak,
-                "unit": "TFLOP/s", "frac": kernels[dom]["tensor_frac"], "traffic": traffic, "peak_source": peak_kind,
-                "share": share, "hbm_frac": kernels[dom]["frac"],
+                "unit": "TFLOP/s", "frac": kernels[dom]["tensor_frac"], "traffic": traffic,
+                "traffic_source": traffic_source, "peak_source": peak_kind, "share": share,
+                "hbm_frac": kernels[dom]["frac"],
                 "note": "algorithmic flops; the split-BF16x3 tensor path executes 3x as many"}
     else:
         roof = {"bound": "hbm", "kernel": dom, "achieved": kernels[dom]["achieved_GBs"], "peak": peak, "unit": "GB/s",
-                "frac": kernels[dom]["frac"], "traffic": traffic, "peak_source": peak_kind, "share": share}
+                "frac": kernels[dom]["frac"], "traffic": traffic, "traffic_source": traffic_source,
+                "peak_source": peak_kind, "share": share}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 (float-float phase and density scan)" if args.precision == "mixed" else "f32",
-        "data": "synthetic",
-        "config": {"workload": args.workload, "grid": list(vd["wave grid"][:3]),
-                   "propagator": vd.get("propagator", "uppe"),
-                   "precision": args.precision, "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": f"working set ({working_set_mb(vd):.0f} MB of fields and operator) vs the 129 MB L2"},
+        "data": "synthetic", "precision": args.precision,
+        "config": config_of(args, vd, ws),
         "roofline": roof, "kernels": kernels, "gpu_launches": launches, "clocks": clk, "finite": finite,
     }
-    if adj_ms is not None:
-        adj_ms, pair_ms = adj_ms
-        fwd_ms = ms / args.steps
-        recompute = {"value": P * ws / ((fwd_ms + adj_ms) / 1e3), "unit": UNIT, "adjoint_ms_per_step": adj_ms,
-                     "forward_ms_per_step": fwd_ms,
-                     "note": "one forward step plus one vector-Jacobian product of the step; the VJP "
-                             "recomputes the step's stage states (checkpointed backward pass)"}
-        if pair_ms is None:
-            line["fwd_adjoint"] = recompute
-        else:
-            line["fwd_adjoint"] = {"value": P * ws / (pair_ms / 1e3), "unit": UNIT, "ms_per_step": pair_ms,
-                                   "note": "one forward step that keeps its stage fields (rk4_step_keep) and the "
-                                           "vector-Jacobian product of that step from them (adjoint_step_kept), "
-                                           "timed together",
-                                   "recompute": recompute}
+    if adj is not None:
+        line["fwd_adjoint"] = fwd_adjoint_entry(P, ws, ms / args.steps, adj)
+    other = "fp32" if args.precision == "mixed" else "mixed"
+    if not args.no_fp32:
+        # the other precision form on the same workload: forward and forward+adjoint rates
+        P2, ms2, _, _, _, finite2, adj2 = run_device(args, vd, ws, rank, local, other, per_class=False)
+        value2, ms2 = aggregate_replicas(ms2, P2, args.steps, ws, "cuda")
+        comp = {"value": value2, "unit": UNIT, "ms_per_step": ms2 / args.steps, "finite": finite2,
+                "mixed_over_fp32": value / value2 if other == "fp32" else value2 / value}
+        if adj2 is not None:
+            comp["fwd_adjoint"] = fwd_adjoint_entry(P2, ws, ms2 / args.steps, adj2)
+        line[other] = comp
     if rank == 0 and not args.no_e2e:
-        e2e, h2d, d2h, ok = run_e2e(args, vd)
+        e2e, h2d, d2h, ok = run_e2e(args, vd, args.precision)
         line["e2e"] = {"value": e2e * ws, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
                        "d2h_bytes_per_step": d2h / args.steps, "call": "searay_gb300.track (host NumPy in/out)"}
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
-        line["cpu_baseline"] = cpu_baseline(vd)
+        base, v_sample, ref = cpu_baseline(vd, outputs=True)
+        line["cpu_baseline"] = base
+        # both forms' first step on the sampled grid against the oracle's (set-up outside any timing)
+        errs = {p: gpu_first_step_errors(v_sample, ref, p) for p in ("mixed", "fp32")}
+        line["err_vs_fp64"] = {"grid": list(v_sample["wave grid"][:3]), "steps": 1, **errs,
+                               "metric": "max |x - x_ref| / max |x_ref| after one fixed RK4 step and the finish; "
+                                         "fluence = sum over w of |A|^2, spectrum = sum over x, y of |A|^2",
+                               "bounds": {"fp32 transforms": 1e-5, "tensor-core transforms": 1e-4}}
+        if other in line:
+            line[other]["err_vs_fp64"] = errs[other]
     if rank == 0:
         print(json.dumps(line))
     if ws > 1:

@@ -206,11 +206,20 @@ const char* uppe_class_name(int cls);
  * amin^2) - min(Re(S q*)/(|q|^2 + amin^2), 0)  (paraxial.cl:40-58, uppe_kernel.py:217-223).  The
  * caller applies the dzmin and end-of-subcycle clamps.
  *
- * Its reduction scratch is one fixed array in device memory, about 128 KB, held by every GPU
- * that loads this library until the process exits.  Limits and rules:
+ * If q or S holds a non-finite value, *dz_out is NaN.
+ *
+ * Its reduction scratch is one fixed array in device memory, about 128 KB.  Limits and rules:
  *   - n may not exceed UPPE_NOALLOC_MAX_POINTS; larger grids get UPPE_E_RANGE and a message.
- *   - The first call on each device looks up the array's device address with that device
- *     current.  Make that first call before any CUDA stream capture.
+ *   - The first call on each device, made with that device current, loads this entry point's
+ *     CUDA module onto the device (the runtime loads modules lazily by default), looks up the
+ *     array's device address and loads its kernels.  That first call is the only one that may
+ *     allocate device memory (the array and the kernels' code).  Make it before the caller's
+ *     no-allocation phase begins (for example before reserving all remaining device memory) and
+ *     before any CUDA stream capture.  From then on the array stays on that device until the
+ *     process exits.
+ *   - Only the device's primary context (the one the CUDA runtime API uses) is supported, and the
+ *     entry point must not be used across a cudaDeviceReset: the address looked up in the first
+ *     call is kept for the life of the process.
  *   - All calls share the one array, which keeps the contents of the last call.  Calls whose work
  *     overlaps on the GPU (for example on two streams at once) race; serialise them.
  * Work is issued on `stream` (cudaStream_t, NULL = legacy default stream).  Errors are reported by

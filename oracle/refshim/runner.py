@@ -2,9 +2,10 @@
 
 ``reference_track(vol_dict)`` calls the reference's unmodified ``uppe_kernel.track``
 (``modules/uppe_kernel.py:333-424``) with its own OpenCL kernels, compiled as C++ by the
-``pyopencl`` stand-in in this folder.  It needs the reference source tree (``SEARAY_REF``,
-default ``/root/reference``), so it runs only where that tree exists; it is used to generate the
-golden fixtures under ``tests/golden/`` and never at test or bench time on a GPU machine.
+``pyopencl`` stand-in in this folder.  It needs the reference source tree: the folder named by ``SEARAY_REF``, by ``set_reference()``,
+or else the one that the build recipe recorded in ``oracle/_ref/reference_root.txt`` when it
+compiled the reference's kernels there.  It runs only where that tree exists; it is used to generate
+the golden fixtures under ``tests/golden/`` and never at test or bench time on a GPU machine.
 """
 import contextlib
 import io
@@ -14,12 +15,36 @@ import sys
 
 import numpy as np
 
-REF = pathlib.Path(os.environ.get("SEARAY_REF", "/root/reference"))
 _HERE = pathlib.Path(__file__).resolve().parent
+RECORD = _HERE.parent / "_ref" / "reference_root.txt"
+
+
+def _resolve():
+    if os.environ.get("SEARAY_REF"):
+        return pathlib.Path(os.environ["SEARAY_REF"])
+    if RECORD.exists():
+        return pathlib.Path(RECORD.read_text().strip())
+    return None
+
+
+REF = _resolve()
+
+
+def set_reference(path):
+    """Use the reference source tree at ``path`` (before the first reference call)."""
+    global REF
+    REF = pathlib.Path(path)
+
+
+def record_reference(path):
+    """Remember ``path`` as the reference tree for later processes (written by the build recipe)."""
+    set_reference(path)
+    RECORD.parent.mkdir(exist_ok=True)
+    RECORD.write_text(str(REF) + "\n")
 
 
 def available():
-    return (REF / "modules" / "uppe_kernel.py").exists()
+    return REF is not None and (REF / "modules" / "uppe_kernel.py").exists()
 
 
 def _setup_path():

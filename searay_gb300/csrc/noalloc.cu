@@ -6,9 +6,13 @@
 // caller cannot create a handle (uppe_create allocates the work buffers).  It can still ask for the
 // next RK4 step size from q and S = dq/dz, which it keeps in its own device memory.
 //
-// The reduction scratch is a file-scope __device__ array of fixed size, resident on every GPU
-// that loads this library until the process exits.  The caller passes only inputs (q, S) and the
-// output (dz, one float in device memory).
+// The reduction scratch is a file-scope __device__ array of fixed size.  It lives in this file's
+// own CUDA module, which the runtime loads onto a device on first use (lazy module loading, the
+// default in current CUDA): the first call on each device therefore loads the module, resolves the
+// array's address and loads the four kernels, and only that first call may allocate device memory
+// (for the array and the kernels' code).  From then on the array stays on that device until the
+// process exits.  The caller passes only inputs (q, S) and the output (dz, one float in device
+// memory).
 #include <math.h>
 #include <mutex>
 
@@ -45,26 +49,39 @@ __device__ __forceinline__ float na_block_reduce(float v, bool is_max, float id)
     return r;  // valid in thread 0
 }
 
-// Pass 1: each block writes max|q| over its chunk.
+// fmaxf and fminf drop NaN operands, so a non-finite value is tracked separately: a block's
+// partial result becomes NaN when its chunk holds one, and the final reductions pass NaN on.
+
+// Pass 1: each block writes max|q| over its chunk (NaN if the chunk holds a non-finite q).
 __global__ void k_na_absmax_partial(const float2* __restrict__ q, long long n, float* scratch) {
     const long long b0 = (long long)blockIdx.x * NOALLOC_CHUNK;
     long long b1 = b0 + NOALLOC_CHUNK;
     if (b1 > n) b1 = n;
     float m = 0.f;
+    bool bad = false;
     for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
         float2 v = q[i];
-        m = fmaxf(m, sqrtf(v.x * v.x + v.y * v.y));
+        const float a = sqrtf(v.x * v.x + v.y * v.y);
+        bad = bad || !isfinite(a);
+        m = fmaxf(m, a);
     }
+    bad = __syncthreads_or(bad ? 1 : 0) != 0;
     m = na_block_reduce(m, true, 0.f);
-    if (threadIdx.x == 0) scratch[blockIdx.x] = m;
+    if (threadIdx.x == 0) scratch[blockIdx.x] = bad ? NAN : m;
 }
 
-// Pass 2: one block reduces the partial maxima into scratch[2 MAXB].
+// Pass 2: one block reduces the partial maxima into scratch[2 MAXB] (NaN if any partial is NaN).
 __global__ void k_na_absmax_final(int nblocks, float* scratch) {
     float m = 0.f;
-    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) m = fmaxf(m, scratch[i]);
+    bool bad = false;
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+        const float v = scratch[i];
+        bad = bad || isnan(v);
+        m = fmaxf(m, v);
+    }
+    bad = __syncthreads_or(bad ? 1 : 0) != 0;
     m = na_block_reduce(m, true, 0.f);
-    if (threadIdx.x == 0) scratch[2 * NOALLOC_MAX_BLOCKS] = m;
+    if (threadIdx.x == 0) scratch[2 * NOALLOC_MAX_BLOCKS] = bad ? NAN : m;
 }
 
 // Pass 3: per-block min of dphi / K (paraxial.cl:40-58) with amin = rel_amin * max|q|.
@@ -76,27 +93,39 @@ __global__ void k_na_dz_partial(const float2* __restrict__ q, const float2* __re
     long long b1 = b0 + NOALLOC_CHUNK;
     if (b1 > n) b1 = n;
     float m = INFINITY;
+    bool bad = isnan(amin);
     for (long long i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
         float2 Q = q[i], S = k[i];
+        bad = bad || !isfinite(S.x) || !isfinite(S.y);
         float den = Q.x * Q.x + Q.y * Q.y + amin2;
         float alpha = (Q.x * S.x + Q.y * S.y) / den;
         float keff = (Q.x * S.y - Q.y * S.x) / den;
         float K = minRate + fabsf(keff) - (alpha < 0.f ? alpha : 0.f);
         m = fminf(m, dphi / K);
     }
+    bad = __syncthreads_or(bad ? 1 : 0) != 0;
     m = na_block_reduce(m, false, INFINITY);
-    if (threadIdx.x == 0) scratch[NOALLOC_MAX_BLOCKS + blockIdx.x] = m;
+    if (threadIdx.x == 0) scratch[NOALLOC_MAX_BLOCKS + blockIdx.x] = bad ? NAN : m;
 }
 
-// Pass 4: one block reduces the partial minima into the caller's output.
+// Pass 4: one block reduces the partial minima into the caller's output (NaN if any is NaN).
 __global__ void k_na_dz_final(int nblocks, const float* scratch, float* dz_out) {
     float m = INFINITY;
-    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) m = fminf(m, scratch[NOALLOC_MAX_BLOCKS + i]);
+    bool bad = false;
+    for (int i = threadIdx.x; i < nblocks; i += blockDim.x) {
+        const float v = scratch[NOALLOC_MAX_BLOCKS + i];
+        bad = bad || isnan(v);
+        m = fminf(m, v);
+    }
+    bad = __syncthreads_or(bad ? 1 : 0) != 0;
     m = na_block_reduce(m, false, INFINITY);
-    if (threadIdx.x == 0) *dz_out = m;
+    if (threadIdx.x == 0) *dz_out = bad ? NAN : m;
 }
 
-// Device address of the scratch array, looked up once per device with that device current.
+// Device address of the scratch array, looked up once per device with that device current.  The
+// same set-up loads the four kernels (cudaFuncGetAttributes), so that under lazy module loading
+// no later call loads anything.  The address is that of the device's primary context (the one the
+// runtime API uses); it is not refreshed after cudaDeviceReset.
 #define NOALLOC_MAX_DEVICES 64
 static float* g_scratch_ptr[NOALLOC_MAX_DEVICES];
 static std::mutex g_scratch_mutex;
@@ -115,6 +144,16 @@ static int scratch_for_current_device(float** out) {
         if (e != cudaSuccess || !ptr) {
             uppe_set_error(nullptr, "uppe_step_size_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
             return UPPE_E_CUDA;
+        }
+        const void* kernels[] = {(const void*)k_na_absmax_partial, (const void*)k_na_absmax_final,
+                                 (const void*)k_na_dz_partial, (const void*)k_na_dz_final};
+        for (const void* f : kernels) {
+            cudaFuncAttributes attr;
+            e = cudaFuncGetAttributes(&attr, f);
+            if (e != cudaSuccess) {
+                uppe_set_error(nullptr, "uppe_step_size_noalloc: loading its kernels failed: %s", cudaGetErrorString(e));
+                return UPPE_E_CUDA;
+            }
         }
         g_scratch_ptr[dev] = (float*)ptr;
     }

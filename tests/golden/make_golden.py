@@ -7,9 +7,9 @@ paraxial cases, and stores, per case, the resolved inputs (incoming field, chi(w
 coefficients) and the outputs (A, J, chiNL, ne on every diagnostic plane after the first, dom4d).
 Also stores reference Hankel bases (``grid_tools.HankelTransformTool``).
 
-Needs the reference source tree (``SEARAY_REF``, default ``/root/reference``)::
+Needs the reference source tree, given by ``--reference PATH`` (or ``SEARAY_REF``)::
 
-    python tests/golden/make_golden.py [case ...]
+    python tests/golden/make_golden.py --reference PATH [case ...]
 
 With case names, only those fixtures are written (and not the Hankel bases).
 """
@@ -117,5 +117,15 @@ def main(names=None):
     np.savez_compressed(HERE / "hankel_bases.npz", **bases)
 
 
+def _args(argv):
+    """Strip ``--reference PATH`` from the arguments and point the reference runner at PATH."""
+    argv = list(argv)
+    if "--reference" in argv:
+        i = argv.index("--reference")
+        runner.set_reference(argv[i + 1])
+        del argv[i:i + 2]
+    return argv
+
+
 if __name__ == "__main__":
-    main(sys.argv[1:])
+    main(_args(sys.argv[1:]))

@@ -9,9 +9,9 @@ wave``) on a small Cartesian Kerr volume (``raywave_track_cart.npz``), and its p
 
 The reference's cylindrical ``RelaunchRays1`` calls ``scipy.integrate.cumtrapz``, which SciPy has
 since renamed ``cumulative_trapezoid`` (same trapezoid rule); the name is supplied before the call.
-Needs the reference source tree (``SEARAY_REF``, default ``/root/reference``)::
+Needs the reference source tree, given by ``--reference PATH`` (or ``SEARAY_REF``)::
 
-    python tests/golden/make_raywave.py
+    python tests/golden/make_raywave.py --reference PATH [paraxial]
 """
 import pathlib
 import sys
@@ -169,5 +169,15 @@ def main(names=None):
     paraxial_fixture(m, cl, np.random.default_rng(11))
 
 
+def _args(argv):
+    """Strip ``--reference PATH`` from the arguments and point the reference runner at PATH."""
+    argv = list(argv)
+    if "--reference" in argv:
+        i = argv.index("--reference")
+        runner.set_reference(argv[i + 1])
+        del argv[i:i + 2]
+    return argv
+
+
 if __name__ == "__main__":
-    main(sys.argv[1:])
+    main(_args(sys.argv[1:]))

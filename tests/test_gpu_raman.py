@@ -4,8 +4,8 @@ FP64 oracle, at shapes the golden case (tests/golden cyl_raman, checked in test_
 not reach: Cartesian slices, Raman together with ionization, longer time axes (fewer transverse
 points per block of the time pass) and a block of fewer than 32 threads.
 
-Error metric max |a - b| / max |b|; tolerances those of the golden parity tests: field within
-2e-5, current and chi within 1e-4.
+Metrics and bounds of tests/parity.py: field, fluence and spectrum within 1e-5 with FP32
+transverse transforms (1e-4 with the tensor-core Hankel transform), current and chi within 1e-4.
 
 Inputs: the 800 nm filamentation medium of the bench workload (air, Kerr, O2 tunnelling, plasma
 current, seeded transverse phase screen) with the N2 rotator of the golden case (32 states, 100 ps
@@ -14,6 +14,7 @@ import numpy as np
 import pytest
 
 import cases
+from parity import DIAG_TOL, check_field, field_errors, fmt
 
 pytestmark = pytest.mark.gpu
 
@@ -76,10 +77,11 @@ def test_raman_rk4_step_vs_oracle(shape, precision):
     a_dev = torch.from_numpy(a.astype(np.complex64)).cuda()
     A, J, chi, ne, evals = uppe.propagator(dev, mat, a_dev, 1, 0.0, L, L)
     assert evals == 4
-    errs = {"A": rel_err(A.cpu().numpy(), A_ref), "J": rel_err(J.cpu().numpy(), J_ref),
-            "chi": rel_err(chi.cpu().numpy(), chi_ref)}
-    print(shape, precision, {k: f"{v:.2e}" for k, v in errs.items()})
-    assert errs["A"] < 2e-5 and errs["J"] < 1e-4 and errs["chi"] < 1e-4
+    errs = field_errors(A.cpu().numpy(), A_ref)
+    errs.update({"J": rel_err(J.cpu().numpy(), J_ref), "chi": rel_err(chi.cpu().numpy(), chi_ref)})
+    print(shape, precision, fmt(errs))
+    check_field(errs, False)
+    assert errs["J"] < DIAG_TOL and errs["chi"] < DIAG_TOL
     dev.close()
 
 
@@ -108,11 +110,12 @@ def test_raman_small_cylindrical_block(precision):
     A_ref, J_ref, chi_ref, _, _ = O.Oracle(vd).propagator(a, 0.0, L, 1, L)
     a_dev = torch.from_numpy(a.astype(np.complex64)).cuda()
     A, J, chi_d, _, _ = uppe.propagator(dev, mat, a_dev, 1, 0.0, L, L)
-    errs = {"A": rel_err(A.cpu().numpy(), A_ref), "J": rel_err(J.cpu().numpy(), J_ref),
-            "chi": rel_err(chi_d.cpu().numpy(), chi_ref)}
-    print("17x4x1", precision, {k: f"{v:.2e}" for k, v in errs.items()})
+    errs = field_errors(A.cpu().numpy(), A_ref)
+    errs.update({"J": rel_err(J.cpu().numpy(), J_ref), "chi": rel_err(chi_d.cpu().numpy(), chi_ref)})
+    print("17x4x1", precision, fmt(errs))
     # the 4-mode Hankel transform of the mixed form runs on the tensor cores (1e-4 bound)
-    assert errs["A"] < (1e-4 if precision == "mixed" else 2e-5) and errs["J"] < 1e-4 and errs["chi"] < 1e-4
+    check_field(errs, precision == "mixed")
+    assert errs["J"] < DIAG_TOL and errs["chi"] < DIAG_TOL
     dev.close()
 
 

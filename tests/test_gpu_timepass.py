@@ -2,10 +2,13 @@
 2049), where it runs with compile-time sizes (searay_gb300/csrc/timepass.cu), and at the longest
 time axis the library accepts (N0 = 4097, Nt = 8192: one transverse point per block, the
 runtime-size kernel): one fixed RK4 step and the finish against the FP64 oracle, on a 16 x 16
-Cartesian grid with the filamentation medium and a pulse strong enough to ionize.  Bounds: the
-golden parity tolerances (field 2e-5; J, chi, ne 1e-4)."""
+Cartesian grid with the filamentation medium and a pulse strong enough to ionize.  Bounds: those of
+tests/parity.py for FP32 transverse transforms (field, fluence and spectrum 1e-5; J, chi, ne
+1e-4)."""
 import numpy as np
 import pytest
+
+from parity import DIAG_TOL, check_field, field_errors, fmt
 
 pytestmark = pytest.mark.gpu
 
@@ -45,9 +48,11 @@ def test_time_pass_rk4_step_vs_oracle(n0, precision):
     A_ref, J_ref, chi_ref, ne_ref, nsteps = O.Oracle(vd).propagator(a, 0.0, L, 1, L)
     A, J, chi_w, ne, evals = uppe.propagator(dev, mat, torch.from_numpy(a.astype(np.complex64)).cuda(), 1, 0.0, L, L)
     assert nsteps == 1 and evals == 4
-    errs = {"A": rel_err(A.cpu().numpy(), A_ref), "J": rel_err(J.cpu().numpy(), J_ref),
-            "chi": rel_err(chi_w.cpu().numpy(), chi_ref), "ne": rel_err(ne.cpu().numpy(), ne_ref)}
-    print(n0, precision, {k: f"{v:.2e}" for k, v in errs.items()})
+    errs = field_errors(A.cpu().numpy(), A_ref)
+    errs.update({"J": rel_err(J.cpu().numpy(), J_ref), "chi": rel_err(chi_w.cpu().numpy(), chi_ref),
+                 "ne": rel_err(ne.cpu().numpy(), ne_ref)})
+    print(n0, precision, fmt(errs))
     assert np.max(np.abs(ne_ref)) > 0
-    assert errs["A"] < 2e-5 and errs["J"] < 1e-4 and errs["chi"] < 1e-4 and errs["ne"] < 1e-4
+    check_field(errs, False)
+    assert errs["J"] < DIAG_TOL and errs["chi"] < DIAG_TOL and errs["ne"] < DIAG_TOL
     dev.close()

@@ -82,7 +82,9 @@ def test_reference_arm_line_keeps_the_bench_contract(capsys):
         assert k in d, k
     assert d["impl"] == "reference" and d["steps"] == 3 and d["warmup"] == 3 and d["value"] > 0
     assert d["config"]["workload"] == "cyl_kerr_64"
-    assert d["config"]["sample_grid"] == d["config"]["grid"] == [257, 64, 1]
+    assert d["sample_grid"] == d["config"]["grid"] == [257, 64, 1]
+    # the workload description is the one the GPU arm's line carries
+    assert d["config"] == bench.config_of(Args(), vd, 1)
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["unit"] == d["unit"]
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
@@ -102,7 +104,28 @@ def test_cpu_baseline_repeats_steps_to_its_time():
     sys.path.insert(0, ROOT)
     import bench
     from searay_gb300 import workloads
-    cb = bench.cpu_baseline(workloads.WORKLOADS["cyl_kerr_64"](), min_seconds=0.5, max_steps=50)
+    vd = workloads.WORKLOADS["cyl_kerr_64"]()
+    cb, v, out = bench.cpu_baseline(vd, min_seconds=0.5, max_steps=50)
     assert cb["kind"] == "port" and cb["value"] > 0 and cb["unit"] == bench.UNIT
     steps = int(cb["sample"].split()[0])
     assert 1 < steps <= 50 and "on the full 257x64x1 grid" in cb["sample"]
+    assert v["wave grid"] == vd["wave grid"] and out is None
+
+
+def test_cpu_baseline_first_step_matches_the_oracle_propagator():
+    """The first-step outputs the bench compares both GPU forms with are the oracle propagator's own
+    outputs for one fixed step (the same medium sample, step and finish)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from oracle import uppe_oracle as O
+    from searay_gb300 import workloads
+    vd = workloads.WORKLOADS["cart_filament_128"]()
+    v = bench.sample_volume(vd, 16)
+    _, steps, _, _, out = bench.oracle_run(v, outputs=True)
+    orc = O.Oracle(v)
+    dz = v["size"][2] / v["subcycles"]
+    a = v["incoming wave"](orc.g.w, orc.g.x1, orc.g.x2)
+    ref = orc.propagator(a, 0.0, dz, 1, dz)
+    assert steps == 1 and ref[4] == 1
+    errs = bench.field_metrics(*out, ref[:4])
+    assert max(errs.values()) < 1e-12, errs

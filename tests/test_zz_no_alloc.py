@@ -53,15 +53,44 @@ def test_noalloc_step_size_matches_handle(lib, name):
         S = dev.empty_field()
         dev.eval_rhs(q, z, S)
         dz_dev = torch.full((1,), -1.0, dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
+        free0, alloc0 = torch.cuda.mem_get_info()[0], torch.cuda.memory_allocated()
         rc = lib.uppe_step_size_noalloc(ctypes.c_void_p(q.data_ptr()), ctypes.c_void_p(S.data_ptr()),
                                         q.numel(), L, 0.4, 1e-2, ctypes.c_void_p(dz_dev.data_ptr()), stream)
         assert rc == 0, lib.uppe_last_error(None)
+        torch.cuda.synchronize()
+        if call > 0:  # after the first call on the device (which loads the module), nothing is allocated
+            assert torch.cuda.mem_get_info()[0] == free0
+            assert torch.cuda.memory_allocated() == alloc0
         dz_noalloc = float(dz_dev.item())
         # the handle path: adaptive RK4 step from the same q at the same z (dzmin 0, no clamp hit)
         dz_handle = dev.rk4_step(z, L, 0.0, 0.0)
         assert 0.0 < dz_noalloc < L
         assert dz_noalloc == pytest.approx(dz_handle, rel=1e-6), (call, dz_noalloc, dz_handle)
     dev.close()
+
+
+def test_noalloc_reports_nonfinite_field(lib):
+    import torch
+    q = torch.ones(3 * 8192 + 5, dtype=torch.complex64, device="cuda")
+    S = torch.full_like(q, 0.5 + 0.25j)
+    out = torch.zeros(1, dtype=torch.float32, device="cuda")
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def call():
+        rc = lib.uppe_step_size_noalloc(ctypes.c_void_p(q.data_ptr()), ctypes.c_void_p(S.data_ptr()), q.numel(),
+                                        10.0, 0.4, 1e-2, ctypes.c_void_p(out.data_ptr()), stream)
+        assert rc == 0, lib.uppe_last_error(None)
+        return float(out.item())
+
+    assert np.isfinite(call())
+    S[2 * 8192 + 3] = float("nan")
+    assert np.isnan(call())
+    S[2 * 8192 + 3] = 0.5
+    q[7] = float("inf")
+    assert np.isnan(call())
+    q[7] = 1.0
+    assert np.isfinite(call())
 
 
 def test_noalloc_rejects_oversize_and_bad_arguments(lib):
