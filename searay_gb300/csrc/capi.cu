@@ -116,7 +116,7 @@ static void free_buffers(UppeHandle* h) {
                     h->MfwdT_tc, h->MinvT_tc,
                     h->adj_q1, h->adj_q2, h->adj_q3, h->adj_lf, h->adj_acc, h->adj_lk, h->adj_mu, h->MfwdT, h->MinvT,
                     h->adj_E[0], h->adj_E[1], h->adj_E[2], h->adj_E[3],
-                    h->dred_d, h->rot, h->Atc};
+                    h->dred_d, h->rot, h->Atc, h->tw_reg, h->tscr};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -206,6 +206,10 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (const char* v = getenv("SEARAY_UPPE_SLICE")) {
         if (strcmp(v, "generic") == 0) h->slice_reg = 0;
     }
+    h->time_reg = 1;
+    if (const char* v = getenv("SEARAY_UPPE_TIME")) {
+        if (strcmp(v, "smem") == 0) h->time_reg = 0;
+    }
     int nt = Nt;
     if (c.n1 > nt) nt = c.n1;
     if (c.n2 > nt) nt = c.n2;
@@ -249,6 +253,11 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
         ALLOC(h->Minv, (size_t)c.n2 * c.n1 * h->Nk * sizeof(float));
         ALLOC(h->Mfwd, (size_t)c.n2 * c.n1 * c.n1 * sizeof(float));
     }
+    // the register-resident time pass (M = 256, 512, 1024): its twiddle tables, and its parking
+    // scratch for ionizing columns when the medium ionizes
+    const bool time_reg = !env && (h->M == 256 || h->M == 512 || h->M == 1024);
+    if (time_reg) ALLOC(h->tw_reg, time_reg_table_len(h->M) * sizeof(float2));
+    if (time_reg && c.rate_form != UPPE_RATE_NONE) ALLOC(h->tscr, time_reg_scratch_len(h) * sizeof(float2));
     ALLOC(h->kr2_d, (size_t)S * sizeof(double));
     ALLOC(h->w2n2_d, (size_t)2 * c.n0 * sizeof(double));
     ALLOC(h->kg_d, (size_t)c.n0 * sizeof(double));
@@ -269,11 +278,17 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
         tw[j] = make_float2((float)cos(a), (float)sin(a));
     }
     e = cudaMemcpy(h->tw, tw.data(), NT * sizeof(float2), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && h->tw_reg) {
+        std::vector<float2> twr(time_reg_table_len(h->M));
+        time_reg_tables(h->M, twr.data());
+        e = cudaMemcpy(h->tw_reg, twr.data(), twr.size() * sizeof(float2), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaMemset(h->dev_err, 0, sizeof(int));
     // Allow the kernels that stage a whole slice / time tile in shared memory the full 227 KB; each
     // launch still requests only what its grid needs.
     if (e == cudaSuccess) e = uppe_configure_slice_kernels(227 * 1024);
     if (e == cudaSuccess) e = uppe_configure_time_kernel(227 * 1024);
+    if (e == cudaSuccess && h->tw_reg) e = uppe_configure_time_reg();
     if (e == cudaSuccess) e = uppe_configure_time_adj_kernel(224 * 1024);  // leaves room for its static shared memory
     if (e == cudaSuccess && env) e = uppe_configure_env_kernel(227 * 1024);
     if (e != cudaSuccess) {

@@ -27,58 +27,10 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "dft_reg.cuh"
 #include "fft_smem.cuh"
 #include "rk_stage.cuh"
 #include "uppe_internal.h"
-
-#define UPPE_COS_PI8 0.92387953251128675613f
-#define UPPE_SIN_PI8 0.38268343236508977173f
-
-// v * W16^E, W16 = exp(-2 pi i / 16); conjugated twiddle for the inverse transform
-template <int E, bool INV>
-UPPE_DEV float2 mul_w16(float2 v) {
-    float2 w;
-    if constexpr (E == 4) {
-        return INV ? cmul_i(v) : cmul_mi(v);
-    } else {
-        if constexpr (E == 1) w = make_float2(UPPE_COS_PI8, -UPPE_SIN_PI8);
-        else if constexpr (E == 2) w = make_float2(UPPE_SQRT1_2, -UPPE_SQRT1_2);
-        else if constexpr (E == 3) w = make_float2(UPPE_SIN_PI8, -UPPE_COS_PI8);
-        else if constexpr (E == 6) w = make_float2(-UPPE_SQRT1_2, -UPPE_SQRT1_2);
-        else w = make_float2(-UPPE_COS_PI8, UPPE_SIN_PI8);  // E == 9
-        if (INV) w.y = -w.y;
-        return cmul(v, w);
-    }
-}
-
-// In-register 16-point DFT, natural order in and out: 4 x 4 with W16 twiddles between the halves.
-template <bool INV>
-UPPE_DEV void dft16(float2 (&v)[16]) {
-    float2 t[4][4];
-#pragma unroll
-    for (int n1 = 0; n1 < 4; ++n1) {
-        float2 u[4] = {v[n1], v[n1 + 4], v[n1 + 8], v[n1 + 12]};
-        dft_small<4>(u, INV);
-#pragma unroll
-        for (int k1 = 0; k1 < 4; ++k1) t[n1][k1] = u[k1];
-    }
-    t[1][1] = mul_w16<1, INV>(t[1][1]);
-    t[1][2] = mul_w16<2, INV>(t[1][2]);
-    t[1][3] = mul_w16<3, INV>(t[1][3]);
-    t[2][1] = mul_w16<2, INV>(t[2][1]);
-    t[2][2] = mul_w16<4, INV>(t[2][2]);
-    t[2][3] = mul_w16<6, INV>(t[2][3]);
-    t[3][1] = mul_w16<3, INV>(t[3][1]);
-    t[3][2] = mul_w16<6, INV>(t[3][2]);
-    t[3][3] = mul_w16<9, INV>(t[3][3]);
-#pragma unroll
-    for (int k1 = 0; k1 < 4; ++k1) {
-        float2 u[4] = {t[0][k1], t[1][k1], t[2][k1], t[3][k1]};
-        dft_small<4>(u, INV);
-#pragma unroll
-        for (int k2 = 0; k2 < 4; ++k2) v[k1 + 4 * k2] = u[k2];
-    }
-}
 
 template <bool INV>
 UPPE_DEV float2 tw_at(const TwGlobal& tw, int k, int sh) {

@@ -352,6 +352,9 @@ TimeParams uppe_time_params(const UppeHandle* h) {
 
 cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1) {
     if (h->cfg.envelope) return launch_time_env(h, mode, E, out0, out1);
+    // the register-resident pass (timepass_reg.cu) for the current J at M = 256, 512, 1024;
+    // SEARAY_UPPE_TIME=smem selects the shared-memory form below for every grid
+    if (mode == TIME_J && h->time_reg && h->tw_reg && time_reg_supported(h)) return launch_time_reg(h, E, out0);
     const TimeParams tp = uppe_time_params(h);
     const int T = h->Nt * h->time_cols / h->time_spt;
     const size_t smem = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);

@@ -57,6 +57,7 @@ struct UppeHandle {
     int smem_per_sm;               // shared memory per multiprocessor (bytes)
     int slice_reg;                 // Cartesian slices use the register-resident transforms (slice_reg.cuh)
     int slice_big;                 // Cartesian slices above 128 x 128: row and column passes (slice_big.cu)
+    int time_reg;                  // TIME_J through the register-resident time pass where it applies (timepass_reg.cu)
     cudaStream_t stream;
     // library-owned device buffers
     float2 *q, *qi, *qf, *k1, *E, *J, *scratch;
@@ -66,6 +67,8 @@ struct UppeHandle {
     int complex_medium;
     float* ng;
     float2* tw;
+    float2* tw_reg;  // twiddle tables of the register-resident time pass (timepass_reg.cu), or NULL
+    float2* tscr;    // its parking scratch for ionizing columns ([S][2 (M + 1)]), or NULL
     float* w;        // omega per bin (FP32)
     float* nlfilt;   // NL filter per bin
     float* Minv;     // cylindrical: [N2][Nr][Nk]
@@ -128,6 +131,13 @@ cudaError_t launch_fused_cart(UppeHandle* h, int mode, float Cs, float Ce, StepA
 // Cartesian first stage from k1 (adaptive step) fused with the inverse transform to E.
 cudaError_t launch_apply1_cart(UppeHandle* h, float Cs, float Ce, StepArgs z);
 cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* out0, float2* out1);
+// register-resident time pass (timepass_reg.cu): TIME_J for M = 256, 512, 1024 without a rotator
+bool time_reg_supported(const UppeHandle* h);
+size_t time_reg_table_len(int M);
+int time_reg_tables(int M, float2* host);
+size_t time_reg_scratch_len(const UppeHandle* h);
+cudaError_t uppe_configure_time_reg();
+cudaError_t launch_time_reg(UppeHandle* h, const float2* E, float2* J);
 // paraxial envelope time pass (envelope.cu)
 cudaError_t launch_time_env(UppeHandle* h, int mode, const float2* A, float2* out0, float2* out1);
 cudaError_t uppe_configure_env_kernel(size_t smem_bytes);
