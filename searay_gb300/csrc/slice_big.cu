@@ -88,7 +88,7 @@ struct BigColArgs {
 // points are loaded before any store of those points: the stores could alias the loads as far as
 // the compiler knows, which otherwise serialises every point behind a full memory latency.
 template <int LN1, int LN2, int KIND>
-__global__ void __launch_bounds__(16 << (LN1 - 4)) k_cols_big(BigColArgs a, OpView opv, const float2* __restrict__ tw,
+__global__ void __launch_bounds__(16 << (LN1 - 4), 3) k_cols_big(BigColArgs a, OpView opv, const float2* __restrict__ tw,
                                                               int twLog) {
     constexpr int N1 = 1 << LN1, N2 = 1 << LN2, R1 = N1 / 16, T = 16 * R1, TILES = N2 / 16;
     constexpr int QC = 17 * R1 + 1;

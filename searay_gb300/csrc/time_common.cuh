@@ -17,6 +17,7 @@ struct TimeParams {
     float c2[6];           // series form: log2(e) * c_i, polynomial in L = ln(Em)
     float em_min;          // below this Em the rate is below FP32's smallest normal (taken as 0)
     int wcut, wwid, plain;
+    int cut_on, cut_off;   // NL filter: J is kept for cut_on <= k < cut_off (uppe_kernel.py:122-125)
     // rotational Raman: transitions in pairs, 20 float4 per pair (constants and powers of h^2) and
     // the phasor table p0[pair][segment] (raman_pass)
     int rot_pairs;

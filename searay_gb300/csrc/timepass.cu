@@ -312,6 +312,8 @@ TimeParams uppe_time_params(const UppeHandle* h) {
     tp.lrc2 = (c.rate_conv > 0) ? (float)log2(c.rate_conv) : 0.f;
     for (int i = 0; i < 6; ++i) tp.c2[i] = (float)(c.clog[i] * log2e);
     tp.wcut = c.window_cutoff;
+    tp.cut_on = c.nl_cut_on;
+    tp.cut_off = c.nl_cut_off;
     tp.wwid = c.window_width;
     tp.plain = (c.precision == UPPE_PREC_FP32);
     tp.rot_pairs = h->rot_pairs;

@@ -130,7 +130,7 @@ UPPE_DEV void tr_unpack(const float2 (&v)[TReg<LOGM>::R1], const float2* __restr
 template <int LOGM>
 __global__ void __launch_bounds__(256, 2)
     k_time_reg(const float2* __restrict__ E, float2* __restrict__ Jout, const float* __restrict__ ng,
-               const float* __restrict__ wv, const float* __restrict__ filt, const float2* __restrict__ twt,
+               const float* __restrict__ wv, const float2* __restrict__ twt,
                float2* __restrict__ tscr, TimeParams tp) {
     using G = TReg<LOGM>;
     constexpr int M = G::M, TC = G::TC, R1 = G::R1, NB = G::NB, NC = G::NC, LD = G::LD;
@@ -297,14 +297,16 @@ __global__ void __launch_bounds__(256, 2)
     // ---- forward transform of P and its real spectrum: J = -i w P (x filter) ----
     tr_forward<LOGM>(v, buf, twF, t);
     __syncwarp();  // the exchange reads of buf are done before the output staging
+    // the NL filter (0 or 1 per bin) from its cut indices
+    const auto kept = [&](int k) { return k >= tp.cut_on && k < tp.cut_off; };
     if (!live) {
         tr_unpack<LOGM>(v, twP, t, lane, [&](int k, float2 P) {
-            buf[k] = cscale(cmul_mi(cscale(P, __ldg(&wv[k]))), __ldg(&filt[k]));
+            buf[k] = kept(k) ? cmul_mi(cscale(P, __ldg(&wv[k]))) : make_float2(0.f, 0.f);
         });
     } else {
         float2* parkJ = park + (M + 1);
         tr_unpack<LOGM>(v, twP, t, lane, [&](int k, float2 P) {
-            parkJ[k] = cscale(cmul_mi(cscale(P, __ldg(&wv[k]))), __ldg(&filt[k]));
+            parkJ[k] = kept(k) ? cmul_mi(cscale(P, __ldg(&wv[k]))) : make_float2(0.f, 0.f);
         });
         // Jpl from its parking place (this lane's own entries), forward transform, and
         // J += Jpl(w) (damping + i w) / (damping^2 + w^2) (x filter)
@@ -319,7 +321,7 @@ __global__ void __launch_bounds__(256, 2)
             const float wk = __ldg(&wv[k]);
             const float rden = __frcp_rn(fmaf(wk, wk, damp * damp));
             const float2 q = cscale(cmul(Q, make_float2(damp, wk)), rden);
-            buf[k] = cadd(parkJ[k], cscale(q, __ldg(&filt[k])));
+            buf[k] = kept(k) ? cadd(parkJ[k], q) : make_float2(0.f, 0.f);
         });
     }
 
@@ -391,15 +393,15 @@ cudaError_t launch_time_reg(UppeHandle* h, const float2* E, float2* J) {
     switch (h->M) {
         case 256:
             k_time_reg<8><<<h->S / TReg<8>::NC, TReg<8>::THREADS, TReg<8>::SMEM, h->stream>>>(
-                E, J, h->ng, h->w, h->nlfilt, h->tw_reg, h->tscr, tp);
+                E, J, h->ng, h->w, h->tw_reg, h->tscr, tp);
             break;
         case 512:
             k_time_reg<9><<<h->S / TReg<9>::NC, TReg<9>::THREADS, TReg<9>::SMEM, h->stream>>>(
-                E, J, h->ng, h->w, h->nlfilt, h->tw_reg, h->tscr, tp);
+                E, J, h->ng, h->w, h->tw_reg, h->tscr, tp);
             break;
         default:
             k_time_reg<10><<<h->S / TReg<10>::NC, TReg<10>::THREADS, TReg<10>::SMEM, h->stream>>>(
-                E, J, h->ng, h->w, h->nlfilt, h->tw_reg, h->tscr, tp);
+                E, J, h->ng, h->w, h->tw_reg, h->tscr, tp);
             break;
     }
     return cudaGetLastError();

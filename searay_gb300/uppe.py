@@ -316,14 +316,21 @@ class TrackOutputs:
     def host(self):
         """NumPy views of pinned host copies.  A copy into freshly allocated pageable memory runs at
         the speed of its first-touch page faults (about 24 GB/s on GB300's host); the pinned blocks
-        of torch's caching host allocator, reused once earlier results are released, take the copy at
-        about 190 GB/s."""
-        out = []
+        of torch's caching host allocator, reused once earlier results are released, take the copy
+        faster, and the four arrays go on four streams so that their copies run side by side."""
+        main = torch.cuda.current_stream()
+        out, streams = [], []
         for x in self.arrays:
             h = torch.empty(x.shape, dtype=x.dtype, pin_memory=True)
-            h.copy_(x)
-            out.append(h.numpy())
-        return tuple(out)
+            s = torch.cuda.Stream()
+            s.wait_stream(main)
+            with torch.cuda.stream(s):
+                h.copy_(x, non_blocking=True)
+            streams.append(s)
+            out.append(h)
+        for s in streams:
+            s.synchronize()
+        return tuple(h.numpy() for h in out)
 
 
 def track(cl, xp, eikonal, vg, vol_dict):

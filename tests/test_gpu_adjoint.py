@@ -283,3 +283,59 @@ def test_legendre_phase_gradient_1025x256():
         assert abs(a - b) < 3e-2 * abs(b), (k, a, b)
     assert abs(gc[0]) < 2e-2 * np.abs(gc).max()
     dev.close()
+
+
+def test_transverse_phase_gradient_large_filament():
+    """The gradient of the large-filament workload's forward+adjoint objective: 1025 x 256 x 256
+    Cartesian, 800 nm 40 fs at 10 critical powers in air with Kerr, O2 tunnelling and the plasma
+    current, mixed precision, checkpoints every 50 steps; the loss is the energy of the central
+    32 x 32 points in the band 0.9 < w < 1.1 after 100 steps (1 cm of the 10 cm), and the parameter
+    the 256 x 256 input transverse phase phi(x, y) (a0 = a e^{i phi}).  The gradient is checked along
+    two smooth directions of phi against central differences of the FP32 forward: centred Gaussian
+    bumps of the beam's radius and of half of it (weak lenses of two widths), h = 0.05 rad, within
+    3e-2.  The loss responds to a lens of 1 rad by a few percent over 1 cm (the Rayleigh length is
+    about 35 cm), so h is large against the FP32 rounding noise (about 1e-6 of the loss) and small
+    enough that the O(h^2) error stays below 1e-2."""
+    import torch
+    from searay_gb300 import adjoint, grid, ionization, uppe, workloads
+    vd = workloads.cart_filament_256()
+    g = grid.VolumeGrid(vd)
+    dev = uppe.DeviceGrid(g, vd, ionization.RateCoefficients(vd["ionizer"]), "mixed")
+    chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+    mat = uppe.Material(dev, g, "cartesian", None, chi, vd["chi3"], vd["density reference"], vd["window speed"],
+                        vd["density lambda"])
+    dz = vd["size"][2] / vd["subcycles"]
+    mat.UpdateMaterial(0.5 * dz)
+    redchi3 = vd["chi3"] / vd["density reference"]
+    nsteps = 100
+    base = torch.from_numpy(vd["incoming wave"](g.w, g.x1, g.x2).astype(np.complex64)).cuda()
+    band = torch.as_tensor((g.w > 0.9) & (g.w < 1.1)).cuda()
+    c = g.N[1] // 2
+
+    def loss(phi):
+        a0 = base * torch.exp(1j * phi.to(torch.float32))[None]
+        A = adjoint.propagate(dev, a0, redchi3, dz, nsteps, checkpoint_every=50)
+        sel = A[band][:, c - 16:c + 16, c - 16:c + 16].to(torch.complex128)
+        return (sel.abs() ** 2).sum()
+
+    phi = torch.zeros(g.N[1], g.N[2], dtype=torch.float64, device="cuda", requires_grad=True)
+    L = loss(phi)
+    L.backward()
+    grad = phi.grad.detach()
+    X, Y = np.meshgrid(g.x1, g.x2, indexing="ij")
+    r0 = 0.3e-3 / (0.8e-6 / (2 * np.pi))  # the beam radius, simulation units
+    gauss = np.exp(-(X ** 2 + Y ** 2) / r0 ** 2)
+    dirs = {"lens": gauss, "narrow lens": np.exp(-4 * (X ** 2 + Y ** 2) / r0 ** 2)}
+    h = 0.05
+    res = {}
+    with torch.no_grad():
+        for name, u in dirs.items():
+            ut = torch.from_numpy(u).cuda()
+            ad = float((grad * ut).sum())
+            fd = (loss(h * ut) - loss(-h * ut)).item() / (2 * h)
+            res[name] = (ad, fd)
+    print(f"L {L.item():.6e}", {k: f"adjoint {a:.6e} fd {b:.6e}" for k, (a, b) in res.items()})
+    for k, (a, b) in res.items():
+        assert abs(b) > 1e-3 * L.item(), (k, b)  # the direction moves the loss measurably
+        assert abs(a - b) < 3e-2 * abs(b), (k, a, b)
+    dev.close()

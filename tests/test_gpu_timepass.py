@@ -56,3 +56,42 @@ def test_time_pass_rk4_step_vs_oracle(n0, precision):
     check_field(errs, False)
     assert errs["J"] < DIAG_TOL and errs["chi"] < DIAG_TOL and errs["ne"] < DIAG_TOL
     dev.close()
+
+
+@pytest.mark.parametrize("n0,n_perp", [(257, 16), (513, 32), (1025, 16)])
+def test_register_time_pass_matches_shared_memory_form(n0, n_perp, monkeypatch):
+    """The register-resident time pass (M = 256, 512, 1024) against the shared-memory Stockham form
+    (SEARAY_UPPE_TIME=smem) on the same field: one RHS evaluation, ionizing columns included.  Both are
+    FP32 transforms of the same sums, each within about 2e-6 of the FP64 RHS on these grids; they are
+    held to the RHS bound of the oracle comparisons, 1e-5 (w-bins 4 and up)."""
+    import torch
+    from searay_gb300 import grid, ionization, uppe, workloads
+    vd = workloads.cart_filament_128(steps=400, n_perp=n_perp)
+    vd["wave grid"] = (n0, n_perp, n_perp, 2)
+    vd["frequency band"] = (0.0, 4.0 * (n0 - 1) / 512)
+    vd["nonlinear band"] = (0.0, 3.5 * (n0 - 1) / 512)
+    wave = vd["incoming wave"]
+    vd["incoming wave"] = lambda w, x1, x2: 3.0 * wave(w, x1, x2)
+    g = grid.VolumeGrid(vd)
+    a = torch.from_numpy(vd["incoming wave"](g.w, g.x1, g.x2).astype(np.complex64)).cuda()
+    out = {}
+    for form in ("reg", "smem"):
+        if form == "smem":
+            monkeypatch.setenv("SEARAY_UPPE_TIME", "smem")
+        else:
+            monkeypatch.delenv("SEARAY_UPPE_TIME", raising=False)
+        dev = uppe.DeviceGrid(g, vd, ionization.RateCoefficients(vd["ionizer"]), "mixed")
+        chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+        mat = uppe.Material(dev, g, "cartesian", None, chi, vd["chi3"], vd["density reference"], vd["window speed"],
+                            vd["density lambda"])
+        mat.UpdateMaterial(100.0)
+        dev.load_field(a)
+        q = dev.empty_field()
+        dev.get_field(q)
+        S = dev.empty_field()
+        dev.eval_rhs(q, 50.0, S)
+        out[form] = S.cpu().numpy()
+        dev.close()
+    e = rel_err(out["reg"][4:], out["smem"][4:])
+    print(n0, n_perp, f"register vs shared-memory time pass: {e:.2e}")
+    assert np.max(np.abs(out["smem"][4:])) > 0 and e < 1e-5
