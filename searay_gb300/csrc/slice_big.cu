@@ -83,12 +83,14 @@ struct BigColArgs {
     float2* q_store;  // BC_FUSED: also store each stage estimate here (when set)
 };
 
-// The pass kind is a template parameter (one body per kind keeps each kernel's code small).  In the
+// The pass kind is a template parameter (one body per kind keeps each kernel's code small).  The
+// adjoint stage kind runs three blocks per multiprocessor (80 registers: more warps hide its operand
+// loads better than the registers it gives up); the forward fused kind keeps 128 registers, two blocks.  In the
 // kinds that update the RK or adjoint state (BC_FUSED, BC_ADJ_STAGE) the pointwise operands of eight
 // points are loaded before any store of those points: the stores could alias the loads as far as
 // the compiler knows, which otherwise serialises every point behind a full memory latency.
 template <int LN1, int LN2, int KIND>
-__global__ void __launch_bounds__(16 << (LN1 - 4), 3) k_cols_big(BigColArgs a, OpView opv, const float2* __restrict__ tw,
+__global__ void __launch_bounds__(16 << (LN1 - 4), KIND == BC_ADJ_STAGE ? 3 : 2) k_cols_big(BigColArgs a, OpView opv, const float2* __restrict__ tw,
                                                               int twLog) {
     constexpr int N1 = 1 << LN1, N2 = 1 << LN2, R1 = N1 / 16, T = 16 * R1, TILES = N2 / 16;
     constexpr int QC = 17 * R1 + 1;

@@ -709,19 +709,40 @@ __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     float2 w[16], v[16];
     slice_fwd_from_global<RS, LN1, LN2, false>(g + base, w, sm, c, twg);
     constexpr float scale = 1.0f / (float)RS::S;
+    // The operands of two points are loaded before any store of those points: the operator's
+    // pointers live in a struct, so the compiler must assume a store to acc or out may alias the next
+    // point's loads, which otherwise puts every point behind a full memory latency.
 #pragma unroll
-    for (int r = 0; r < 16; ++r) {
-        const size_t idx = base + col_elem(c, r);
-        const OpPoint o = op_at(opv, idx, kgw);
-        const float2 mu = cmul(cconj(op_ikz(o)), cmul(cconj(propagator_factor(o, pe, 1.f)), cscale(w[r], scale)));
-        if (mode == 2) {
-            out[idx] = cadd(acc[idx], mu);
-        } else {
-            const float2 cm = cscale(mu, cond);
-            acc[idx] = cadd(acc[idx], cm);
-            const float2 lk = cadd(cscale(lam_f[idx], a_f), cscale(cm, a_mu));
-            const float2 f = cconj(propagator_factor(o, ps, -1.f));
-            w[r] = cscale(cmul_mi(cmul(f, lk)), 0.5f / o.kzr);
+    for (int r4 = 0; r4 < 16; r4 += 2) {
+        float2 K4[2], A4[2], L4[2];
+        float ki4[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const size_t idx = base + col_elem(c, r4 + j);
+            K4[j] = opv.K[idx];
+            ki4[j] = opv.ki ? opv.ki[idx] : 0.f;
+            A4[j] = acc[idx];
+            L4[j] = (mode == 2) ? make_float2(0.f, 0.f) : lam_f[idx];
+        }
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            const int r = r4 + j;
+            const size_t idx = base + col_elem(c, r);
+            OpPoint o;
+            o.Khi = K4[j].x;
+            o.Klo = K4[j].y;
+            o.kzr = opv.envelope ? kgw.x : (K4[j].x - kgw.x) + (K4[j].y - kgw.y);
+            o.kzi = ki4[j];
+            const float2 mu = cmul(cconj(op_ikz(o)), cmul(cconj(propagator_factor(o, pe, 1.f)), cscale(w[r], scale)));
+            if (mode == 2) {
+                out[idx] = cadd(A4[j], mu);
+            } else {
+                const float2 cm = cscale(mu, cond);
+                acc[idx] = cadd(A4[j], cm);
+                const float2 lk = cadd(cscale(L4[j], a_f), cscale(cm, a_mu));
+                const float2 f = cconj(propagator_factor(o, ps, -1.f));
+                w[r] = cscale(cmul_mi(cmul(f, lk)), 0.5f / o.kzr);
+            }
         }
     }
     if (mode == 2) return;

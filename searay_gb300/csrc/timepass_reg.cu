@@ -62,10 +62,13 @@ struct TReg {
     static constexpr int SEG = M / TC;  // packed pairs per lane in the contiguous (scan) layout
     static constexpr int LSEG = tr_log2(SEG);
     // column buffer: staged half spectrum (M + 1), exchange 1 (R1 rows of TC + 1), exchange 2 (TC
-    // rows of R1 + 1), the padded natural-order scan array (M + M / SEG); odd pitch
-    static constexpr int LD = tr_max(tr_max(M + 1, R1 * (TC + 1)), tr_max(TC * (R1 + 1), M + M / SEG)) | 1;
+    // rows of R1 + 1), the padded natural-order scan array (M + M / SEG).  Its pitch sets the banks of
+    // the staging and output accesses, where a half-warp touches 16 / NC rows of NC columns: odd for
+    // NC = 16, 2 mod 16 (in float2 units) for NC = 8, so those 16 accesses fall on distinct banks.
+    static constexpr int LD0 = tr_max(tr_max(M + 1, R1 * (TC + 1)), tr_max(TC * (R1 + 1), M + M / SEG));
+    static constexpr int LD = (NC == 16) ? (LD0 | 1) : ((LD0 + 13) / 16) * 16 + 2;
     static constexpr size_t SMEM = (size_t)NC * LD * sizeof(float2);
-    static_assert(NB * TC == R1 && THREADS == 256, "time-pass shape");
+    static_assert(NB * TC == R1 && THREADS == 256 && (NC == 16 || NC == 8) && LD >= LD0, "time-pass shape");
 };
 
 // natural pair index m -> padded position in the column buffer (a pad after every SEG pairs keeps
