@@ -471,11 +471,29 @@ def gpu_first_step_errors(v, ref, precision):
     return field_metrics(*host, ref)
 
 
+def reduced_volume(vd, n_perp=None, n0=None):
+    """The workload on its n_perp x n_perp sub-grid (sample_volume) and/or with n0 frequency nodes at
+    the same spacing (the band and the nonlinear band scaled by (n0 - 1) / (N0 - 1)); unchanged when
+    both are None.  Small cases of the same kernels for profiling."""
+    v = sample_volume(vd, n_perp)
+    N = v["wave grid"]
+    if n0 is not None and n0 != N[0]:
+        f = (n0 - 1) / (N[0] - 1)
+        v["wave grid"] = (n0,) + tuple(N[1:])
+        v["frequency band"] = (v["frequency band"][0] * f, v["frequency band"][1] * f)
+        if "nonlinear band" in v:
+            v["nonlinear band"] = (v["nonlinear band"][0] * f, v["nonlinear band"][1] * f)
+    return v
+
+
 def config_of(args, vd, ws):
-    """The workload description shared by both arms' lines."""
-    return {"workload": args.workload, "grid": list(vd["wave grid"][:3]), "propagator": vd.get("propagator", "uppe"),
-            "parallelism": "replicas" if ws > 1 else "single",
-            "l2": f"working set ({working_set_mb(vd):.0f} MB of fields and operator) vs the 129 MB L2"}
+    """The workload description shared by both arms' lines (marked when reduced for profiling)."""
+    c = {"workload": args.workload, "grid": list(vd["wave grid"][:3]), "propagator": vd.get("propagator", "uppe"),
+         "parallelism": "replicas" if ws > 1 else "single",
+         "l2": f"working set ({working_set_mb(vd):.0f} MB of fields and operator) vs the 129 MB L2"}
+    if getattr(args, "n_perp", None) is not None or getattr(args, "n0", None) is not None:
+        c["reduced"] = "sub-grid of the workload (--n-perp / --n0): a profiling case, not the workload"
+    return c
 
 
 def reference_arm(args, vd, ws, rank):
@@ -546,11 +564,15 @@ def main():
     ap.add_argument("--no-fp32", action="store_true", help="skip the plain FP32 companion rates")
     ap.add_argument("--adjoint-steps", type=int, default=20,
                     help="adjoint (VJP) steps timed for the forward+adjoint rate; 0 to skip")
+    ap.add_argument("--n-perp", type=int, default=None,
+                    help="run the workload on its n x n transverse sub-grid (box scaled): small cases for profiling")
+    ap.add_argument("--n0", type=int, default=None,
+                    help="run the workload with n0 = 2^k + 1 frequencies at the same spacing: small cases for profiling")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     from searay_gb300 import workloads
-    vd = workloads.WORKLOADS[args.workload]()
+    vd = reduced_volume(workloads.WORKLOADS[args.workload](), args.n_perp, args.n0)
     ws, rank, local = dist_env()
     if args.impl == "reference":
         reference_arm(args, vd, ws, rank)
