@@ -210,6 +210,12 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (const char* v = getenv("SEARAY_UPPE_TIME")) {
         if (strcmp(v, "smem") == 0) h->time_reg = 0;
     }
+    // 256 x 256 slices: the three-pass tail; SEARAY_UPPE_CLUSTER=1 selects the cluster-fused tail
+    // (slice_cluster.cu: one launch, 40-48 bytes per point, but measured twice as slow)
+    h->slice_cluster = 0;
+    if (const char* v = getenv("SEARAY_UPPE_CLUSTER")) {
+        if (strcmp(v, "1") == 0) h->slice_cluster = h->slice_big && cluster_slice_supported(c.n1, c.n2);
+    }
     int nt = Nt;
     if (c.n1 > nt) nt = c.n1;
     if (c.n2 > nt) nt = c.n2;

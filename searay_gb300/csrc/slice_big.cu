@@ -62,27 +62,6 @@ __global__ void __launch_bounds__(256)
     }
 }
 
-enum BigColKind {
-    BC_FUSED = 0,    // forward column FFT, RK stage (SPEC_STAGE1/STAGE23/FINISH), next phase, inverse column FFT
-    BC_SPEC = 1,     // forward column FFT, spectral update (SPEC_* modes)
-    BC_REAL = 2,     // pointwise from q (REAL_* modes), inverse column FFT
-    BC_ADJ_IN = 3,   // ADJ_S / ADJ_LOAD pointwise, inverse column FFT (unnormalised)
-    BC_ADJ_FWD = 4,  // forward column FFT, ADJ_E / ADJ_FIN pointwise with 1/S
-    BC_ADJ_STAGE = 5,  // forward column FFT, ADJ_E, the reverse RK bookkeeping and (mode 1) ADJ_S at z1,
-                       // inverse column FFT (the column part of k_adj_fused_reg)
-};
-
-struct BigColArgs {
-    int kind, mode;
-    const float2* src;
-    float2* dst;
-    float2 *q_out, *qf;  // BC_ADJ_STAGE: qf = the accumulated cotangent
-    const float2 *qi, *k1;  // BC_ADJ_STAGE: qi = lam_f
-    float Cs, Ce;           // BC_ADJ_STAGE: a_f, a_mu
-    StepArgs z0, z1;
-    float2* q_store;  // BC_FUSED: also store each stage estimate here (when set)
-};
-
 // The pass kind is a template parameter (one body per kind keeps each kernel's code small).  The
 // adjoint stage kind runs three blocks per multiprocessor (80 registers: more warps hide its operand
 // loads better than the registers it gives up); the forward fused kind keeps 128 registers, two blocks.  In the
@@ -283,7 +262,6 @@ cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepAr
     const int jhi = h->cfg.nl_cut_off;
     const int nfwd = (!h->cfg.envelope && h->cfg.nl_cut_on <= 0 && jhi > 0 && jhi < h->N0) ? jhi : h->N0;
     const int nall = (zs_current && nfwd < h->N0 && jhi >= 4 && !h->stage_q) ? nfwd : h->N0;
-    cudaError_t e = rows<false>(h, h->J, h->J, 1.f, 0, nullptr, nfwd);
     BigColArgs a{};
     a.kind = BC_FUSED;
     a.mode = mode;
@@ -297,6 +275,14 @@ cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepAr
     a.z0 = z_rhs;
     a.z1 = z_next;
     a.q_store = h->stage_q;
+    // 256 x 256 slices with SEARAY_UPPE_CLUSTER=1: the three passes in one launch, the slice held by a
+    // cluster of CTAs (slice_cluster.cu); the three-pass form otherwise or where that cannot run
+    if (h->slice_cluster) {
+        cudaError_t ec = launch_fused_cluster(h, a, nfwd, nall);
+        if (ec != cudaErrorNotSupported) return ec;
+        h->slice_cluster = 0;
+    }
+    cudaError_t e = rows<false>(h, h->J, h->J, 1.f, 0, nullptr, nfwd);
     if (e == cudaSuccess) e = cols(h, a, nall);
     if (e == cudaSuccess) e = rows<true>(h, h->J, h->E, 1.0f / (float)h->S, 0, nullptr, nall);
     return e;

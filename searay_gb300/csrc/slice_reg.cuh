@@ -127,6 +127,29 @@ UPPE_DEV void reg_m2n(float2 (&w)[16], float2 (&v)[16], float2* ex, int j, const
     dft16<INV>(v);
 }
 
+// Kinds and arguments of the column pass of the slices above 128 x 128 (slice_big.cu) and of the
+// cluster-fused tail of 256 x 256 slices (slice_cluster.cu).
+enum BigColKind {
+    BC_FUSED = 0,    // forward column FFT, RK stage (SPEC_STAGE1/STAGE23/FINISH), next phase, inverse column FFT
+    BC_SPEC = 1,     // forward column FFT, spectral update (SPEC_* modes)
+    BC_REAL = 2,     // pointwise from q (REAL_* modes), inverse column FFT
+    BC_ADJ_IN = 3,   // ADJ_S / ADJ_LOAD pointwise, inverse column FFT (unnormalised)
+    BC_ADJ_FWD = 4,  // forward column FFT, ADJ_E / ADJ_FIN pointwise with 1/S
+    BC_ADJ_STAGE = 5,  // forward column FFT, ADJ_E, the reverse RK bookkeeping and (mode 1) ADJ_S at z1,
+                       // inverse column FFT (the column part of k_adj_fused_reg)
+};
+
+struct BigColArgs {
+    int kind, mode;
+    const float2* src;
+    float2* dst;
+    float2 *q_out, *qf;  // BC_ADJ_STAGE: qf = the accumulated cotangent
+    const float2 *qi, *k1;  // BC_ADJ_STAGE: qi = lam_f
+    float Cs, Ce;           // BC_ADJ_STAGE: a_f, a_mu
+    StepArgs z0, z1;
+    float2* q_store;  // BC_FUSED: also store each stage estimate here (when set)
+};
+
 __host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
 
 template <int LN1, int LN2>

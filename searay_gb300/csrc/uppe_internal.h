@@ -58,6 +58,7 @@ struct UppeHandle {
     int slice_reg;                 // Cartesian slices use the register-resident transforms (slice_reg.cuh)
     int slice_big;                 // Cartesian slices above 128 x 128: row and column passes (slice_big.cu)
     int time_reg;                  // TIME_J through the register-resident time pass where it applies (timepass_reg.cu)
+    int slice_cluster;             // 256 x 256 slices: the fused tail in one cluster launch (slice_cluster.cu)
     cudaStream_t stream;
     // library-owned device buffers
     float2 *q, *qi, *qf, *k1, *E, *J, *scratch;
@@ -174,6 +175,11 @@ cudaError_t launch_adj_fused_big(UppeHandle* h, int mode, const float2* g, float
 
 // ---- Cartesian slices of 128 x 256, 256 x 128, 256 x 256 (slice_big.cu): row + column passes ----
 bool big_slice_supported(int N1, int N2);
+struct BigColArgs;
+// the fused tail of 256 x 256 slices in one launch (a cluster of 8 CTAs per slice); returns
+// cudaErrorNotSupported where the cluster form cannot run
+bool cluster_slice_supported(int N1, int N2);
+cudaError_t launch_fused_cluster(UppeHandle* h, const BigColArgs& a, int nfwd, int nall);
 cudaError_t launch_fused_big(UppeHandle* h, int mode, float Cs, float Ce, StepArgs z_rhs, StepArgs z_next,
                              bool zs_current = false);
 cudaError_t launch_real_big(UppeHandle* h, int mode, const float2* src, float2* A_out, const float2* k1, float2* qf,

@@ -126,3 +126,36 @@ def test_big_slice_adjoints_match_torch_fp64(shape):
     for k, e in errs.items():
         assert e < 2e-4, (k, e)
     dev.close()
+
+
+def test_cluster_tail_matches_three_passes(monkeypatch):
+    """256 x 256 slices: the fused evaluation tail on a cluster of 8 CTAs (slice_cluster.cu: the slice
+    in distributed shared memory, one launch) against the three-pass form (rows, columns, inverse
+    rows through HBM, the default) on the same field: three fixed RK4 steps (every stage
+    mode, the slices above the nonlinear cut included) and the finish.  Both run the same line
+    transforms and pointwise arithmetic, so they agree to rounding (1e-6 of the maximum)."""
+    import torch
+    from searay_gb300 import uppe
+    out, launches = {}, {}
+    for form in ("cluster", "passes"):
+        if form == "cluster":
+            monkeypatch.setenv("SEARAY_UPPE_CLUSTER", "1")
+        else:
+            monkeypatch.delenv("SEARAY_UPPE_CLUSTER", raising=False)
+        vd, g, dev, mat, orc = _setup((65, 256, 256))
+        L = vd["size"][2] / 400
+        a_dev = torch.from_numpy(vd["incoming wave"](g.w, g.x1, g.x2).astype(np.complex64)).cuda()
+        l0 = dev.launches()
+        A, J, chi, ne, evals = uppe.propagator(dev, mat, a_dev, 3, 0.0, 3 * L, L)
+        assert evals == 12 and not dev.nonfinite()
+        q = dev.empty_field()
+        dev.get_field(q)
+        out[form] = (A.cpu().numpy(), J.cpu().numpy(), q.cpu().numpy())
+        launches[form] = dev.launches() - l0
+        dev.close()
+    # one launch per evaluation tail instead of three: the cluster form really ran
+    assert launches["passes"] - launches["cluster"] == 2 * 12, launches
+    errs = {k: rel_err(out["cluster"][n], out["passes"][n]) for n, k in enumerate(("A", "J", "q"))}
+    print("cluster vs three passes", {k: f"{v:.2e}" for k, v in errs.items()})
+    for k, e in errs.items():
+        assert e < 1e-6, (k, e)

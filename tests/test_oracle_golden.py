@@ -109,10 +109,11 @@ def test_grid_checks():
 
 
 def test_torch_reference_step_matches_oracle():
-    """The PyTorch FP64 step used to check the adjoint equals the oracle's RK4 step."""
+    """The PyTorch FP64 step used to check the adjoint equals the oracle's RK4 step (with the
+    rotational Raman response on cyl_raman)."""
     import torch
     from torch_reference import TorchStep
-    for name in ("cart_ion", "cyl_kerr"):
+    for name in ("cart_ion", "cyl_kerr", "cyl_raman"):
         vd, _ = replay.load_case(name)
         orc = O.Oracle(vd)
         orc.mat.update(3000.0)

@@ -22,6 +22,7 @@ class TorchStep:
         self.dt = g.dt
         self.Nt = g.Nt
         self.rates = orc.rates
+        self.rotator = orc.rotator
         if not self.cart:
             self.H = t(g.H)
             self.lam = t(g.Lambda)
@@ -65,6 +66,26 @@ class TorchStep:
         c = r.clog
         return r.rate_conv * torch.exp(c[0] + c[1] * L + c[2] * L ** 2 + c[3] * L ** 3 + c[4] * L ** 4 + c[5] * L ** 5)
 
+    def raman_chi(self, Et):
+        """The oracle's raman_chi (AddChiUPPE, kernels/rotations.cl:85-129) with torch operations."""
+        rot = self.rotator
+        Nt = Et.shape[0]
+        Er = torch.flip(Et, [0])
+        F = 0.5 * (rot.dalpha / rot.hbar) * Er ** 2
+        n = torch.arange(Nt, dtype=torch.float64)[:, None, None]
+        chi = torch.zeros_like(Et)
+        for j in range(2, rot.Wj.shape[0]):
+            if rot.Tj[j] == 0.0:
+                continue
+            wdt = complex(rot.Wj[j]) * self.dt
+            S = 2.0 * j * (j - 1) / (15 * (2 * j - 1))
+            h2n = torch.exp(1j * wdt * n)
+            a = F * h2n * np.exp(0.5j * wdt)
+            rho = -1j * self.dt * (torch.cumsum(a, dim=0) - a)
+            term = rot.Tj[j] * S * rho * torch.conj(h2n) * wdt
+            chi = chi + torch.flip(torch.cumsum(2 * term.imag * self.ng[None] * rot.dalpha, dim=0), [0])
+        return chi
+
     def rhs(self, q, z, redchi3):
         E = 1j * self.kz * self.phase(z) * q
         E = self.rspace(E)
@@ -80,6 +101,8 @@ class TorchStep:
             ne = self.ng[None] * (1.0 - torch.exp(-S)) * self.window
             Jw = torch.fft.rfft(ne * Et, dim=0) / (0.1 - 1j * self.w)
         chi = self.ng[None] * redchi3 * Et * Et
+        if self.rotator is not None:  # before the Kerr term, as uppe_kernel.py:174-176
+            chi = self.raman_chi(Et) + chi
         Jw = Jw + (-1j * self.w) * torch.fft.rfft(chi * Et, dim=0)
         Jw = Jw * self.nl
         Jw = self.kspace(Jw)
