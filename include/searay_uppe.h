@@ -139,8 +139,8 @@ int uppe_set_chi3(UppeHandle* h, double chi3_over_nref);
  * term as uppe_kernel.py:173-179 does, by AddChiUPPE, rotations.cl:85-129).  Host arrays of a
  * Rotator's tables, nstates entries: Tj (population differences T_j) and Wj (complex transition
  * frequencies W_j interleaved as re, im), with its dalpha and hbar; transitions j -> j-2 for
- * j >= 2.  nstates = 0 removes the response.  The adjoint entry points refuse a handle with a
- * rotator (UPPE_E_ARG). */
+ * j >= 2.  nstates = 0 removes the response.  The adjoint entry points include it (the transpose
+ * of the Raman map in the adjoint time pass). */
 int uppe_set_rotator(UppeHandle* h, int nstates, const double* Tj, const double* Wj, double dalpha, double hbar);
 
 /* Set the spectral amplitude q directly (a checkpoint restart), device complex64 [N0][N1][N2]. */

@@ -803,10 +803,6 @@ static int ensure_adjoint(UppeHandle* h) {
         uppe_set_error(h, "the adjoint is not built for the paraxial envelope solver");
         return UPPE_E_ARG;
     }
-    if (h->rot_pairs > 0) {
-        uppe_set_error(h, "the adjoint does not include the rotational Raman response (uppe_set_rotator)");
-        return UPPE_E_ARG;
-    }
     if (h->adj_mu) return UPPE_OK;
     // Only buffers still missing are allocated, so a call after a failed allocation neither leaks
     // nor reallocates; adj_mu, the "allocated" mark, comes last, after the scalar dred_d.

@@ -323,5 +323,69 @@ __device__ __forceinline__ void raman_pass(const TimeParams& tp, const float4* R
 }
 
 
+// Transpose of raman_pass: the cotangent of the drive F of this thread's SPT consecutive samples
+// (t ascending, index i = t - t0) from the cotangent ybar of the Raman susceptibility at the same
+// samples.  With p_n = h^{2n+1}, n = Nt - 1 - t the reference's time order, the forward map is
+//     chi_n = sum_{n' <= n} g_{n'},   g_n = ng Im(cq conj(p_n) R_n),   R_n = sum_{m < n} F_m p_m,
+// so, with gbar_n = sum_{n' >= n} ybar_{n'} (a prefix sum along t), its transpose is
+//     Fbar_m = ng Im(cq p_m W_m),   W_m = sum_{n > m} gbar_n conj(p_n)   (a prefix sum along t).
+// Per transition: the segment's sum of gbar conj(p) as conj(p0) sum_i gbar_i conj(h^{2i'}) (i' the
+// position in the reference's order, the powers and p0 from the same tables as raman_pass), the sums of
+// the earlier segments give W at the segment's first sample, then a running sum along t.  The prefix
+// sum of ybar is float-float in the mixed form; the transition sums are FP32, as in raman_pass.
+template <int SPT>
+__device__ __forceinline__ void raman_adjoint_pass(const TimeParams& tp, const float4* Rs, ffloat* tot, int C,
+                                                   int logC, int T, int tid, int seg, float ngc,
+                                                   const float (&ybar)[SPT], float (&Fbar)[SPT]) {
+    const int nseg = T >> logC;
+    const int plain = tp.plain;
+    // gbar(t) = sum_{t' <= t} ybar(t')
+    ffloat part = {0.f, 0.f};
+#pragma unroll
+    for (int i = 0; i < SPT; ++i) acc_add(part, ybar[i], plain);
+    ffloat run = earlier_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, [plain](ffloat x, ffloat y) {
+        if (plain) return ffloat{x.hi + y.hi, 0.f};
+        return ff_add(x, y);
+    });
+    float gbar[SPT];
+#pragma unroll
+    for (int i = 0; i < SPT; ++i) {
+        acc_add(run, ybar[i], plain);
+        gbar[i] = ff_value(run);
+        Fbar[i] = 0.f;
+    }
+    float4* tot4 = reinterpret_cast<float4*>(tot);
+    const auto add4 = [](float4 x, float4 y) { return make_float4(x.x + y.x, x.y + y.y, x.z + y.z, x.w + y.w); };
+    for (int r = 0; r < tp.rot_pairs; ++r) {
+        const float4* Rp = Rs + 20 * r;
+        const float4 p0 = __ldg(&tp.rot_p0[(size_t)r * nseg + seg]);  // {re A, re B, im A, im B}
+        const float4 cq4 = Rp[2];
+        // segment sums of gbar conj(p), p(i) = p0 h^{2 i'}, i' = SPT - 1 - i, both transitions of the pair
+        float2 sA = make_float2(0.f, 0.f), sB = sA;
+#pragma unroll
+        for (int i = 0; i < SPT; ++i) {
+            const float4 H = Rp[4 + (SPT - 1 - i)];
+            const float2 pA = cmul(make_float2(p0.x, p0.z), make_float2(H.x, H.z));
+            const float2 pB = cmul(make_float2(p0.y, p0.w), make_float2(H.y, H.w));
+            sA = cadd(sA, cscale(cconj(pA), gbar[i]));
+            sB = cadd(sB, cscale(cconj(pB), gbar[i]));
+        }
+        const float4 Wc = earlier_segments_sum(make_float4(sA.x, sB.x, sA.y, sB.y), make_float4(0.f, 0.f, 0.f, 0.f),
+                                               tot4, C, logC, T, tid, add4);
+        float2 WA = make_float2(Wc.x, Wc.z), WB = make_float2(Wc.y, Wc.w);
+        const float2 cqA = make_float2(cq4.x, cq4.z), cqB = make_float2(cq4.y, cq4.w);
+#pragma unroll
+        for (int i = 0; i < SPT; ++i) {
+            const float4 H = Rp[4 + (SPT - 1 - i)];
+            const float2 pA = cmul(make_float2(p0.x, p0.z), make_float2(H.x, H.z));
+            const float2 pB = cmul(make_float2(p0.y, p0.w), make_float2(H.y, H.w));
+            Fbar[i] += ngc * (cmul(cqA, cmul(pA, WA)).y + cmul(cqB, cmul(pB, WB)).y);
+            WA = cadd(WA, cscale(cconj(pA), gbar[i]));
+            WB = cadd(WB, cscale(cconj(pB), gbar[i]));
+        }
+    }
+    __syncthreads();  // `tot` is reused by the caller
+}
+
 // Host: the time-pass parameters of a handle (timepass.cu).
 TimeParams uppe_time_params(const UppeHandle* h);

@@ -489,8 +489,12 @@ __device__ __noinline__ void adj_inverse_fft_ct(float2* Z, const float2* twl, in
     fft_axis_ct<8, LOGM, LOGC, LOGM + 1>(Z, TwHalfSharedCT<LOGM + 1>{twl}, true, tid);
 }
 
-template <int LOGM = 0, int LOGC = -1>
-__global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time_adj(const float2* __restrict__ E,
+// RAMAN = 1 adds the rotational Raman response (the handle has a rotator): chi_R is recomputed by
+// raman_pass and its transpose applied by raman_adjoint_pass; their contribution to the cotangent of
+// e(t), chi_R gp + (dF/de) Fbar, goes to a fifth array Zr [M][C] that step 4 adds.  The segment totals
+// then take 2T entries (float4 carries), and the pair tables Rs follow Zr.
+template <int LOGM = 0, int LOGC = -1, int RAMAN = 0>
+__global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 3 : 1)) k_time_adj(const float2* __restrict__ E,
                                                                    const float2* __restrict__ G,
                                                                    float2* __restrict__ gE,
                                                                    const float* __restrict__ ng,
@@ -511,6 +515,8 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
     ffloat* tot = reinterpret_cast<ffloat*>(twl + (Nt >> 1));
     __shared__ double red_sh[32];
     const int tid = threadIdx.x, T = CT ? ((2 << LOGM) << LOGC) / 16 : (int)blockDim.x;
+    float2* Zr = reinterpret_cast<float2*>(tot + 2 * T);  // RAMAN only
+    float4* Rs = reinterpret_cast<float4*>(Zr + (((size_t)M * C + 1) & ~(size_t)1));
     const size_t col0 = (size_t)blockIdx.x * C;
     const bool ionize = tp.rate_form != UPPE_RATE_NONE;
     const TwHalfShared tws{twl, tp.logNt};
@@ -529,6 +535,8 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
         cp_async8(&Zn[sw(k) * C + c], &E[(size_t)k * S + col0 + c]);
         cp_async8(&Zl[sw(k) * C + c], &G[(size_t)k * S + col0 + c]);
     }
+    if constexpr (RAMAN != 0)
+        for (int i = tid; i < 20 * tp.rot_pairs; i += T) cp_async16_time(&Rs[i], &tp.rot_tab[i]);
     asm volatile("cp.async.commit_group;\n" ::);
     for (int j = tid; j < (Nt >> 1); j += T) twl[j] = __ldg(&tw[j << (twLog - tp.logNt)]);
     asm volatile("cp.async.wait_group 0;\n" ::);
@@ -558,6 +566,36 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
         if (plain) return ffloat{x.hi + y.hi, 0.f};
         return ff_add(x, y);
     };
+    if constexpr (RAMAN != 0) {
+        // chi_R of this thread's 16 samples (the forward's raman_pass on e), then the transpose of the
+        // Raman map applied to ybar = gp e (P = chi e); Zr gets chi_R gp + (dF/de) Fbar with the
+        // drive F = z^2 of the unnormalised field z = Nt e, dF/de = 2 Nt z
+        float chiR[16], ybar[16], Fbar[16];
+        raman_pass<16, false>(
+            tp, Rs, tot, C, logC, T, tid, seg, ngc,
+            [&](int k) {
+                const float2 zv = Ze[sw(m0 + k) * C + c];
+                return make_float2(zv.x * zv.x, zv.y * zv.y);
+            },
+            [&](int k, float chi0, float chi1) {
+                chiR[2 * k] = chi0;
+                chiR[2 * k + 1] = chi1;
+            });
+#pragma unroll
+        for (int k = 0; k < MPS; ++k) {
+            const float2 zv = Ze[sw(m0 + k) * C + c], gv = Zp[sw(m0 + k) * C + c];
+            ybar[2 * k] = gv.x * zv.x * inv;
+            ybar[2 * k + 1] = gv.y * zv.y * inv;
+        }
+        raman_adjoint_pass<16>(tp, Rs, tot, C, logC, T, tid, seg, ngc, ybar, Fbar);
+        const float two_nt = 2.f * (float)Nt;
+#pragma unroll
+        for (int k = 0; k < MPS; ++k) {
+            const float2 zv = Ze[sw(m0 + k) * C + c], gv = Zp[sw(m0 + k) * C + c];
+            Zr[sw(m0 + k) * C + c] = make_float2(fmaf(chiR[2 * k], gv.x, two_nt * zv.x * Fbar[2 * k]),
+                                                 fmaf(chiR[2 * k + 1], gv.y, two_nt * zv.y * Fbar[2 * k + 1]));
+        }
+    }
     // With no nonzero rate anywhere in the block the density, the plasma-current cotangent and the
     // rate-derivative terms are all zero: `ion` leaves them out (and the inverse FFT of gpl).
     bool ion = false;
@@ -634,7 +672,8 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
             float ge[2];
             const float ev[2] = {e2.x * inv, e2.y * inv};
             const float gp[2] = {p2.x, p2.y};
-            float2 l2 = make_float2(0.f, 0.f), s2 = l2;
+            float2 l2 = make_float2(0.f, 0.f), s2 = l2, r2 = l2;
+            if constexpr (RAMAN != 0) r2 = Zr[sw(m) * C + c];
             if (ion) {
                 l2 = Zl[sw(m) * C + c];
                 s2 = Zn[sw(m) * C + c];
@@ -643,7 +682,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, LOGM > 0 ? 3 : 1) k_time
             for (int h = 0; h < 2; ++h) {
                 const int t = 2 * m + h;
                 const float e = ev[h];
-                float g = 3.f * kerr * e * e * gp[h];
+                float g = 3.f * kerr * e * e * gp[h] + (h ? r2.y : r2.x);
                 dred_part = fmaf(gp[h] * ngc * e * e, e, dred_part);
                 if (ion) {
                     const float gl = h ? l2.y : l2.x;
@@ -707,6 +746,8 @@ cudaError_t uppe_configure_time_adj_kernel(size_t smem_bytes) {
         e = cudaFuncSetAttribute(k_time_adj<A_, B_>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     UPPE_TIME_ADJ_CT(UPPE_TIME_ADJ_CONF)
 #undef UPPE_TIME_ADJ_CONF
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(k_time_adj<0, -1, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes);
     return e;
 }
 
@@ -731,6 +772,15 @@ cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G,
     const size_t smem = ((size_t)(h->M + 1) * 4 * Ca + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
     const int nblk = h->S / Ca;
     h->launches++;
+    if (h->rot_pairs > 0) {  // the Raman response: 2T segment totals, Zr [M][C] (even length), the pair tables
+        const size_t zr = (((size_t)h->M * Ca + 1) & ~(size_t)1) * sizeof(float2);
+        const size_t smem_r = ((size_t)(h->M + 1) * 4 * Ca + h->Nt / 2) * sizeof(float2) +
+                              (size_t)2 * T * sizeof(ffloat) + zr + (size_t)20 * h->rot_pairs * sizeof(float4);
+        if (smem_r > 224 * 1024) return cudaErrorInvalidValue;
+        k_time_adj<0, -1, 1><<<nblk, T, smem_r, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp,
+                                                          dred);
+        return cudaGetLastError();
+    }
 #define UPPE_TIME_ADJ_CASE(A_, B_)                                                                              \
     if (tp.logM == A_ && tp.logC == B_) {                                                                       \
         k_time_adj<A_, B_><<<nblk, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred); \

@@ -29,6 +29,7 @@ def _setup(name, precision, zmat):
     g = grid.VolumeGrid(vd)
     rates = ionization.RateCoefficients(vd["ionizer"]) if vd.get("ionizer") else None
     dev = uppe.DeviceGrid(g, vd, rates, precision)
+    dev.set_rotator(vd.get("rotator"))
     chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
     mat = uppe.Material(dev, g, vd["wave coordinates"], None, chi, vd.get("chi3", 0.0), vd["density reference"],
                         vd.get("window speed", 1.0), vd["density lambda"])
@@ -40,7 +41,7 @@ def _setup(name, precision, zmat):
 
 # tolerance of the VJP: FP32 transforms 2e-4, the tensor-core Hankel transform of the mixed form 2e-3
 @pytest.mark.parametrize("name,precision", [("cart_ion", "mixed"), ("cart_series", "fp32"), ("cyl_kerr", "fp32"),
-                                            ("cyl_kerr", "mixed")])
+                                            ("cyl_kerr", "mixed"), ("cyl_raman", "fp32"), ("cyl_raman", "mixed")])
 def test_vjp_of_rk4_step_matches_torch_fp64(name, precision):
     import torch
     from torch_reference import TorchStep

@@ -140,16 +140,56 @@ def test_raman_changes_chi_and_can_be_removed():
     assert share > 0.02
 
 
-def test_adjoint_refuses_rotator():
+@pytest.mark.parametrize("shape,precision", [((129, 16, 16), "mixed"), ((1025, 16, 8), "fp32"), ((4097, 4, 4), "mixed")],
+                         ids=["129x16x16", "1025x16x8", "4097x4x4"])
+def test_adjoint_with_rotator_matches_torch_fp64(shape, precision):
+    """The vector-Jacobian product of one RK4 step with the rotational Raman response (the transpose
+    of AddChiUPPE, rotations.cl:85-129, in the adjoint time pass) and ionization, against FP64 torch
+    autograd of the same step (tests/torch_reference.py, which carries the oracle's raman_chi), at
+    16, 4 and 1 transverse points per block of the adjoint time pass.  The rotator's polarizability
+    difference is raised 100-fold (the Raman chi grows with its square) so that the Raman response
+    carries a measurable part of the VJP.  Checked: the VJP (2e-4, the tolerance of the FP32
+    transforms) and, separately, the Raman part of it, the difference between the VJPs with and
+    without the rotator, on the GPU and in torch (2e-3 of its maximum)."""
     import torch
-    from searay_gb300 import uppe
-    vd, g, dev, mat = _setup((65, 16, 16), n2_rotator(), ionize=False)
-    mat.UpdateMaterial(10.0)
-    q = dev.empty_field()
-    lam = dev.empty_field()
-    out = dev.empty_field()
-    q.zero_()
-    lam.zero_()
-    with pytest.raises(RuntimeError, match="Raman"):
-        dev.adjoint_step(q, lam, out, 0.0, 10.0)
+    from oracle import uppe_oracle as O
+    from torch_reference import TorchStep
+    rot = n2_rotator()
+    rot.dalpha *= 100.0
+    vd, g, dev, mat = _setup(shape, rot, precision=precision)
+    zmat = 100.0
+    mat.UpdateMaterial(zmat)
+    orc = O.Oracle(vd)
+    assert orc.rotator is rot
+    orc.mat.update(zmat)
+    ts = TorchStep(orc)
+    redchi3 = vd["chi3"] / vd["density reference"]
+    q0 = orc.g.kspace(vd["incoming wave"](g.w, g.x1, g.x2))
+    rng = np.random.default_rng(13)
+    lam = (rng.standard_normal(q0.shape) + 1j * rng.standard_normal(q0.shape)) * (np.abs(q0) + 1e-3 * np.abs(q0).max())
+    z, dz = 50.0, vd["size"][2] / 400
+    q0d = torch.from_numpy(q0.astype(np.complex64)).cuda()
+    lamd = torch.from_numpy(lam.astype(np.complex64)).cuda()
+    ref, gpu = {}, {}
+    for with_raman in (True, False):
+        ts.rotator = rot if with_raman else None
+        x = torch.tensor(q0.real, requires_grad=True)
+        y = torch.tensor(q0.imag, requires_grad=True)
+        c3 = torch.tensor(redchi3, dtype=torch.float64, requires_grad=True)
+        q1 = ts.step(torch.complex(x, y), z, dz, c3)
+        (torch.as_tensor(lam).conj() * q1).real.sum().backward()
+        ref[with_raman] = (x.grad.numpy() + 1j * y.grad.numpy(), float(c3.grad))
+        dev.set_rotator(rot if with_raman else None)
+        out = dev.empty_field()
+        dred = dev.adjoint_step(q0d, lamd, out, z, dz)
+        gpu[with_raman] = (out.cpu().numpy(), dred)
+    e = rel_err(gpu[True][0], ref[True][0])
+    ed = abs(gpu[True][1] - ref[True][1]) / abs(ref[True][1])
+    d_ref = ref[True][0] - ref[False][0]
+    d_gpu = gpu[True][0].astype(np.complex128) - gpu[False][0]
+    share = np.max(np.abs(d_ref)) / np.max(np.abs(ref[True][0]))
+    er = rel_err(d_gpu, d_ref)
+    print(shape, precision, f"vjp {e:.2e} dchi3 {ed:.2e}; Raman part {er:.2e} (share of the VJP {share:.2e})")
+    assert e < 2e-4 and ed < 2e-4
+    assert share > 5e-3 and er < 2e-3
     dev.close()
