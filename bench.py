@@ -408,7 +408,10 @@ def oracle_run(v, min_seconds=0.0, max_steps=1, outputs=False):
             q1 = q
     out = None
     if outputs:
-        out = orc.finish(q1, dz)
+        if env:  # the envelope solver's step is adaptive (no minimum step): its own propagator, ascending w
+            out = orc.propagator(a, 0.0, dz, 1)[:4]
+        else:
+            out = orc.finish(q1, dz)
     return tot, steps, int(np.prod(g.N[:3])), g.N, out
 
 
