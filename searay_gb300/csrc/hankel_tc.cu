@@ -20,13 +20,9 @@
 #include <vector>
 
 #include "common.cuh"
+#include "hankel_tc.cuh"
 #include "uppe_internal.h"
 
-#define TC_ROWS 128  // MMA rows per tile (64 frequencies x re/im)
-#define TC_W 64      // frequencies per tile
-#define TC_N 128     // output columns per tile
-#define TC_K 64      // reduction elements per shared tile (four K=16 MMAs)
-#define TC_TILE_BYTES (TC_ROWS * TC_K * 2)  // 16 KB per bf16 operand tile
 #define TC_STAGE_LD (TC_N + 1)              // padded row of the epilogue staging tile (float2)
 #define TC_WAIT_LIMIT (1 << 24)
 
@@ -50,13 +46,6 @@ struct TcArgs {
     StepArgs z;
     int* err;
 };
-
-// Byte offset of element (row, k) of a 128 x 64 bf16 tile in the K-major, no-swizzle canonical
-// layout: 8x8 core matrices of 128 contiguous bytes (8 rows of 16 bytes); core matrices adjacent in
-// K are 128 bytes apart (leading byte offset), adjacent in M/N 1024 bytes apart (stride byte offset).
-__device__ __forceinline__ uint32_t core_off(int row, int k) {
-    return (uint32_t)((row >> 3) * 1024 + (k >> 3) * 128 + (row & 7) * 16 + (k & 7) * 2);
-}
 
 // Shared-memory matrix descriptor of tcgen05 (start address, LBO, SBO in 16-byte units; version 1;
 // no swizzle).
@@ -88,11 +77,6 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, int* er
     }
     if (err) atomicExch(err, 1);
     return false;
-}
-
-__device__ __forceinline__ void split_bf16(float x, __nv_bfloat16& hi, __nv_bfloat16& lo) {
-    hi = __float2bfloat16_rn(x);
-    lo = __float2bfloat16_rn(x - __bfloat162float(hi));
 }
 
 #define TC_THREADS 512  // 16 warps: the copies and the fused epilogue are spread over more threads
@@ -161,16 +145,7 @@ __global__ void __launch_bounds__(256) k_hankel_tc_prep(TcArgs g, uint8_t* __res
             if (AMODE == TA_QPHASE_IKZ) v = op_field(g.op, o, v);
         }
     }
-    __nv_bfloat16 rh, rl, ih, il;
-    split_bf16(v.x, rh, rl);
-    split_bf16(v.y, ih, il);
-    const int wl = w % TC_W, kk = k % TC_K;
-    uint8_t* tile = Atc + (((size_t)m * g.nwt + w / TC_W) * g.nkt + k / TC_K) * (size_t)(2 * TC_TILE_BYTES);
-    const uint32_t ore = core_off(2 * wl, kk), oim = core_off(2 * wl + 1, kk);
-    *reinterpret_cast<__nv_bfloat16*>(tile + ore) = rh;
-    *reinterpret_cast<__nv_bfloat16*>(tile + oim) = ih;
-    *reinterpret_cast<__nv_bfloat16*>(tile + TC_TILE_BYTES + ore) = rl;
-    *reinterpret_cast<__nv_bfloat16*>(tile + TC_TILE_BYTES + oim) = il;
+    tc_store_split(Atc, g.nwt, g.nkt, m, w, k, v);
 }
 
 // The GEMM of one output tile (64 frequencies x 128 columns) on pre-split operand tiles (AMODE =
@@ -392,9 +367,20 @@ cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* 
     a.err = h->dev_err;
     a.nwt = (h->N0 + TC_W - 1) / TC_W;
     a.Atc = h->Atc;
-    // the A operand once per transform (k_hankel_tc_prep), then the GEMM on pre-split tiles
+    // the A operand once per transform (k_hankel_tc_prep), then the GEMM on pre-split tiles.  The
+    // inverse transform of a stage estimate finds its operand already written when the spectral
+    // update that produced the estimate was asked for it (k_spec_point with a TcNext): same source,
+    // same z, no transform in between (atc_next is cleared by every other use of the tiles).
     if (!h->Atc || (size_t)h->N2 * a.nwt * a.nkt * 2 * TC_TILE_BYTES > h->Atc_bytes) return cudaErrorInvalidValue;
-    {
+    // Likewise the forward transform of J finds its operand written by the time pass that formed J.
+    const bool ready_inv = amode == TA_QPHASE_IKZ && which == 1 && h->atc_next && h->atc_next_src == A &&
+                           h->atc_next_z.zhi == z.zhi && h->atc_next_z.zlo == z.zlo &&
+                           h->atc_next_z.plain == z.plain;
+    const bool ready_fwd = amode == TA_PLAIN && which == 0 && h->atc_fwd && A == h->J;
+    const bool ready = ready_inv || ready_fwd;
+    h->atc_next = 0;
+    h->atc_fwd = 0;
+    if (!ready) {
         const size_t n = (size_t)a.nwt * TC_W * a.nkt * TC_K;
         dim3 grid((unsigned)((n + 255) / 256), h->N2);
         h->launches++;
@@ -415,6 +401,18 @@ cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* 
     if (cmode == TC_QADJ) return run_tc<TA_PRESPLIT, TC_QADJ>(h, a);
     if (cmode == TC_FADJ) return run_tc<TA_PRESPLIT, TC_FADJ>(h, a);
     return cudaErrorInvalidValue;
+}
+
+// The operand of the next inverse transform, for the spectral update that writes it (N2 = 1): the
+// tile counts of the Minv transform and its z.
+TcNext hankel_tc_next(const UppeHandle* h, StepArgs z_next) {
+    TcNext nx;
+    nx.Atc = h->Atc;
+    nx.nwt = (h->N0 + TC_W - 1) / TC_W;
+    nx.nkt = (h->Nk + TC_K - 1) / TC_K;
+    nx.Nk = h->Nk;
+    nx.z = z_next;
+    return nx;
 }
 
 // Bytes of the pre-split A tiles for the transforms of a handle (reduction length up to N1).

@@ -23,6 +23,10 @@ struct TimeParams {
     int rot_pairs;
     const float4* rot_tab;
     const float4* rot_p0;
+    // TIME_J with atc set: J goes straight into the split operand tiles of the forward tensor-core
+    // Hankel transform (hankel_tc.cuh, azimuthal mode 0) instead of out0
+    uint8_t* atc;
+    int atc_nwt, atc_nkt;
 };
 
 #define UPPE_LN2 0.69314718055994530942f

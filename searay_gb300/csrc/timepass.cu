@@ -19,6 +19,7 @@
 
 #include "common.cuh"
 #include "fft_smem.cuh"
+#include "hankel_tc.cuh"
 #include "time_common.cuh"
 #include "uppe_internal.h"
 
@@ -259,7 +260,10 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
                 const float rden = __frcp_rn(fmaf(wk, wk, tp.damping * tp.damping));
                 J = cadd(J, cscale(cmul(Q, make_float2(tp.damping, wk)), rden));
             }
-            out0[o] = cscale(J, filt[k]);
+            if (tp.atc)
+                tc_store_split(tp.atc, tp.atc_nwt, tp.atc_nkt, 0, k, (int)(col0 + cc), cscale(J, filt[k]));
+            else
+                out0[o] = cscale(J, filt[k]);
         } else {
             if (out0) out0[o] = P;
             if (out1) out1[o] = ionize ? Q : make_float2(0.f, 0.f);
@@ -319,6 +323,13 @@ TimeParams uppe_time_params(const UppeHandle* h) {
     tp.rot_pairs = h->rot_pairs;
     tp.rot_tab = reinterpret_cast<const float4*>(h->rot);
     tp.rot_p0 = reinterpret_cast<const float4*>(h->rot + 80 * h->rot_pairs);
+    tp.atc = nullptr;
+    tp.atc_nwt = tp.atc_nkt = 0;
+    if (h->time_atc && h->Atc) {
+        tp.atc = h->Atc;
+        tp.atc_nwt = (h->N0 + TC_W - 1) / TC_W;
+        tp.atc_nkt = (h->N1 + TC_K - 1) / TC_K;
+    }
     tp.em_min = 0.f;
     if (c.rate_form != UPPE_RATE_NONE) {
         // log2(rate) as a function of Em (atomic units); it rises from -inf at Em -> 0 for physical
@@ -501,7 +512,8 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
                                                                    const float* __restrict__ wv,
                                                                    const float* __restrict__ filt,
                                                                    const float2* __restrict__ tw, int twLog,
-                                                                   TimeParams tp, double* dred) {
+                                                                   TimeParams tp, double* dred,
+                                                                   const int* __restrict__ list) {
     extern __shared__ float2 sa[];
     constexpr bool CT = LOGM > 0;
     const int C = CT ? (1 << LOGC) : tp.C, logC = CT ? LOGC : tp.logC;
@@ -517,7 +529,6 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
     const int tid = threadIdx.x, T = CT ? ((2 << LOGM) << LOGC) / 16 : (int)blockDim.x;
     float2* Zr = reinterpret_cast<float2*>(tot + 2 * T);  // RAMAN only
     float4* Rs = reinterpret_cast<float4*>(Zr + (((size_t)M * C + 1) & ~(size_t)1));
-    const size_t col0 = (size_t)blockIdx.x * C;
     const bool ionize = tp.rate_form != UPPE_RATE_NONE;
     const TwHalfShared tws{twl, tp.logNt};
     const RowSwizzle sw{logC <= 2 ? M - 1 : 0, logC == 0 ? 4 : 3};
@@ -528,211 +539,224 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
             fft_axis_tw<8>(Z, tp.logM, logC, 1, C, tws, true, tid, T, -1, sw);
     };
 
-    // ---- 1. stage E and G, recompute e(t), form the transposed-rfft inputs ----
-    for (int it = tid; it < R; it += T) {
-        const int c = it & (C - 1);
-        const int k = it >> logC;
-        cp_async8(&Zn[sw(k) * C + c], &E[(size_t)k * S + col0 + c]);
-        cp_async8(&Zl[sw(k) * C + c], &G[(size_t)k * S + col0 + c]);
-    }
-    if constexpr (RAMAN != 0)
-        for (int i = tid; i < 20 * tp.rot_pairs; i += T) cp_async16_time(&Rs[i], &tp.rot_tab[i]);
-    asm volatile("cp.async.commit_group;\n" ::);
-    for (int j = tid; j < (Nt >> 1); j += T) twl[j] = __ldg(&tw[j << (twLog - tp.logNt)]);
-    asm volatile("cp.async.wait_group 0;\n" ::);
-    __syncthreads();
-    pack_half_spectrum(Ze, C, logC, M, tws, [&](int k, int c) { return Zn[sw(k) * C + c]; }, tid, T, sw);
-    // Gp_k = W_k filt_k (i w_k) G_k ; Gl_k = W_k filt_k G_k / (0.1 + i w_k), W = 1/2 inside the band
-    pack_half_spectrum(Zp, C, logC, M, tws, [&](int k, int c) {
-        const float wk = wv[k];
-        const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
-        return cscale(cmul_i(Zl[sw(k) * C + c]), wk * wt * filt[k]);
-    }, tid, T, sw);
-    __syncthreads();
-    inv_fft(Ze);
-    inv_fft(Zp);
-
-    // ---- 2. forward sources along t (rates and the density exponent S), as in k_time ----
-    const int c = tid & (C - 1);
-    const int seg = tid >> logC;
-    constexpr int MPS = 8;  // packed pairs (16 samples) per thread
-    const int m0 = seg * MPS;
-    const int t1 = 2 * (m0 + MPS);
-    const float ngc = ng[col0 + c];
-    const float kerr = ngc * tp.redchi3;
-    const float inv = tp.inv_nt;
-    const int plain = tp.plain;
-    const auto ffsum = [plain](ffloat x, ffloat y) {
-        if (plain) return ffloat{x.hi + y.hi, 0.f};
-        return ff_add(x, y);
-    };
-    if constexpr (RAMAN != 0) {
-        // chi_R of this thread's 16 samples (the forward's raman_pass on e), then the transpose of the
-        // Raman map applied to ybar = gp e (P = chi e); Zr gets chi_R gp + (dF/de) Fbar with the
-        // drive F = z^2 of the unnormalised field z = Nt e, dF/de = 2 Nt z
-        float chiR[16], ybar[16], Fbar[16];
-        raman_pass<16, false>(
-            tp, Rs, tot, C, logC, T, tid, seg, ngc,
-            [&](int k) {
-                const float2 zv = Ze[sw(m0 + k) * C + c];
-                return make_float2(zv.x * zv.x, zv.y * zv.y);
-            },
-            [&](int k, float chi0, float chi1) {
-                chiR[2 * k] = chi0;
-                chiR[2 * k + 1] = chi1;
-            });
-#pragma unroll
-        for (int k = 0; k < MPS; ++k) {
-            const float2 zv = Ze[sw(m0 + k) * C + c], gv = Zp[sw(m0 + k) * C + c];
-            ybar[2 * k] = gv.x * zv.x * inv;
-            ybar[2 * k + 1] = gv.y * zv.y * inv;
+    // One column group per pass of the loop: blockIdx.x alone, or (list != NULL) the groups list[1 ..
+    // list[0]] taken in turn by the blocks of a smaller grid.
+    for (int gi = (int)blockIdx.x;; gi += (int)gridDim.x) {
+        size_t col0;
+        if (list) {
+            if (gi >= list[0]) break;
+            col0 = (size_t)list[1 + gi] * C;
+        } else {
+            if (gi != (int)blockIdx.x) break;
+            col0 = (size_t)blockIdx.x * C;
         }
-        raman_adjoint_pass<16>(tp, Rs, tot, C, logC, T, tid, seg, ngc, ybar, Fbar);
-        const float two_nt = 2.f * (float)Nt;
-#pragma unroll
-        for (int k = 0; k < MPS; ++k) {
-            const float2 zv = Ze[sw(m0 + k) * C + c], gv = Zp[sw(m0 + k) * C + c];
-            Zr[sw(m0 + k) * C + c] = make_float2(fmaf(chiR[2 * k], gv.x, two_nt * zv.x * Fbar[2 * k]),
-                                                 fmaf(chiR[2 * k + 1], gv.y, two_nt * zv.y * Fbar[2 * k + 1]));
+        // ---- 1. stage E and G, recompute e(t), form the transposed-rfft inputs ----
+        for (int it = tid; it < R; it += T) {
+            const int c = it & (C - 1);
+            const int k = it >> logC;
+            cp_async8(&Zn[sw(k) * C + c], &E[(size_t)k * S + col0 + c]);
+            cp_async8(&Zl[sw(k) * C + c], &G[(size_t)k * S + col0 + c]);
         }
-    }
-    // With no nonzero rate anywhere in the block the density, the plasma-current cotangent and the
-    // rate-derivative terms are all zero: `ion` leaves them out (and the inverse FFT of gpl).
-    bool ion = false;
-    float r_next = 0.f;
-    ffloat part = {0.f, 0.f};
-    if (ionize) {
-        if (t1 <= Nt - 2) r_next = ion_rate(tp, Ze[sw(t1 >> 1) * C + c].x * inv);
-        float rn = r_next;
-        bool live = r_next != 0.f;
-#pragma unroll 1
-        for (int j = MPS - 1; j >= 0; --j) {
-            const int m = m0 + j;
-            const float2 zv = Ze[sw(m) * C + c];
-            const int t = 2 * m + 1;
-            const float r1 = (t == Nt - 1) ? 0.f : ion_rate(tp, zv.y * inv);
-            if (t <= Nt - 2) acc_add(part, tp.hdt * (r1 + rn), tp.plain);
-            const float r0 = ion_rate(tp, zv.x * inv);
-            acc_add(part, tp.hdt * (r0 + r1), tp.plain);
-            live = live || r0 != 0.f || r1 != 0.f;
-            rn = r0;
-            Zn[sw(m) * C + c] = make_float2(r0, r1);
-        }
-        ion = __syncthreads_or(live ? 1 : 0) != 0;
-    }
-    if (ion) {
-        ffloat Sacc = later_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
-        float rn = r_next;
-#pragma unroll 1
-        for (int j = MPS - 1; j >= 0; --j) {
-            const int m = m0 + j;
-            const float2 rr = Zn[sw(m) * C + c];
-            const int t = 2 * m + 1;
-            if (t <= Nt - 2) acc_add(Sacc, tp.hdt * (rr.y + rn), tp.plain);
-            const float S1 = ff_value(Sacc);
-            acc_add(Sacc, tp.hdt * (rr.x + rr.y), tp.plain);
-            rn = rr.x;
-            Zn[sw(m) * C + c] = make_float2(ff_value(Sacc), S1);
-        }
-        // Gl over the raw G, which Zl has held since staging (its pack reads every G it overwrites)
-        pack_half_spectrum(Zl, C, logC, M, tws, [&](int k, int c) {
+        if constexpr (RAMAN != 0)
+            for (int i = tid; i < 20 * tp.rot_pairs; i += T) cp_async16_time(&Rs[i], &tp.rot_tab[i]);
+        asm volatile("cp.async.commit_group;\n" ::);
+        for (int j = tid; j < (Nt >> 1); j += T) twl[j] = __ldg(&tw[j << (twLog - tp.logNt)]);
+        asm volatile("cp.async.wait_group 0;\n" ::);
+        __syncthreads();
+        pack_half_spectrum(Ze, C, logC, M, tws, [&](int k, int c) { return Zn[sw(k) * C + c]; }, tid, T, sw);
+        // Gp_k = W_k filt_k (i w_k) G_k ; Gl_k = W_k filt_k G_k / (0.1 + i w_k), W = 1/2 inside the band
+        pack_half_spectrum(Zp, C, logC, M, tws, [&](int k, int c) {
             const float wk = wv[k];
             const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
-            const float rden = __frcp_rn(fmaf(wk, wk, tp.damping * tp.damping));
-            return cscale(cmul(Zl[sw(k) * C + c], make_float2(tp.damping, -wk)), rden * wt * filt[k]);
+            return cscale(cmul_i(Zl[sw(k) * C + c]), wk * wt * filt[k]);
         }, tid, T, sw);
-        __syncthreads();  // the packed Gl is complete; the segment totals are reused below
-        inv_fft(Zl);
-    }
+        __syncthreads();
+        inv_fft(Ze);
+        inv_fft(Zp);
 
-    // ---- 3. transposed scan: Pfx(j) = sum_{t <= j} gpl e a, a = ng w exp(-S), increasing t ----
-    ffloat carry = {0.f, 0.f};
-    if (ion) {
+        // ---- 2. forward sources along t (rates and the density exponent S), as in k_time ----
+        const int c = tid & (C - 1);
+        const int seg = tid >> logC;
+        constexpr int MPS = 8;  // packed pairs (16 samples) per thread
+        const int m0 = seg * MPS;
+        const int t1 = 2 * (m0 + MPS);
+        const float ngc = ng[col0 + c];
+        const float kerr = ngc * tp.redchi3;
+        const float inv = tp.inv_nt;
+        const int plain = tp.plain;
+        const auto ffsum = [plain](ffloat x, ffloat y) {
+            if (plain) return ffloat{x.hi + y.hi, 0.f};
+            return ff_add(x, y);
+        };
+        if constexpr (RAMAN != 0) {
+            // chi_R of this thread's 16 samples (the forward's raman_pass on e), then the transpose of the
+            // Raman map applied to ybar = gp e (P = chi e); Zr gets chi_R gp + (dF/de) Fbar with the
+            // drive F = z^2 of the unnormalised field z = Nt e, dF/de = 2 Nt z
+            float chiR[16], ybar[16], Fbar[16];
+            raman_pass<16, false>(
+                tp, Rs, tot, C, logC, T, tid, seg, ngc,
+                [&](int k) {
+                    const float2 zv = Ze[sw(m0 + k) * C + c];
+                    return make_float2(zv.x * zv.x, zv.y * zv.y);
+                },
+                [&](int k, float chi0, float chi1) {
+                    chiR[2 * k] = chi0;
+                    chiR[2 * k + 1] = chi1;
+                });
+    #pragma unroll
+            for (int k = 0; k < MPS; ++k) {
+                const float2 zv = Ze[sw(m0 + k) * C + c], gv = Zp[sw(m0 + k) * C + c];
+                ybar[2 * k] = gv.x * zv.x * inv;
+                ybar[2 * k + 1] = gv.y * zv.y * inv;
+            }
+            raman_adjoint_pass<16>(tp, Rs, tot, C, logC, T, tid, seg, ngc, ybar, Fbar);
+            const float two_nt = 2.f * (float)Nt;
+    #pragma unroll
+            for (int k = 0; k < MPS; ++k) {
+                const float2 zv = Ze[sw(m0 + k) * C + c], gv = Zp[sw(m0 + k) * C + c];
+                Zr[sw(m0 + k) * C + c] = make_float2(fmaf(chiR[2 * k], gv.x, two_nt * zv.x * Fbar[2 * k]),
+                                                     fmaf(chiR[2 * k + 1], gv.y, two_nt * zv.y * Fbar[2 * k + 1]));
+            }
+        }
+        // With no nonzero rate anywhere in the block the density, the plasma-current cotangent and the
+        // rate-derivative terms are all zero: `ion` leaves them out (and the inverse FFT of gpl).
+        bool ion = false;
+        float r_next = 0.f;
         ffloat part = {0.f, 0.f};
-#pragma unroll 1
-        for (int j = 0; j < MPS; ++j) {
-            const int m = m0 + j;
-            const float2 e2 = Ze[sw(m) * C + c], l2 = Zl[sw(m) * C + c], s2 = Zn[sw(m) * C + c];
-            const float a0 = ngc * soft_window(2 * m, Nt, tp.wcut, tp.wwid) * expf(-s2.x);
-            const float a1 = ngc * soft_window(2 * m + 1, Nt, tp.wcut, tp.wwid) * expf(-s2.y);
-            acc_add(part, l2.x * e2.x * inv * a0, tp.plain);
-            acc_add(part, l2.y * e2.y * inv * a1, tp.plain);
-        }
-        carry = earlier_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
-    }
-    // ---- 4. pointwise cotangent of e(t), written over the e pairs ----
-    float dred_part = 0.f;
-    {
-        ffloat Pprev = carry;  // Pfx(t - 1)
-#pragma unroll 1
-        for (int j = 0; j < MPS; ++j) {
-            const int m = m0 + j;
-            const float2 e2 = Ze[sw(m) * C + c];
-            const float2 p2 = Zp[sw(m) * C + c];
-            float ge[2];
-            const float ev[2] = {e2.x * inv, e2.y * inv};
-            const float gp[2] = {p2.x, p2.y};
-            float2 l2 = make_float2(0.f, 0.f), s2 = l2, r2 = l2;
-            if constexpr (RAMAN != 0) r2 = Zr[sw(m) * C + c];
-            if (ion) {
-                l2 = Zl[sw(m) * C + c];
-                s2 = Zn[sw(m) * C + c];
+        if (ionize) {
+            if (t1 <= Nt - 2) r_next = ion_rate(tp, Ze[sw(t1 >> 1) * C + c].x * inv);
+            float rn = r_next;
+            bool live = r_next != 0.f;
+    #pragma unroll 1
+            for (int j = MPS - 1; j >= 0; --j) {
+                const int m = m0 + j;
+                const float2 zv = Ze[sw(m) * C + c];
+                const int t = 2 * m + 1;
+                const float r1 = (t == Nt - 1) ? 0.f : ion_rate(tp, zv.y * inv);
+                if (t <= Nt - 2) acc_add(part, tp.hdt * (r1 + rn), tp.plain);
+                const float r0 = ion_rate(tp, zv.x * inv);
+                acc_add(part, tp.hdt * (r0 + r1), tp.plain);
+                live = live || r0 != 0.f || r1 != 0.f;
+                rn = r0;
+                Zn[sw(m) * C + c] = make_float2(r0, r1);
             }
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int t = 2 * m + h;
-                const float e = ev[h];
-                float g = 3.f * kerr * e * e * gp[h] + (h ? r2.y : r2.x);
-                dred_part = fmaf(gp[h] * ngc * e * e, e, dred_part);
-                if (ion) {
-                    const float gl = h ? l2.y : l2.x;
-                    const float Sv = h ? s2.y : s2.x;
-                    const float wv_t = soft_window(t, Nt, tp.wcut, tp.wwid);
-                    const float ne = ngc * one_minus_exp_neg(Sv) * wv_t;
-                    const float a = ngc * wv_t * expf(-Sv);
-                    g = fmaf(ne, gl, g);
-                    ffloat P = Pprev;
-                    acc_add(P, gl * e * a, tp.plain);
-                    if (t <= Nt - 2) {
-                        const float r = ion_rate(tp, e);
-                        const float gr = tp.hdt * (ff_value(P) + ff_value(Pprev));
-                        g = fmaf(gr, ion_rate_deriv(tp, e, r), g);
-                    }
-                    Pprev = P;
-                }
-                ge[h] = g;
-            }
-            Ze[sw(m) * C + c] = make_float2(ge[0], ge[1]);
+            ion = __syncthreads_or(live ? 1 : 0) != 0;
         }
-    }
-    // block reduction of the chi3 derivative (a block of fewer than 32 threads reduces through shared memory)
-    double dsum = (double)dred_part;
-    if (T >= 32) {
-        for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
-        if ((tid & 31) == 0) red_sh[tid >> 5] = dsum;
-    } else {
-        red_sh[tid] = dsum;
-    }
-    __syncthreads();
-    if (tid == 0) {
-        double b = 0.0;
-        const int nred = (T >= 32) ? (T >> 5) : T;
-        for (int i = 0; i < nred; ++i) b += red_sh[i];
-        atomicAdd(dred, b);
-    }
+        if (ion) {
+            ffloat Sacc = later_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
+            float rn = r_next;
+    #pragma unroll 1
+            for (int j = MPS - 1; j >= 0; --j) {
+                const int m = m0 + j;
+                const float2 rr = Zn[sw(m) * C + c];
+                const int t = 2 * m + 1;
+                if (t <= Nt - 2) acc_add(Sacc, tp.hdt * (rr.y + rn), tp.plain);
+                const float S1 = ff_value(Sacc);
+                acc_add(Sacc, tp.hdt * (rr.x + rr.y), tp.plain);
+                rn = rr.x;
+                Zn[sw(m) * C + c] = make_float2(ff_value(Sacc), S1);
+            }
+            // Gl over the raw G, which Zl has held since staging (its pack reads every G it overwrites)
+            pack_half_spectrum(Zl, C, logC, M, tws, [&](int k, int c) {
+                const float wk = wv[k];
+                const float wt = (k == 0 || k == M) ? 1.f : 0.5f;
+                const float rden = __frcp_rn(fmaf(wk, wk, tp.damping * tp.damping));
+                return cscale(cmul(Zl[sw(k) * C + c], make_float2(tp.damping, -wk)), rden * wt * filt[k]);
+            }, tid, T, sw);
+            __syncthreads();  // the packed Gl is complete; the segment totals are reused below
+            inv_fft(Zl);
+        }
 
-    // ---- 5. transpose of irfft: gE = (1/Nt) W2 rfft(ge) ----
-    if constexpr (CT)
-        fft_axis_ct<8, LOGM, LOGC, LOGM + 1>(Ze, TwHalfSharedCT<LOGM + 1>{twl}, false, tid);
-    else
-        fft_axis_tw<8>(Ze, tp.logM, logC, 1, C, tws, false, tid, T, -1, sw);
-    for (int it = tid; it < (M + 1) * C; it += T) {
-        const int cc = it & (C - 1);
-        const int k = it >> logC;
-        const int ka = k & (M - 1), kb = (M - k) & (M - 1);
-        const float2 X = real_spectrum(Ze[sw(ka) * C + cc], Ze[sw(kb) * C + cc], tws.get(k));
-        const float wt = (k == 0 || k == M) ? inv : 2.f * inv;
-        gE[(size_t)k * S + col0 + cc] = cscale(X, wt);
+        // ---- 3. transposed scan: Pfx(j) = sum_{t <= j} gpl e a, a = ng w exp(-S), increasing t ----
+        ffloat carry = {0.f, 0.f};
+        if (ion) {
+            ffloat part = {0.f, 0.f};
+    #pragma unroll 1
+            for (int j = 0; j < MPS; ++j) {
+                const int m = m0 + j;
+                const float2 e2 = Ze[sw(m) * C + c], l2 = Zl[sw(m) * C + c], s2 = Zn[sw(m) * C + c];
+                const float a0 = ngc * soft_window(2 * m, Nt, tp.wcut, tp.wwid) * expf(-s2.x);
+                const float a1 = ngc * soft_window(2 * m + 1, Nt, tp.wcut, tp.wwid) * expf(-s2.y);
+                acc_add(part, l2.x * e2.x * inv * a0, tp.plain);
+                acc_add(part, l2.y * e2.y * inv * a1, tp.plain);
+            }
+            carry = earlier_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
+        }
+        // ---- 4. pointwise cotangent of e(t), written over the e pairs ----
+        float dred_part = 0.f;
+        {
+            ffloat Pprev = carry;  // Pfx(t - 1)
+    #pragma unroll 1
+            for (int j = 0; j < MPS; ++j) {
+                const int m = m0 + j;
+                const float2 e2 = Ze[sw(m) * C + c];
+                const float2 p2 = Zp[sw(m) * C + c];
+                float ge[2];
+                const float ev[2] = {e2.x * inv, e2.y * inv};
+                const float gp[2] = {p2.x, p2.y};
+                float2 l2 = make_float2(0.f, 0.f), s2 = l2, r2 = l2;
+                if constexpr (RAMAN != 0) r2 = Zr[sw(m) * C + c];
+                if (ion) {
+                    l2 = Zl[sw(m) * C + c];
+                    s2 = Zn[sw(m) * C + c];
+                }
+    #pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    const int t = 2 * m + h;
+                    const float e = ev[h];
+                    float g = 3.f * kerr * e * e * gp[h] + (h ? r2.y : r2.x);
+                    dred_part = fmaf(gp[h] * ngc * e * e, e, dred_part);
+                    if (ion) {
+                        const float gl = h ? l2.y : l2.x;
+                        const float Sv = h ? s2.y : s2.x;
+                        const float wv_t = soft_window(t, Nt, tp.wcut, tp.wwid);
+                        const float ne = ngc * one_minus_exp_neg(Sv) * wv_t;
+                        const float a = ngc * wv_t * expf(-Sv);
+                        g = fmaf(ne, gl, g);
+                        ffloat P = Pprev;
+                        acc_add(P, gl * e * a, tp.plain);
+                        if (t <= Nt - 2) {
+                            const float r = ion_rate(tp, e);
+                            const float gr = tp.hdt * (ff_value(P) + ff_value(Pprev));
+                            g = fmaf(gr, ion_rate_deriv(tp, e, r), g);
+                        }
+                        Pprev = P;
+                    }
+                    ge[h] = g;
+                }
+                Ze[sw(m) * C + c] = make_float2(ge[0], ge[1]);
+            }
+        }
+        // block reduction of the chi3 derivative (a block of fewer than 32 threads reduces through shared memory)
+        double dsum = (double)dred_part;
+        if (T >= 32) {
+            for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+            if ((tid & 31) == 0) red_sh[tid >> 5] = dsum;
+        } else {
+            red_sh[tid] = dsum;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double b = 0.0;
+            const int nred = (T >= 32) ? (T >> 5) : T;
+            for (int i = 0; i < nred; ++i) b += red_sh[i];
+            atomicAdd(dred, b);
+        }
+
+        // ---- 5. transpose of irfft: gE = (1/Nt) W2 rfft(ge) ----
+        if constexpr (CT)
+            fft_axis_ct<8, LOGM, LOGC, LOGM + 1>(Ze, TwHalfSharedCT<LOGM + 1>{twl}, false, tid);
+        else
+            fft_axis_tw<8>(Ze, tp.logM, logC, 1, C, tws, false, tid, T, -1, sw);
+        for (int it = tid; it < (M + 1) * C; it += T) {
+            const int cc = it & (C - 1);
+            const int k = it >> logC;
+            const int ka = k & (M - 1), kb = (M - k) & (M - 1);
+            const float2 X = real_spectrum(Ze[sw(ka) * C + cc], Ze[sw(kb) * C + cc], tws.get(k));
+            const float wt = (k == 0 || k == M) ? inv : 2.f * inv;
+            gE[(size_t)k * S + col0 + cc] = cscale(X, wt);
+        }
+        __syncthreads();  // the next group overwrites the shared arrays
     }
 }
 
@@ -762,7 +786,10 @@ static int adjoint_cols(const UppeHandle* h) {
     return c;
 }
 
-cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G, float2* gE, double* dred) {
+// The shared-memory adjoint time pass over every column group (list NULL), or over the groups
+// list[1 .. list[0]] with a grid of at most nlist blocks that take them in turn.
+static cudaError_t launch_time_adj_smem(UppeHandle* h, const float2* E, const float2* G, float2* gE, double* dred,
+                                        const int* list, int nlist) {
     TimeParams tp = uppe_time_params(h);
     const int Ca = adjoint_cols(h);
     tp.C = Ca;
@@ -770,7 +797,8 @@ cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G,
     tp.spt = 16;
     const int T = h->Nt * Ca / 16;
     const size_t smem = ((size_t)(h->M + 1) * 4 * Ca + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
-    const int nblk = h->S / Ca;
+    int nblk = h->S / Ca;
+    if (list && nlist < nblk) nblk = nlist;
     h->launches++;
     if (h->rot_pairs > 0) {  // the Raman response: 2T segment totals, Zr [M][C] (even length), the pair tables
         const size_t zr = (((size_t)h->M * Ca + 1) & ~(size_t)1) * sizeof(float2);
@@ -778,16 +806,29 @@ cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G,
                               (size_t)2 * T * sizeof(ffloat) + zr + (size_t)20 * h->rot_pairs * sizeof(float4);
         if (smem_r > 224 * 1024) return cudaErrorInvalidValue;
         k_time_adj<0, -1, 1><<<nblk, T, smem_r, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp,
-                                                          dred);
+                                                          dred, list);
         return cudaGetLastError();
     }
-#define UPPE_TIME_ADJ_CASE(A_, B_)                                                                              \
-    if (tp.logM == A_ && tp.logC == B_) {                                                                       \
-        k_time_adj<A_, B_><<<nblk, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred); \
-        return cudaGetLastError();                                                                              \
+#define UPPE_TIME_ADJ_CASE(A_, B_)                                                                             \
+    if (tp.logM == A_ && tp.logC == B_) {                                                                      \
+        k_time_adj<A_, B_><<<nblk, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred, \
+                                                        list);                                                 \
+        return cudaGetLastError();                                                                             \
     }
     UPPE_TIME_ADJ_CT(UPPE_TIME_ADJ_CASE)
 #undef UPPE_TIME_ADJ_CASE
-    k_time_adj<><<<nblk, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred);
+    k_time_adj<><<<nblk, T, smem, h->stream>>>(E, G, gE, h->ng, h->w, h->nlfilt, h->tw, h->twLog, tp, dred, list);
     return cudaGetLastError();
+}
+
+// The adjoint time pass.  Where the register-resident form applies (timepass_adj_reg.cu) it takes
+// the column groups without ionization and lists the others, which the shared-memory kernel then
+// takes (a grid of three blocks per multiprocessor walking the list).
+cudaError_t launch_time_adjoint(UppeHandle* h, const float2* E, const float2* G, float2* gE, double* dred) {
+    if (time_adj_reg_ready(h) && adjoint_cols(h) == time_adj_reg_group(h->M)) {
+        cudaError_t e = launch_time_adj_reg(h, E, G, gE, dred);
+        if (e != cudaSuccess || h->cfg.rate_form == UPPE_RATE_NONE) return e;
+        return launch_time_adj_smem(h, E, G, gE, dred, h->adj_live, 3 * h->num_sms);
+    }
+    return launch_time_adj_smem(h, E, G, gE, dred, nullptr, 0);
 }

@@ -59,6 +59,7 @@ struct UppeHandle {
     int slice_big;                 // Cartesian slices above 128 x 128: row and column passes (slice_big.cu)
     int time_reg;                  // TIME_J through the register-resident time pass where it applies (timepass_reg.cu)
     int slice_cluster;             // 256 x 256 slices: the fused tail in one cluster launch (slice_cluster.cu)
+    int tc_next;                   // tensor-core Hankel: stage updates write the next inverse transform's operand
     cudaStream_t stream;
     // library-owned device buffers
     float2 *q, *qi, *qf, *k1, *E, *J, *scratch;
@@ -70,6 +71,8 @@ struct UppeHandle {
     float2* tw;
     float2* tw_reg;  // twiddle tables of the register-resident time pass (timepass_reg.cu), or NULL
     float2* tscr;    // its parking scratch for ionizing columns ([S][2 (M + 1)]), or NULL
+    int* adj_live;   // register-resident adjoint time pass: count + column groups left to k_time_adj, or NULL
+    float2* adj_park; // its parking scratch for e(t) ([S][M]) when tscr is NULL, or NULL
     float* w;        // omega per bin (FP32)
     float* nlfilt;   // NL filter per bin
     float* Minv;     // cylindrical: [N2][Nr][Nk]
@@ -80,6 +83,11 @@ struct UppeHandle {
     uint8_t* MinvT_tc;
     uint8_t* Atc;     // pre-split A operand tiles of the tensor-core Hankel transform (mixed form)
     size_t Atc_bytes;
+    int time_atc;                // the next TIME_J pass writes J into Atc (the forward transform's operand)
+    int atc_fwd;                 // Atc holds the forward transform's operand of J (written by the time pass)
+    int atc_next;                // Atc holds the operand of the inverse transform of atc_next_src at atc_next_z
+    const void* atc_next_src;
+    StepArgs atc_next_z;
     double* kr2_d;   // [S] transverse eigenvalues (FP64)
     double* w2n2_d;  // [N0] complex w^2 (1 + chi0) interleaved
     double* kg_d;    // [N0]
@@ -139,6 +147,12 @@ int time_reg_tables(int M, float2* host);
 size_t time_reg_scratch_len(const UppeHandle* h);
 cudaError_t uppe_configure_time_reg();
 cudaError_t launch_time_reg(UppeHandle* h, const float2* E, float2* J);
+// register-resident adjoint time pass (timepass_adj_reg.cu): the columns without ionization
+int time_adj_reg_group(int M);
+size_t time_adj_reg_list_len(const UppeHandle* h);
+bool time_adj_reg_ready(const UppeHandle* h);
+cudaError_t uppe_configure_time_adj_reg();
+cudaError_t launch_time_adj_reg(UppeHandle* h, const float2* E, const float2* G, float2* gE, double* dred);
 // paraxial envelope time pass (envelope.cu)
 cudaError_t launch_time_env(UppeHandle* h, int mode, const float2* A, float2* out0, float2* out1);
 cudaError_t uppe_configure_env_kernel(size_t smem_bytes);
@@ -169,7 +183,9 @@ cudaError_t launch_adj_reg(UppeHandle* h, int mode, const float2* in, float2* ou
 cudaError_t launch_adj_fused_reg(UppeHandle* h, int mode, const float2* g, float2* out, float a_f, float a_mu,
                                  StepArgs z_e, StepArgs z_s);
 cudaError_t launch_spec_point(UppeHandle* h, int mode, const float2* C, float2* q_out, float2* qf, const float2* qi,
-                              float Cs, float Ce, StepArgs z);
+                              float Cs, float Ce, StepArgs z, const StepArgs* z_next);
+struct TcNext;
+TcNext hankel_tc_next(const UppeHandle* h, StepArgs z_next);
 cudaError_t launch_adj_fused_big(UppeHandle* h, int mode, const float2* g, float2* out, float a_f, float a_mu,
                                  StepArgs z_e, StepArgs z_s);
 
@@ -195,4 +211,4 @@ cudaError_t launch_adj_cyl(UppeHandle* h, int mode, const float2* in, float2* ou
 // ---- cylindrical transverse transform (hankel.cu) ----
 cudaError_t launch_real_cyl(UppeHandle* h, int mode, const float2* src, float2* A_out, StepArgs z);
 cudaError_t launch_spec_cyl(UppeHandle* h, int mode, const float2* src_real, float2* q_out, float2* qf_io,
-                            const float2* qi, float Cs, float Ce, StepArgs z);
+                            const float2* qi, float Cs, float Ce, StepArgs z, const StepArgs* z_next = nullptr);

@@ -10,6 +10,7 @@
 
 #include "common.cuh"
 #include "fft_smem.cuh"
+#include "hankel_tc.cuh"
 #include "rk_stage.cuh"
 #include "uppe_internal.h"
 
@@ -393,25 +394,43 @@ __global__ void k_adj_rk(int mode, const float2* __restrict__ lam_out, float2* _
 // The spectral update of every point from the transformed current C (the ODE right-hand side and the
 // RK stage of spec_update), as a separate pass after a tensor-core transform that stored C: many
 // warps per multiprocessor hide the latency of its operand reads, which the GEMM's own epilogue,
-// with one block per multiprocessor, does not.
+// with one block per multiprocessor, does not.  With nx.Atc set (one azimuthal node) it also writes
+// the operand of the next inverse transform, i kz exp(i (kz + kg) z_next) qw of the new stage
+// estimate qw, split into the transform's bf16 tiles (zero beyond the Nk radial modes), which
+// k_hankel_tc_prep would otherwise form from qw.
 __global__ void k_spec_point(int mode, const float2* __restrict__ C, OpView opv, float2* __restrict__ q_out,
                              float2* __restrict__ qf, const float2* __restrict__ qi, float Cs, float Ce, StepArgs z,
-                             size_t n, int S) {
+                             size_t n, int S, TcNext nx) {
     const PhaseArgs pa{z.zhi, z.zlo, z.plain};
+    const PhaseArgs pn{nx.z.zhi, nx.z.zlo, nx.z.plain};
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
         const int w = (int)(idx / (size_t)S);
         const float cond = (w < opv.ncond) ? 0.f : 1.f;
         const OpPoint o = op_at(opv, idx, opv.kg[w]);
-        spec_update(mode, idx, C[idx], o, cond, q_out, qf, qi, Cs, Ce, pa, true);
+        const float2 qw = spec_update(mode, idx, C[idx], o, cond, q_out, qf, qi, Cs, Ce, pa, true);
+        if (nx.Atc) {
+            const int k = (int)(idx - (size_t)w * S);
+            float2 a = make_float2(0.f, 0.f);
+            if (k < nx.Nk) a = op_field(opv, o, cmul(propagator_factor(o, pn, 1.f), qw));
+            tc_store_split(nx.Atc, nx.nwt, nx.nkt, 0, w, k, a);
+        }
     }
 }
 
 cudaError_t launch_spec_point(UppeHandle* h, int mode, const float2* C, float2* q_out, float2* qf, const float2* qi,
-                              float Cs, float Ce, StepArgs z) {
+                              float Cs, float Ce, StepArgs z, const StepArgs* z_next) {
+    TcNext nx{};
+    if (z_next) nx = hankel_tc_next(h, *z_next);
     h->launches++;
     k_spec_point<<<reduce_blocks_host(h->P), 256, 0, h->stream>>>(mode, C, uppe_op_view(h), q_out, qf, qi, Cs, Ce, z,
-                                                                   h->P, h->S);
-    return cudaGetLastError();
+                                                                   h->P, h->S, nx);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess && z_next) {
+        h->atc_next = 1;
+        h->atc_next_src = q_out;
+        h->atc_next_z = *z_next;
+    }
+    return e;
 }
 
 cudaError_t launch_adj_rk(UppeHandle* h, int mode, const float2* lam_out, float2* lam_in, float a_f, float a_mu) {

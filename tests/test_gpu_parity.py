@@ -92,6 +92,39 @@ def test_tensor_core_and_simt_hankel_agree():
     assert eq < 5e-5 and es < 1e-4
 
 
+@pytest.mark.parametrize("name", ["cyl_kerr", "cyl_raman"])
+def test_stage_update_writes_next_transform_operand(name, monkeypatch):
+    """Mixed form, one azimuthal node: the time pass writes J straight into the split operand tiles
+    of the forward tensor-core transform, and the spectral update of RK stages 1-3 writes those of
+    the next inverse transform (k_spec_point); both transforms then skip their pre-pass
+    (k_hankel_tc_prep).  Against SEARAY_UPPE_TC_NEXT=0 (every transform forms its operand itself)
+    over three fixed steps: the same arithmetic on the same values, so the field, J and the held q
+    agree bit for bit, with seven launches fewer per step (four forward, three inverse)."""
+    import torch
+    from searay_gb300 import uppe
+    out, launches = {}, {}
+    for form in ("fused", "prepass"):
+        if form == "prepass":
+            monkeypatch.setenv("SEARAY_UPPE_TC_NEXT", "0")
+        else:
+            monkeypatch.delenv("SEARAY_UPPE_TC_NEXT", raising=False)
+        vd, g, dev, mat, orc = _device_case(name, "mixed")
+        L = vd["size"][2] / 20
+        a = torch.from_numpy(vd["incoming wave"](g.w, g.x1, g.x2).astype(np.complex64)).cuda()
+        l0 = dev.launches()
+        A, J, chi, ne, evals = uppe.propagator(dev, mat, a, 3, 0.0, 3 * L, L)
+        assert evals == 12 and not dev.nonfinite()
+        launches[form] = dev.launches() - l0
+        q = dev.empty_field()
+        dev.get_field(q)
+        out[form] = (A.cpu().numpy(), J.cpu().numpy(), q.cpu().numpy())
+        dev.close()
+    print(name, launches)
+    assert launches["prepass"] - launches["fused"] == 3 * 7, launches
+    for x, y in zip(out["fused"], out["prepass"]):
+        assert np.array_equal(x, y)
+
+
 @pytest.mark.parametrize("name", replay.CASE_NAMES)
 def test_transform_and_rhs_vs_oracle(name):
     """One kspacex of the incoming field and one load_source evaluation, against FP64."""

@@ -95,3 +95,75 @@ def test_register_time_pass_matches_shared_memory_form(n0, n_perp, monkeypatch):
     e = rel_err(out["reg"][4:], out["smem"][4:])
     print(n0, n_perp, f"register vs shared-memory time pass: {e:.2e}")
     assert np.max(np.abs(out["smem"][4:])) > 0 and e < 1e-5
+
+
+def _adjoint_step(vd, g, a, lam, form, ionizing, chi3, monkeypatch):
+    """(cotangent of q, chi3 derivative, kernel launches) of one RK4 step's VJP in the given form."""
+    import torch
+    from searay_gb300 import ionization, uppe
+    if form == "smem":
+        monkeypatch.setenv("SEARAY_UPPE_TIME", "smem")
+    else:
+        monkeypatch.delenv("SEARAY_UPPE_TIME", raising=False)
+    rates = ionization.RateCoefficients(vd["ionizer"]) if ionizing else None
+    dev = uppe.DeviceGrid(g, vd, rates, "mixed")
+    dev.set_chi3(chi3 / vd["density reference"])
+    chi = vd["dispersion inside"].chi(g.w).astype(np.cdouble)
+    mat = uppe.Material(dev, g, "cartesian", None, chi, chi3, vd["density reference"], vd["window speed"],
+                        vd["density lambda"])
+    mat.UpdateMaterial(100.0)
+    dev.load_field(torch.from_numpy(a.astype(np.complex64)).cuda())
+    q = dev.empty_field()
+    dev.get_field(q)
+    gq = dev.empty_field()
+    l0 = dev.launches()
+    dred = dev.adjoint_step(q, torch.from_numpy(lam.astype(np.complex64)).cuda(), gq, 50.0, 100.0)
+    launches = dev.launches() - l0
+    assert not dev.nonfinite()
+    out = gq.cpu().numpy()
+    dev.close()
+    return out, dred, launches
+
+
+@pytest.mark.parametrize("ionizing", [True, False], ids=["ionizing", "kerr"])
+@pytest.mark.parametrize("n0,n_perp", [(257, 16), (513, 32), (1025, 16)])
+def test_register_adjoint_time_pass_matches_shared_memory_form(n0, n_perp, ionizing, monkeypatch):
+    """The vector-Jacobian product of one RK4 step with the register-resident adjoint time pass
+    (timepass_adj_reg.cu: the column groups without ionization; the groups with a nonzero rate go to
+    the shared-memory kernel from its list) against the shared-memory form alone
+    (SEARAY_UPPE_TIME=smem) on the same field and cotangent.  The time pass gives the nonlinear
+    part of the cotangent of q, so the error is measured on that part: the difference of the two
+    forms over max |g - g_lin|, g_lin the cotangent with chi3 = 0 and no ionization (time pass
+    output zero).  Both are FP32 forms of the same sums: held to 1e-4 there, and to 1e-5 relative
+    on the chi3 derivative.  Kerr coefficient at 30x the workload's, so that the nonlinear part is
+    a measurable share of the cotangent (the linear part is the same code, bit for bit, in both
+    forms).  With ionization the register form launches one more kernel per
+    stage (the listed groups), which shows both kernels ran."""
+    from searay_gb300 import grid, workloads
+    vd = workloads.cart_filament_128(steps=400, n_perp=n_perp)
+    vd["wave grid"] = (n0, n_perp, n_perp, 2)
+    vd["frequency band"] = (0.0, 4.0 * (n0 - 1) / 512)
+    vd["nonlinear band"] = (0.0, 3.5 * (n0 - 1) / 512)
+    wave = vd["incoming wave"]
+    vd["incoming wave"] = lambda w, x1, x2: 3.0 * wave(w, x1, x2)
+    g = grid.VolumeGrid(vd)
+    a = vd["incoming wave"](g.w, g.x1, g.x2)
+    rng = np.random.default_rng(11)
+    lam = (rng.standard_normal(a.shape) + 1j * rng.standard_normal(a.shape)) * (np.abs(a) + 1e-3 * np.abs(a).max())
+    chi3 = 30.0 * vd["chi3"]
+    g_lin, _, _ = _adjoint_step(vd, g, a, lam, "reg", False, 0.0, monkeypatch)
+    out, launches = {}, {}
+    for form in ("reg", "smem"):
+        gq, dred, launches[form] = _adjoint_step(vd, g, a, lam, form, ionizing, chi3, monkeypatch)
+        out[form] = (gq, dred)
+    nl = np.max(np.abs(out["smem"][0] - g_lin))
+    share = nl / np.max(np.abs(out["smem"][0]))
+    e = float(np.max(np.abs(out["reg"][0] - out["smem"][0])) / nl)
+    ed = abs(out["reg"][1] - out["smem"][1]) / abs(out["smem"][1])
+    print(n0, n_perp, "ionizing" if ionizing else "kerr", f"nonlinear share {share:.2e}",
+          f"register vs shared-memory adjoint time pass: {e:.2e}, chi3 derivative {ed:.2e}", launches)
+    assert share > 1e-4
+    assert e < 1e-4
+    assert ed < 1e-5
+    if ionizing:
+        assert launches["reg"] - launches["smem"] == 4, launches
