@@ -10,9 +10,10 @@ searay_gb300/workloads.py), the largest workload that fits one GPU.
 
 value: P * K / (device time of K steps), fields resident in HBM, CUDA events on the library's stream.
 e2e:   the same metric through the reference-facing call searay_gb300.track() with host (NumPy)
-       input and outputs: grid and handle set-up, the host->device copy of the input plane, the
-       steps and the device->host copies of every output inside the timed region; the input plane
-       itself (the user's incoming-wave function on the grid) is evaluated before it.
+       input and outputs, one call over the workload's whole propagation (its own step count,
+       --e2e-steps to change it): grid and handle set-up, the host->device copy of the input plane,
+       the steps and the device->host copies of every output inside the timed region; the input
+       plane itself (the user's incoming-wave function on the grid) is evaluated before it.
 roofline: the kernel class with the largest share of the step, algorithmic bytes per launch over its
        average event-timed duration, against the measured HBM copy bandwidth.
 cpu_baseline: the FP64 NumPy oracle (a restatement of the reference path) timed on the host cores:
@@ -306,15 +307,18 @@ def run_device(args, vd, ws, rank, local, precision, per_class=True):
 
 
 def run_e2e(args, vd, precision):
-    """K steps through track() with host input/outputs (one diagnostic interval)."""
+    """One track() call with host input/outputs over n steps (one diagnostic interval): the
+    workload's whole propagation (its own step count) unless --e2e-steps says otherwise.  Returns
+    (rate, h2d bytes, d2h bytes, finite, n)."""
     import torch
     from searay_gb300 import paraxial, uppe
     solver = paraxial if is_paraxial(vd) else uppe
     Lz = vd["size"][2]
     dz = Lz / vd["subcycles"]
+    n = args.e2e_steps if args.e2e_steps else vd["subcycles"]
     v = dict(vd)
-    v["size"] = (vd["size"][0], vd["size"][1], dz * args.steps)
-    v["subcycles"] = args.steps
+    v["size"] = (vd["size"][0], vd["size"][1], dz * n)
+    v["subcycles"] = n
     v["minimum step"] = dz
     v["precision"] = precision
     # the input plane is the user's data: evaluated on the host before the timed region, handed to
@@ -337,7 +341,7 @@ def run_e2e(args, vd, precision):
     # (every diagnostic plane) out
     h2d = P * 16 + (2 * N[0] + N[0]) * 8 + N[1] * N[2] * 8
     d2h = 4 * P * N[3] * 16
-    return P * args.steps / wall, h2d, d2h, bool(np.isfinite(A[..., -1]).all())
+    return P * n / wall, h2d, d2h, bool(np.isfinite(A[..., -1]).all()), n
 
 
 def aggregate_replicas(ms, points, steps, ws, device):
@@ -572,6 +576,8 @@ def main():
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None,
+                    help="steps of the e2e track() call (default: the workload's whole propagation)")
     ap.add_argument("--no-fp32", action="store_true", help="skip the plain FP32 companion rates")
     ap.add_argument("--adjoint-steps", type=int, default=20,
                     help="adjoint (VJP) steps timed for the forward+adjoint rate; 0 to skip")
@@ -666,9 +672,10 @@ def main():
             comp["fwd_adjoint"] = fwd_adjoint_entry(P2, ws, ms2 / args.steps, adj2)
         line[other] = comp
     if rank == 0 and not args.no_e2e:
-        e2e, h2d, d2h, ok = run_e2e(args, vd, args.precision)
-        line["e2e"] = {"value": e2e * ws, "unit": UNIT, "h2d_bytes_per_step": h2d / args.steps,
-                       "d2h_bytes_per_step": d2h / args.steps, "call": "searay_gb300.track (host NumPy in/out)"}
+        e2e, h2d, d2h, ok, n_e2e = run_e2e(args, vd, args.precision)
+        line["e2e"] = {"value": e2e * ws, "unit": UNIT, "h2d_bytes_per_step": h2d / n_e2e,
+                       "d2h_bytes_per_step": d2h / n_e2e, "steps": n_e2e,
+                       "call": "searay_gb300.track (host NumPy in/out), one call over the steps"}
     if rank == 0 and not args.no_cpu_baseline and ws == 1:
         base, v_sample, ref = cpu_baseline(vd, outputs=True)
         line["cpu_baseline"] = base

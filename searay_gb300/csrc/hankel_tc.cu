@@ -23,7 +23,6 @@
 #include "hankel_tc.cuh"
 #include "uppe_internal.h"
 
-#define TC_STAGE_LD (TC_N + 1)              // padded row of the epilogue staging tile (float2)
 #define TC_WAIT_LIMIT (1 << 24)
 
 // operand modes (TA_SADJ: the cotangent of S times conj(D2), the A operand of the adjoint ADJ_S)
@@ -58,9 +57,10 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
     return d;
 }
 
-// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, N = 128, M = 128.
+// Instruction descriptor, kind::f16: D = F32, A = B = BF16, both K-major, M = 128, N = TN.
+template <int TN>
 __device__ __forceinline__ uint32_t instr_desc() {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TC_N >> 3) << 17) | ((uint32_t)(TC_ROWS >> 4) << 24);
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TC_ROWS >> 4) << 24);
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -79,9 +79,19 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, int* er
     return false;
 }
 
-#define TC_THREADS 512  // 16 warps: the copies and the fused epilogue are spread over more threads
-#define TC_STAGE_BYTES (4 * TC_TILE_BYTES)  // A_hi | A_lo | B_hi | B_lo
-#define TC_NSTAGE 3                         // pipeline stages of the K loop (192 KB)
+// Output-tile shapes of the GEMM: TN = 128 columns per tile, 512 threads, three 64 KB stages, one
+// block per multiprocessor; TN = 64, 256 threads, two 48 KB stages, two blocks per multiprocessor
+// (twice the tiles in flight for the same grid).  A stage is [A_hi | A_lo | B_hi | B_lo]; a B tile of
+// TN rows is the upper or lower half (contiguous 8 KB) of the 128-row split matrix tiles.
+template <int TN>
+struct TcShape {
+    static constexpr int THREADS = TN == 128 ? 512 : 256;
+    static constexpr int NSTAGE = TN == 128 ? 3 : 2;
+    static constexpr int MINB = TN == 128 ? 1 : 2;
+    static constexpr uint32_t BTILE = (uint32_t)TN * TC_K * 2;  // bytes of one B operand (hi or lo)
+    static constexpr uint32_t STAGE = 2 * TC_TILE_BYTES + 2 * BTILE;
+    static constexpr int LD = TN + 1;  // padded row of the epilogue staging tile (float2)
+};
 
 // One 16-byte-aligned block of global memory (a multiple of 16 bytes) into this CTA's shared memory
 // by the bulk-copy engine; completion is counted in transaction bytes on the mbarrier.
@@ -91,7 +101,9 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
                  : "memory");
 }
 
+template <int TN>
 __device__ __forceinline__ void tc_issue(uint32_t tmem_d, uint32_t st_a, uint32_t idesc, bool first, uint32_t mbar) {
+    constexpr uint32_t BT = TcShape<TN>::BTILE;
     asm volatile("tcgen05.fence::after_thread_sync;\n");
 #pragma unroll
     for (int ks = 0; ks < TC_K / 16; ++ks) {
@@ -99,7 +111,7 @@ __device__ __forceinline__ void tc_issue(uint32_t tmem_d, uint32_t st_a, uint32_
         const uint64_t ahi = smem_desc(st_a + koff);
         const uint64_t alo = smem_desc(st_a + TC_TILE_BYTES + koff);
         const uint64_t bhi = smem_desc(st_a + 2 * TC_TILE_BYTES + koff);
-        const uint64_t blo = smem_desc(st_a + 3 * TC_TILE_BYTES + koff);
+        const uint64_t blo = smem_desc(st_a + 2 * TC_TILE_BYTES + BT + koff);
         const uint32_t acc0 = (!first || ks > 0) ? 1u : 0u;
         asm volatile(
             "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
@@ -148,35 +160,37 @@ __global__ void __launch_bounds__(256) k_hankel_tc_prep(TcArgs g, uint8_t* __res
     tc_store_split(Atc, g.nwt, g.nkt, m, w, k, v);
 }
 
-// The GEMM of one output tile (64 frequencies x 128 columns) on pre-split operand tiles (AMODE =
-// TA_PRESPLIT).  Thread 0 drives a ring of TC_NSTAGE stages: it issues both 32 KB tiles of a K step
+// The GEMM of one output tile (64 frequencies x TN columns) on pre-split operand tiles (AMODE =
+// TA_PRESPLIT).  Thread 0 drives a ring of NSTAGE stages: it issues the A and B tiles of a K step
 // as bulk copies that complete on the stage's `full` mbarrier, waits for them, issues the MMAs of the
 // step (committed to the stage's `done` mbarrier), and refills the stage of the previous step once
-// its MMAs have completed, so the copies run TC_NSTAGE - 1 steps ahead of the tensor core.
-template <int AMODE, int CMODE>
-__global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
+// its MMAs have completed, so the copies run NSTAGE - 1 steps ahead of the tensor core.
+template <int AMODE, int CMODE, int TN>
+__global__ void __launch_bounds__(TcShape<TN>::THREADS, TcShape<TN>::MINB) k_hankel_tc(TcArgs g) {
+    using SH = TcShape<TN>;
+    constexpr int NST = SH::NSTAGE, TT = SH::THREADS, LD = SH::LD;
     static_assert(AMODE == TA_PRESPLIT, "the GEMM reads pre-split operand tiles");
     extern __shared__ __align__(1024) uint8_t smem_raw[];
-    // TC_NSTAGE pipeline stages of [A_hi | A_lo | B_hi | B_lo] (1024-byte aligned), reused afterwards
+    // NST pipeline stages of [A_hi | A_lo | B_hi | B_lo] (1024-byte aligned), reused afterwards
     // as the epilogue staging tile
     const uint32_t raw_a = (uint32_t)__cvta_generic_to_shared(smem_raw);
     uint8_t* tiles = smem_raw + (((raw_a + 1023u) & ~1023u) - raw_a);
     float2* stage = reinterpret_cast<float2*>(tiles);
-    __shared__ uint64_t full[TC_NSTAGE], done[TC_NSTAGE];
+    __shared__ uint64_t full[NST], done[NST];
     __shared__ uint32_t tmem_slot;
     __shared__ int aborted;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int m = blockIdx.z;
     const int w0 = blockIdx.y * TC_W;
     const int it = blockIdx.x;
-    const int i0 = it * TC_N;
+    const int i0 = it * TN;
     const PhaseArgs pa{g.z.zhi, g.z.zlo, g.z.plain};
     const uint32_t tiles_a = smem_u32(tiles);
     const uint32_t full0 = smem_u32(&full[0]), done0 = smem_u32(&done[0]);  // stage s at + 8 s
 
     if (tid == 0) {
         aborted = 0;
-        for (int s2 = 0; s2 < TC_NSTAGE; ++s2) {
+        for (int s2 = 0; s2 < NST; ++s2) {
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(full0 + 8u * s2));
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(done0 + 8u * s2));
         }
@@ -184,7 +198,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
     }
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(smem_u32(&tmem_slot)),
-                     "r"(TC_N));
+                     "r"(TN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
@@ -192,46 +206,55 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
     asm volatile("tcgen05.fence::after_thread_sync;\n");
     const uint32_t tmem_d = tmem_slot;
     const int nkt = g.nkt;
-    const uint32_t idesc = instr_desc();
-    const uint8_t* Bbase = g.Btc + ((size_t)(m * g.nit + it) * nkt) * (2 * TC_TILE_BYTES);
+    const uint32_t idesc = instr_desc<TN>();
+    // B: the 128-row split tile of this output tile, and the TN-row half of it (TN = 64)
+    const int it128 = (it * TN) / 128;
+    const uint32_t bhalf = (uint32_t)(((it * TN) & 127) / TN) * SH::BTILE;
+    const uint8_t* Bbase = g.Btc + ((size_t)(m * g.nit + it128) * nkt) * (2 * TC_TILE_BYTES);
     const uint8_t* Abase = g.Atc + ((size_t)m * g.nwt + w0 / TC_W) * nkt * (size_t)(2 * TC_TILE_BYTES);
 
     if (tid == 0) {
         const auto load = [&](int kt, int s2) {
-            const uint32_t st = tiles_a + (uint32_t)s2 * TC_STAGE_BYTES, fb = full0 + 8u * s2;
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(4 * TC_TILE_BYTES)
+            const uint32_t st = tiles_a + (uint32_t)s2 * SH::STAGE, fb = full0 + 8u * s2;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(fb), "r"(SH::STAGE)
                          : "memory");
             bulk_g2s(st, Abase + (size_t)kt * (2 * TC_TILE_BYTES), 2 * TC_TILE_BYTES, fb);
-            bulk_g2s(st + 2 * TC_TILE_BYTES, Bbase + (size_t)kt * (2 * TC_TILE_BYTES), 2 * TC_TILE_BYTES, fb);
+            const uint8_t* bk = Bbase + (size_t)kt * (2 * TC_TILE_BYTES);
+            if constexpr (TN == 128) {
+                bulk_g2s(st + 2 * TC_TILE_BYTES, bk, 2 * TC_TILE_BYTES, fb);
+            } else {
+                bulk_g2s(st + 2 * TC_TILE_BYTES, bk + bhalf, SH::BTILE, fb);
+                bulk_g2s(st + 2 * TC_TILE_BYTES + SH::BTILE, bk + TC_TILE_BYTES + bhalf, SH::BTILE, fb);
+            }
         };
         int issued = 0;  // K steps whose copies are issued
         int landed = 0;  // K steps whose copies have been waited for
         int mmas = 0;    // K steps whose MMAs are issued
         bool ok = true;
-        for (; issued < nkt && issued < TC_NSTAGE; ++issued) load(issued, issued);
+        for (; issued < nkt && issued < NST; ++issued) load(issued, issued);
         for (int kt = 0; kt < nkt && ok; ++kt) {
-            const int s2 = kt % TC_NSTAGE;
-            ok = mbar_wait(full0 + 8u * s2, (uint32_t)((kt / TC_NSTAGE) & 1), g.err);
+            const int s2 = kt % NST;
+            ok = mbar_wait(full0 + 8u * s2, (uint32_t)((kt / NST) & 1), g.err);
             if (!ok) break;
             landed = kt + 1;
-            tc_issue(tmem_d, tiles_a + (uint32_t)s2 * TC_STAGE_BYTES, idesc, kt == 0, done0 + 8u * s2);
+            tc_issue<TN>(tmem_d, tiles_a + (uint32_t)s2 * SH::STAGE, idesc, kt == 0, done0 + 8u * s2);
             mmas = kt + 1;
             if (kt >= 1 && issued < nkt) {
-                const int sp = (kt - 1) % TC_NSTAGE;  // == issued % TC_NSTAGE
-                ok = mbar_wait(done0 + 8u * sp, (uint32_t)(((kt - 1) / TC_NSTAGE) & 1), g.err);
+                const int sp = (kt - 1) % NST;  // == issued % NST
+                ok = mbar_wait(done0 + 8u * sp, (uint32_t)(((kt - 1) / NST) & 1), g.err);
                 if (!ok) break;
                 load(issued, sp);
                 ++issued;
             }
         }
         // all MMAs are complete once the last commit has arrived (commits track all earlier MMAs)
-        if (ok) ok = mbar_wait(done0 + 8u * ((nkt - 1) % TC_NSTAGE), (uint32_t)(((nkt - 1) / TC_NSTAGE) & 1), g.err);
+        if (ok) ok = mbar_wait(done0 + 8u * ((nkt - 1) % NST), (uint32_t)(((nkt - 1) / NST) & 1), g.err);
         if (!ok) {
             // drain: the copies still in flight into this CTA's shared memory, then the issued MMAs
             for (int t = landed; t < issued; ++t)
-                mbar_wait(full0 + 8u * (t % TC_NSTAGE), (uint32_t)((t / TC_NSTAGE) & 1), nullptr);
+                mbar_wait(full0 + 8u * (t % NST), (uint32_t)((t / NST) & 1), nullptr);
             if (mmas > 0)
-                mbar_wait(done0 + 8u * ((mmas - 1) % TC_NSTAGE), (uint32_t)(((mmas - 1) / TC_NSTAGE) & 1), nullptr);
+                mbar_wait(done0 + 8u * ((mmas - 1) % NST), (uint32_t)(((mmas - 1) / NST) & 1), nullptr);
             aborted = 1;
         }
     }
@@ -246,7 +269,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
     const int wl = row >> 1;
     const int part = row & 1;
 #pragma unroll 1
-    for (int c0 = (warp >> 2) * 32; c0 < TC_N; c0 += (TC_THREADS / 128) * 32) {
+    for (int c0 = (warp >> 2) * 32; c0 < TN; c0 += (TT / 128) * 32) {
         uint32_t r[32];
         const uint32_t taddr = tmem_d + ((uint32_t)(quarter * 32) << 16) + (uint32_t)c0;
         asm volatile(
@@ -259,21 +282,21 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
               "=r"(r[30]), "=r"(r[31])
             : "r"(taddr));
         asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
-        float* st = reinterpret_cast<float*>(stage + wl * TC_STAGE_LD + c0) + part;
+        float* st = reinterpret_cast<float*>(stage + wl * LD + c0) + part;
 #pragma unroll
         for (int j = 0; j < 32; ++j) st[2 * j] = __uint_as_float(r[j]);
     }
     asm volatile("tcgen05.fence::before_thread_sync;\n");
     __syncthreads();
-    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_d), "r"(TC_N));
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_d), "r"(TN));
     if (aborted) return;
 
     // ---- fused epilogue, coalesced along the output columns ----
-    for (int e = tid; e < TC_W * TC_N; e += TC_THREADS) {
-        const int col = e & (TC_N - 1), wle = e >> 7;
+    for (int e = tid; e < TC_W * TN; e += TT) {
+        const int col = e & (TN - 1), wle = e / TN;
         const int w = w0 + wle, i = i0 + col;
         if (w >= g.N0 || i >= g.NI) continue;
-        const float2 v = stage[wle * TC_STAGE_LD + col];
+        const float2 v = stage[wle * LD + col];
         const size_t idx = ((size_t)w * g.N1 + i) * g.N2 + m;
         if (CMODE == TC_STORE) {
             g.C0[idx] = v;
@@ -315,26 +338,32 @@ __global__ void __launch_bounds__(TC_THREADS) k_hankel_tc(TcArgs g) {
     }
 }
 
+template <int TN>
 static size_t tc_smem_bytes() {
-    const size_t ops = TC_NSTAGE * (size_t)TC_STAGE_BYTES;
-    const size_t stage = (size_t)TC_W * TC_STAGE_LD * sizeof(float2);
+    const size_t ops = TcShape<TN>::NSTAGE * (size_t)TcShape<TN>::STAGE;
+    const size_t stage = (size_t)TC_W * TcShape<TN>::LD * sizeof(float2);
     return (ops > stage ? ops : stage) + 1024;  // + alignment slack
+}
+
+template <int AMODE, int CMODE, int TN>
+static cudaError_t run_tc_shape(UppeHandle* h, TcArgs& a) {
+    static bool configured = false;
+    const size_t smem = tc_smem_bytes<TN>();
+    if (!configured) {
+        cudaError_t e = cudaFuncSetAttribute(k_hankel_tc<AMODE, CMODE, TN>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        configured = true;
+    }
+    dim3 grid((a.NI + TN - 1) / TN, (a.N0 + TC_W - 1) / TC_W, a.N2);
+    h->launches++;
+    k_hankel_tc<AMODE, CMODE, TN><<<grid, TcShape<TN>::THREADS, smem, h->stream>>>(a);
+    return cudaGetLastError();
 }
 
 template <int AMODE, int CMODE>
 static cudaError_t run_tc(UppeHandle* h, TcArgs& a) {
-    static bool configured = false;
-    const size_t smem = tc_smem_bytes();
-    if (!configured) {
-        cudaError_t e = cudaFuncSetAttribute(k_hankel_tc<AMODE, CMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-        configured = true;
-    }
-    dim3 grid((a.NI + TC_N - 1) / TC_N, (a.N0 + TC_W - 1) / TC_W, a.N2);
-    h->launches++;
-    k_hankel_tc<AMODE, CMODE><<<grid, TC_THREADS, smem, h->stream>>>(a);
-    return cudaGetLastError();
+    return h->tc_tile64 ? run_tc_shape<AMODE, CMODE, 64>(h, a) : run_tc_shape<AMODE, CMODE, 128>(h, a);
 }
 
 // Entry used by hankel.cu in the mixed-precision form.  amode/cmode follow hankel.cu's A_*/C_* codes
