@@ -216,11 +216,6 @@ extern "C" int uppe_create(const UppeConfig* cfg, UppeHandle** out) {
     if (const char* v = getenv("SEARAY_UPPE_TC_NEXT")) {
         if (strcmp(v, "0") == 0) h->tc_next = 0;
     }
-    // tensor-core Hankel GEMM output tiles: 128 columns, or 64 (SEARAY_UPPE_TC_N=64)
-    h->tc_tile64 = 0;
-    if (const char* v = getenv("SEARAY_UPPE_TC_N")) {
-        if (strcmp(v, "64") == 0) h->tc_tile64 = 1;
-    }
     // 256 x 256 slices: the three-pass tail; SEARAY_UPPE_CLUSTER=1 selects the cluster-fused tail
     // (slice_cluster.cu: one launch, 40-48 bytes per point, but measured twice as slow)
     h->slice_cluster = 0;

@@ -80,9 +80,11 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t phase, int* er
 }
 
 // Output-tile shapes of the GEMM: TN = 128 columns per tile, 512 threads, three 64 KB stages, one
-// block per multiprocessor; TN = 64, 256 threads, two 48 KB stages, two blocks per multiprocessor
-// (twice the tiles in flight for the same grid).  A stage is [A_hi | A_lo | B_hi | B_lo]; a B tile of
-// TN rows is the upper or lower half (contiguous 8 KB) of the 128-row split matrix tiles.
+// block per multiprocessor (the shape in use); TN = 64, 256 threads, two 48 KB stages, two blocks
+// per multiprocessor, gave the same results bit for bit but ran slower (18.7 against 15.7 us per
+// inverse transform at 2049 x 512: every A tile is fetched by twice as many blocks).  A stage is
+// [A_hi | A_lo | B_hi | B_lo]; a B tile of TN rows is the upper or lower half (contiguous 8 KB) of the
+// 128-row split matrix tiles.
 template <int TN>
 struct TcShape {
     static constexpr int THREADS = TN == 128 ? 512 : 256;
@@ -363,7 +365,7 @@ static cudaError_t run_tc_shape(UppeHandle* h, TcArgs& a) {
 
 template <int AMODE, int CMODE>
 static cudaError_t run_tc(UppeHandle* h, TcArgs& a) {
-    return h->tc_tile64 ? run_tc_shape<AMODE, CMODE, 64>(h, a) : run_tc_shape<AMODE, CMODE, 128>(h, a);
+    return run_tc_shape<AMODE, CMODE, 128>(h, a);
 }
 
 // Entry used by hankel.cu in the mixed-precision form.  amode/cmode follow hankel.cu's A_*/C_* codes

@@ -21,7 +21,7 @@
 // Per column: stage E (rows of NC columns, cp.async), pack and inverse-transform it in registers,
 // park e (time order, column-contiguous) in a global scratch array, stage G, pack and inverse-
 // transform it, form ge against the parked e, forward-transform ge and write gE.  Same block shape,
-// shared-memory column buffers and register budget as k_time_reg (two blocks per multiprocessor).
+// shared-memory column buffers and register budget as k_time_reg.
 #include <math.h>
 
 #include "time_common.cuh"
@@ -29,13 +29,13 @@
 #include "uppe_internal.h"
 
 template <int LOGM>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, TReg<LOGM>::MINB)
     k_time_adj_reg(const float2* __restrict__ E, const float2* __restrict__ Gc, float2* __restrict__ gE,
                    const float* __restrict__ ng, const float* __restrict__ wv, const float2* __restrict__ twt,
                    float2* __restrict__ park_all, int* __restrict__ list, TimeParams tp,
                    double* __restrict__ dred) {
     using G = TReg<LOGM>;
-    constexpr int M = G::M, TC = G::TC, R1 = G::R1, NB = G::NB, NC = G::NC, LD = G::LD;
+    constexpr int M = G::M, TC = G::TC, R1 = G::R1, NC = G::NC, LD = G::LD;
     constexpr int CA = 2048 / M, NG = NC / CA;  // k_time_adj's group width; groups per block
     static_assert(NG * CA == NC && NG >= 1 && (TC == 32 || CA >= 2), "groups hold whole warps");
     extern __shared__ float2 sm[];
@@ -98,9 +98,7 @@ __global__ void __launch_bounds__(256, 2)
     float2* park = park_all + col * (size_t)M;
     if (!skip) {
 #pragma unroll
-        for (int j = 0; j < NB; ++j)
-#pragma unroll
-            for (int c = 0; c < TC; ++c) park[t + TC * j + R1 * c] = v[j * TC + c];
+        for (int r = 0; r < R1; ++r) park[G::tm(t, r)] = v[r];
     }
     __syncthreads();  // every column's exchange reads of its buffer are done
 
@@ -123,16 +121,14 @@ __global__ void __launch_bounds__(256, 2)
         });
         // ge = 3 kerr e^2 gp against the parked e (this lane's own entries)
 #pragma unroll
-        for (int j = 0; j < NB; ++j)
-#pragma unroll
-            for (int c = 0; c < TC; ++c) {
-                const float2 z = park[t + TC * j + R1 * c];
-                const float2 gp = v[j * TC + c];
-                const float e0 = z.x * inv, e1 = z.y * inv;
-                dpart = fmaf(gp.x * ngc * e0 * e0, e0, dpart);
-                dpart = fmaf(gp.y * ngc * e1 * e1, e1, dpart);
-                v[j * TC + c] = make_float2(3.f * kerr * e0 * e0 * gp.x, 3.f * kerr * e1 * e1 * gp.y);
-            }
+        for (int r = 0; r < R1; ++r) {
+            const float2 z = park[G::tm(t, r)];
+            const float2 gp = v[r];
+            const float e0 = z.x * inv, e1 = z.y * inv;
+            dpart = fmaf(gp.x * ngc * e0 * e0, e0, dpart);
+            dpart = fmaf(gp.y * ngc * e1 * e1, e1, dpart);
+            v[r] = make_float2(3.f * kerr * e0 * e0 * gp.x, 3.f * kerr * e1 * e1 * gp.y);
+        }
         // gE = (1/Nt) W2 rfft(ge)
         tr_forward<LOGM>(v, buf, twF, t);
         __syncwarp();  // the exchange reads of buf are done before the output staging
@@ -165,8 +161,14 @@ int time_adj_reg_group(int M) { return 2048 / M; }
 
 size_t time_adj_reg_list_len(const UppeHandle* h) { return 1 + (size_t)h->S / (2048 / h->M); }
 
+// The register pass takes a grid only when its blocks (NC columns each) fill the multiprocessors:
+// on small transverse grids (256 radial points: 32 blocks at M = 1024) the shared-memory kernel's
+// narrower blocks (2048 / M columns) spread the work wider and ran faster (forward+adjoint at
+// 1025 x 256: 6.97e8 grid-pt steps/s with it, 6.42e8 with the register pass).
 bool time_adj_reg_ready(const UppeHandle* h) {
-    return h->time_reg && h->tw_reg && h->adj_live && (h->tscr || h->adj_park) && time_reg_supported(h);
+    const int nc = h->M == 1024 ? TReg<10>::NC : h->M == 512 ? TReg<9>::NC : TReg<8>::NC;
+    return h->time_reg && h->tw_reg && h->adj_live && (h->tscr || h->adj_park) && time_reg_supported(h) &&
+           h->S / nc >= h->num_sms;
 }
 
 cudaError_t uppe_configure_time_adj_reg() {

@@ -36,12 +36,12 @@
 #include "uppe_internal.h"
 
 template <int LOGM>
-__global__ void __launch_bounds__(256, 2)
+__global__ void __launch_bounds__(256, TReg<LOGM>::MINB)
     k_time_reg(const float2* __restrict__ E, float2* __restrict__ Jout, const float* __restrict__ ng,
                const float* __restrict__ wv, const float2* __restrict__ twt,
                float2* __restrict__ tscr, TimeParams tp) {
     using G = TReg<LOGM>;
-    constexpr int M = G::M, TC = G::TC, R1 = G::R1, NB = G::NB, NC = G::NC, LD = G::LD;
+    constexpr int M = G::M, TC = G::TC, R1 = G::R1, NC = G::NC, LD = G::LD;
     extern __shared__ float2 sm[];
     const int tid = threadIdx.x;
     const size_t S = (size_t)tp.S;
@@ -92,15 +92,13 @@ __global__ void __launch_bounds__(256, 2)
         // rates in natural order (padded positions)
         __syncwarp();  // exchange reads of buf are done
 #pragma unroll
-        for (int j = 0; j < NB; ++j)
-#pragma unroll
-            for (int c = 0; c < TC; ++c) {
-                const int m = t + TC * j + R1 * c;
-                const float2 z = v[j * TC + c];
-                const float r0 = ion_rate(tp, z.x * inv);
-                const float r1 = (2 * m + 1 == G::NT - 1) ? 0.f : ion_rate(tp, z.y * inv);
-                buf[tr_pad<G::LSEG>(m)] = make_float2(r0, r1);
-            }
+        for (int r = 0; r < R1; ++r) {
+            const int m = G::tm(t, r);
+            const float2 z = v[r];
+            const float r0 = ion_rate(tp, z.x * inv);
+            const float r1 = (2 * m + 1 == G::NT - 1) ? 0.f : ion_rate(tp, z.y * inv);
+            buf[tr_pad<G::LSEG>(m)] = make_float2(r0, r1);
+        }
         __syncwarp();
         // density: lane t scans the pairs [t SEG, (t+1) SEG) from high to low time
         const int mb = t * G::SEG;
@@ -158,15 +156,13 @@ __global__ void __launch_bounds__(256, 2)
         __syncwarp();
         // Jpl = ne E, parked in time order; P = chi E in registers
 #pragma unroll
-        for (int j = 0; j < NB; ++j)
-#pragma unroll
-            for (int c = 0; c < TC; ++c) {
-                const int m = t + TC * j + R1 * c;
-                const float2 ne = buf[tr_pad<G::LSEG>(m)];
-                const float e0 = v[j * TC + c].x * inv, e1 = v[j * TC + c].y * inv;
-                park[m] = make_float2(ne.x * e0, ne.y * e1);
-                v[j * TC + c] = make_float2(kerr * e0 * e0 * e0, kerr * e1 * e1 * e1);
-            }
+        for (int r = 0; r < R1; ++r) {
+            const int m = G::tm(t, r);
+            const float2 ne = buf[tr_pad<G::LSEG>(m)];
+            const float e0 = v[r].x * inv, e1 = v[r].y * inv;
+            park[m] = make_float2(ne.x * e0, ne.y * e1);
+            v[r] = make_float2(kerr * e0 * e0 * e0, kerr * e1 * e1 * e1);
+        }
     } else {
 #pragma unroll
         for (int r = 0; r < R1; ++r) {
@@ -192,9 +188,7 @@ __global__ void __launch_bounds__(256, 2)
         // Jpl from its parking place (this lane's own entries), forward transform, and
         // J += Jpl(w) (damping + i w) / (damping^2 + w^2) (x filter)
 #pragma unroll
-        for (int j = 0; j < NB; ++j)
-#pragma unroll
-            for (int c = 0; c < TC; ++c) v[j * TC + c] = park[t + TC * j + R1 * c];
+        for (int r = 0; r < R1; ++r) v[r] = park[G::tm(t, r)];
         tr_forward<LOGM>(v, buf, twF, t);
         __syncwarp();
         const float damp = tp.damping;
@@ -222,7 +216,7 @@ __global__ void __launch_bounds__(256, 2)
 bool time_reg_supported(const UppeHandle* h) {
     if (h->cfg.envelope || h->rot_pairs > 0) return false;
     if (h->M != 256 && h->M != 512 && h->M != 1024) return false;
-    const int nc = (h->M == 1024) ? TReg<10>::NC : TReg<9>::NC;
+    const int nc = (h->M == 1024) ? TReg<10>::NC : (h->M == 512) ? TReg<9>::NC : TReg<8>::NC;
     return h->S % nc == 0;
 }
 
@@ -251,10 +245,16 @@ int time_reg_tables(int M, float2* host) {
     };
     for (int b = 0; b < R1; ++b)
         for (int t = 0; t < TC; ++t) host[b * TC + t] = w((long long)t * b, M);
-    const int NB = R1 / TC;
-    for (int j = 0; j < NB; ++j)
-        for (int k1 = 0; k1 < TC; ++k1)
-            for (int t = 0; t < TC; ++t) host[M + (j * TC + k1) * TC + t] = w((long long)(t + TC * j) * k1, M);
+    if (TC > R1) {
+        // lane pairs (TC = 2 R1): twF[i TC + t] = W_M^(b (2 i + h)), t = b + R1 h
+        for (int i = 0; i < R1; ++i)
+            for (int t = 0; t < TC; ++t) host[M + i * TC + t] = w((long long)(t % R1) * (2 * i + t / R1), M);
+    } else {
+        const int NB = R1 / TC;
+        for (int j = 0; j < NB; ++j)
+            for (int k1 = 0; k1 < TC; ++k1)
+                for (int t = 0; t < TC; ++t) host[M + (j * TC + k1) * TC + t] = w((long long)(t + TC * j) * k1, M);
+    }
     for (int a = 0; a < R1; ++a)
         for (int t = 0; t < TC; ++t) host[2 * M + a * TC + t] = w(t + (long long)TC * a, 2 * M);
     return 0;

@@ -13,17 +13,19 @@
 
 template <int LOGM>
 struct TRegShape;
+// TC lanes per column, R1 complex values per lane, NC columns per 256-thread block, MINB blocks per
+// multiprocessor (the register budget: 128 registers at 2, 64 at 4).
 template <>
 struct TRegShape<8> {
-    static constexpr int TC = 16, R1 = 16, NC = 16;
+    static constexpr int TC = 16, R1 = 16, NC = 16, MINB = 2;
 };
 template <>
 struct TRegShape<9> {
-    static constexpr int TC = 16, R1 = 32, NC = 16;
+    static constexpr int TC = 32, R1 = 16, NC = 8, MINB = 3;
 };
 template <>
 struct TRegShape<10> {
-    static constexpr int TC = 32, R1 = 32, NC = 8;
+    static constexpr int TC = 32, R1 = 32, NC = 8, MINB = 2;
 };
 
 __host__ __device__ constexpr int tr_max(int a, int b) { return a > b ? a : b; }
@@ -33,7 +35,11 @@ template <int LOGM>
 struct TReg {
     static constexpr int M = 1 << LOGM, NT = 2 * M;
     static constexpr int TC = TRegShape<LOGM>::TC, R1 = TRegShape<LOGM>::R1, NC = TRegShape<LOGM>::NC;
-    static constexpr int NB = R1 / TC;
+    // H = 1: R1 = NB TC, lane t holds the time lines b = t + TC j; H = 2: TC = 2 R1, the lane pair
+    // (b, h = 0, 1) shares line b (the TC-point DFT over c split into a radix-2 step across the pair)
+    static constexpr int H = TC > R1 ? TC / R1 : 1;
+    static constexpr int NB = TC > R1 ? 1 : R1 / TC;
+    static constexpr int MINB = TRegShape<LOGM>::MINB;
     static constexpr int THREADS = NC * TC;
     static constexpr int SEG = M / TC;  // packed pairs per lane in the contiguous (scan) layout
     static constexpr int LSEG = tr_log2(SEG);
@@ -44,8 +50,40 @@ struct TReg {
     static constexpr int LD0 = tr_max(tr_max(M + 1, R1 * (TC + 1)), tr_max(TC * (R1 + 1), M + M / SEG));
     static constexpr int LD = (NC == 16) ? (LD0 | 1) : ((LD0 + 13) / 16) * 16 + 2;
     static constexpr size_t SMEM = (size_t)NC * LD * sizeof(float2);
-    static_assert(NB * TC == R1 && THREADS == 256 && (NC == 16 || NC == 8) && LD >= LD0, "time-pass shape");
+    static_assert((H == 1 ? NB * TC == R1 : (H == 2 && 2 * R1 == TC && R1 == 16)) && THREADS == 256 &&
+                      (NC == 16 || NC == 8) && LD >= LD0,
+                  "time-pass shape");
+    // T layout: the time pair m held in register r of lane t
+    static UPPE_DEV int tm(int t, int r) {
+        if constexpr (H == 1)
+            return t + TC * (r / TC) + R1 * (r % TC);
+        else
+            return (t % R1) + R1 * (R1 * (t / R1) + r);
+    }
 };
+
+// The radix-2 step of a 32-point DFT split over a lane pair (lanes t and t ^ 16 hold the two
+// halves of one line): W32^C constants per register, C = 0 .. 15.
+template <int C, bool INV>
+UPPE_DEV void tr_pair_inverse(float2 (&v)[16], bool h) {
+    if constexpr (C < 16) {
+        // z[c] = E0[c] + W32^-c E1[c], z[c + 16] = E0[c] - W32^-c E1[c]: lane h = 0 keeps the first
+        const float2 p = make_float2(__shfl_xor_sync(0xffffffffu, v[C].x, 16), __shfl_xor_sync(0xffffffffu, v[C].y, 16));
+        const float2 e = h ? p : v[C];
+        const float2 o = mul_w32<C, INV>(h ? v[C] : p);
+        v[C] = h ? csub(e, o) : cadd(e, o);
+        tr_pair_inverse<C + 1, INV>(v, h);
+    }
+}
+template <int C>
+UPPE_DEV void tr_pair_forward(float2 (&v)[16], bool h) {
+    if constexpr (C < 16) {
+        // even outputs from x0 + x1 (lane h = 0), odd ones from (x0 - x1) W32^c (lane h = 1)
+        const float2 p = make_float2(__shfl_xor_sync(0xffffffffu, v[C].x, 16), __shfl_xor_sync(0xffffffffu, v[C].y, 16));
+        v[C] = h ? mul_w32<C, false>(csub(p, v[C])) : cadd(v[C], p);
+        tr_pair_forward<C + 1>(v, h);
+    }
+}
 
 // natural pair index m -> padded position in the column buffer (a pad after every SEG pairs keeps
 // both the lane-consecutive and the segment-strided accesses conflict-free)
@@ -54,10 +92,39 @@ UPPE_DEV int tr_pad(int m) {
     return m + (m >> LSEG);
 }
 
+template <int LOGM>
+UPPE_DEV void tr_forward_lines(float2 (&v)[TReg<LOGM>::R1], float2* buf, const float2* __restrict__ twF, int t);
+
 // Forward transform of the packed sequence in the T layout (v[j TC + c] = z[t + TC j + R1 c]) into
 // the F layout (v[a] = Z[t + TC a]); buf is the column's buffer, twF the forward twiddles.
 template <int LOGM>
 UPPE_DEV void tr_forward(float2 (&v)[TReg<LOGM>::R1], float2* buf, const float2* __restrict__ twF, int t) {
+    using G = TReg<LOGM>;
+    if constexpr (G::H == 2) {
+        // lane t = b + R1 h holds z[b + R1 (R1 h + c)]: radix-2 across the pair, R1-point DFT over c,
+        // giving Y_b[k1] for k1 = 2 i + h; then W_M^(b k1) (twF[i TC + t])
+        const int b = t % G::R1;
+        const bool h = t >= G::R1;
+        tr_pair_forward<0>(v, h);
+        dft_at<G::R1, 0, false>(v);
+#pragma unroll
+        for (int i = 0; i < G::R1; ++i) v[i] = cmul(v[i], __ldg(&twF[i * G::TC + t]));
+        __syncwarp();  // the column's earlier reads of buf are done
+#pragma unroll
+        for (int i = 0; i < G::R1; ++i) buf[(2 * i + (h ? 1 : 0)) * (G::R1 + 1) + b] = v[i];
+        __syncwarp();
+        // lane t = k1 takes every b; R1-point DFT over b -> k2: Z[t + TC k2]
+#pragma unroll
+        for (int bb = 0; bb < G::R1; ++bb) v[bb] = buf[t * (G::R1 + 1) + bb];
+        dft_at<G::R1, 0, false>(v);
+    } else {
+        tr_forward_lines<LOGM>(v, buf, twF, t);
+    }
+}
+
+// tr_forward for H = 1: lane t holds whole time lines.
+template <int LOGM>
+UPPE_DEV void tr_forward_lines(float2 (&v)[TReg<LOGM>::R1], float2* buf, const float2* __restrict__ twF, int t) {
     using G = TReg<LOGM>;
     // stage 1: TC-point DFTs over c -> k1, then W_M^(b k1), b = t + TC j
     dft_at<G::TC, 0, false>(v);
@@ -138,10 +205,21 @@ UPPE_DEV void tr_pack_inverse(float2 (&v)[TReg<LOGM>::R1], float2* buf, const fl
 #pragma unroll
     for (int b = 0; b < R1; ++b) buf[b * (TC + 1) + t] = v[b];
     __syncwarp();
+    if constexpr (G::H == 2) {
+        // lane b + R1 h: the R1-point DFT of line b over the lanes t = h + 2 i, then the radix-2 step
+        // across the pair: v[c] = z[b + R1 (R1 h + c)]
+        const int b = t % R1;
+        const bool h = t >= R1;
 #pragma unroll
-    for (int j = 0; j < NB; ++j)
+        for (int i = 0; i < R1; ++i) v[i] = buf[b * (TC + 1) + (h ? 1 : 0) + 2 * i];
+        dft_at<R1, 0, true>(v);
+        tr_pair_inverse<0, true>(v, h);
+    } else {
 #pragma unroll
-        for (int tt = 0; tt < TC; ++tt) v[j * TC + tt] = buf[(t + TC * j) * (TC + 1) + tt];
-    dft_at<TC, 0, true>(v);
-    if constexpr (NB == 2) dft_at<TC, TC, true>(v);
+        for (int j = 0; j < NB; ++j)
+#pragma unroll
+            for (int tt = 0; tt < TC; ++tt) v[j * TC + tt] = buf[(t + TC * j) * (TC + 1) + tt];
+        dft_at<TC, 0, true>(v);
+        if constexpr (NB == 2) dft_at<TC, TC, true>(v);
+    }
 }

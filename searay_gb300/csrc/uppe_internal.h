@@ -60,7 +60,6 @@ struct UppeHandle {
     int time_reg;                  // TIME_J through the register-resident time pass where it applies (timepass_reg.cu)
     int slice_cluster;             // 256 x 256 slices: the fused tail in one cluster launch (slice_cluster.cu)
     int tc_next;                   // tensor-core Hankel: stage updates write the next inverse transform's operand
-    int tc_tile64;                 // tensor-core Hankel GEMM with 64-column output tiles (two blocks per multiprocessor)
     cudaStream_t stream;
     // library-owned device buffers
     float2 *q, *qi, *qf, *k1, *E, *J, *scratch;

@@ -126,7 +126,7 @@ def _adjoint_step(vd, g, a, lam, form, ionizing, chi3, monkeypatch):
 
 
 @pytest.mark.parametrize("ionizing", [True, False], ids=["ionizing", "kerr"])
-@pytest.mark.parametrize("n0,n_perp", [(257, 16), (513, 32), (1025, 16)])
+@pytest.mark.parametrize("n0,n_perp", [(257, 64), (513, 64), (1025, 64)])
 def test_register_adjoint_time_pass_matches_shared_memory_form(n0, n_perp, ionizing, monkeypatch):
     """The vector-Jacobian product of one RK4 step with the register-resident adjoint time pass
     (timepass_adj_reg.cu: the column groups without ionization; the groups with a nonzero rate go to
@@ -138,7 +138,8 @@ def test_register_adjoint_time_pass_matches_shared_memory_form(n0, n_perp, ioniz
     on the chi3 derivative.  Kerr coefficient at 30x the workload's, so that the nonlinear part is
     a measurable share of the cotangent (the linear part is the same code, bit for bit, in both
     forms).  With ionization the register form launches one more kernel per
-    stage (the listed groups), which shows both kernels ran."""
+    stage (the listed groups), which shows both kernels ran.  64 x 64 columns: the register pass takes
+    grids whose blocks fill the multiprocessors."""
     from searay_gb300 import grid, workloads
     vd = workloads.cart_filament_128(steps=400, n_perp=n_perp)
     vd["wave grid"] = (n0, n_perp, n_perp, 2)
