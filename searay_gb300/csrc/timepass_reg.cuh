@@ -14,7 +14,7 @@
 template <int LOGM>
 struct TRegShape;
 // TC lanes per column, R1 complex values per lane, NC columns per 256-thread block, MINB blocks per
-// multiprocessor (the register budget: 128 registers at 2, 64 at 4).
+// multiprocessor (the register budget: 128 registers at 2, 80 at 3).
 template <>
 struct TRegShape<8> {
     static constexpr int TC = 16, R1 = 16, NC = 16, MINB = 2;
@@ -27,6 +27,7 @@ template <>
 struct TRegShape<10> {
     static constexpr int TC = 32, R1 = 32, NC = 8, MINB = 2;
 };
+
 
 __host__ __device__ constexpr int tr_max(int a, int b) { return a > b ? a : b; }
 __host__ __device__ constexpr int tr_log2(int n) { return n <= 1 ? 0 : 1 + tr_log2(n / 2); }
@@ -178,25 +179,12 @@ UPPE_DEV void tr_unpack(const float2 (&v)[TReg<LOGM>::R1], const float2* __restr
 // at k = 0 and M do not enter irfft), into the F layout, then the inverse transform into the T
 // layout: v[j TC + c] = z[t + TC j + R1 c] with z[m] = Nt (x(2m) + i x(2m+1)) of x = irfft(X).
 // xk reads the column's staged spectrum from buf; every read is done before buf serves the exchange.
-template <int LOGM, class XK>
-UPPE_DEV void tr_pack_inverse(float2 (&v)[TReg<LOGM>::R1], float2* buf, const float2* __restrict__ twI,
-                              const float2* __restrict__ twP, int t, XK xk) {
+// Inverse transform from the F layout (v[a] = Z[t + TC a]) into the T layout; every earlier read of
+// buf by the column is done before buf serves the exchange.
+template <int LOGM>
+UPPE_DEV void tr_inverse(float2 (&v)[TReg<LOGM>::R1], float2* buf, const float2* __restrict__ twI, int t) {
     using G = TReg<LOGM>;
-    constexpr int TC = G::TC, R1 = G::R1, NB = G::NB, M = G::M;
-    // Z[k] = (X[k] + conj X[M-k]) + i e^{2 pi i k/Nt} (X[k] - conj X[M-k])
-#pragma unroll
-    for (int a = 0; a < R1; ++a) {
-        const int k = t + TC * a;
-        float2 Xa = xk(k);
-        float2 Xm = xk(M - k);
-        if (a == 0 && t == 0) {
-            Xa.y = 0.f;
-            Xm.y = 0.f;
-        }
-        const float2 tk = cconj(__ldg(&twP[a * TC + t]));  // e^{+2 pi i k / Nt}
-        const float2 b = cconj(Xm);
-        v[a] = cadd(cadd(Xa, b), cmul_i(cmul(tk, csub(Xa, b))));
-    }
+    constexpr int TC = G::TC, R1 = G::R1, NB = G::NB;
     // R1-point DFT over a, twiddle, exchange, TC-point DFTs over t
     dft_at<R1, 0, true>(v);
 #pragma unroll
@@ -222,4 +210,26 @@ UPPE_DEV void tr_pack_inverse(float2 (&v)[TReg<LOGM>::R1], float2* buf, const fl
         dft_at<TC, 0, true>(v);
         if constexpr (NB == 2) dft_at<TC, TC, true>(v);
     }
+}
+
+template <int LOGM, class XK>
+UPPE_DEV void tr_pack_inverse(float2 (&v)[TReg<LOGM>::R1], float2* buf, const float2* __restrict__ twI,
+                              const float2* __restrict__ twP, int t, XK xk) {
+    using G = TReg<LOGM>;
+    constexpr int TC = G::TC, R1 = G::R1, M = G::M;
+    // Z[k] = (X[k] + conj X[M-k]) + i e^{2 pi i k/Nt} (X[k] - conj X[M-k])
+#pragma unroll
+    for (int a = 0; a < R1; ++a) {
+        const int k = t + TC * a;
+        float2 Xa = xk(k);
+        float2 Xm = xk(M - k);
+        if (a == 0 && t == 0) {
+            Xa.y = 0.f;
+            Xm.y = 0.f;
+        }
+        const float2 tk = cconj(__ldg(&twP[a * TC + t]));  // e^{+2 pi i k / Nt}
+        const float2 b = cconj(Xm);
+        v[a] = cadd(cadd(Xa, b), cmul_i(cmul(tk, csub(Xa, b))));
+    }
+    tr_inverse<LOGM>(v, buf, twI, t);
 }
