@@ -251,8 +251,8 @@ def run_device(args, vd, ws, rank, local, precision, per_class=True):
     # forward + adjoint: K_a vector-Jacobian products of the RK4 step (each recomputes its stage
     # states from the step's input, as the checkpointed backward pass does)
     adj = None
-    # the adjoint has no Raman response and no envelope form
-    if args.adjoint_steps > 0 and vd.get("rotator") is None and not is_paraxial(vd):
+    # the adjoint has no envelope form
+    if args.adjoint_steps > 0 and not is_paraxial(vd):
         q = dev.empty_field()
         dev.get_field(q)
         gen = torch.Generator(device="cuda").manual_seed(0)
