@@ -72,13 +72,12 @@ __global__ void __launch_bounds__(256, TReg<LOGM>::MINB)
     const float kerr = ngc * tp.redchi3;
     bool live = false;
     if (tp.rate_form != UPPE_RATE_NONE) {
-        bool any = false;
+        // any sample with Em = fconv |e| + cutoff >= em_min: Em grows with |e| (fconv > 0), so the
+        // largest |e| of the lane decides (the same roundings as per sample)
+        float mx = 0.f;
 #pragma unroll
-        for (int r = 0; r < R1; ++r) {
-            const float em0 = fmaf(tp.fconv, fabsf(v[r].x * inv), tp.cutoff);
-            const float em1 = fmaf(tp.fconv, fabsf(v[r].y * inv), tp.cutoff);
-            any = any || em0 >= tp.em_min || em1 >= tp.em_min;
-        }
+        for (int r = 0; r < R1; ++r) mx = fmaxf(mx, fmaxf(fabsf(v[r].x), fabsf(v[r].y)));
+        const bool any = fmaf(tp.fconv, mx * inv, tp.cutoff) >= tp.em_min;
         live = __any_sync(0xffffffffu, any);  // both columns of a warp when TC = 16: one group
     }
     if (t == 0) col_live[cl] = live ? 1 : 0;

@@ -76,13 +76,12 @@ __global__ void __launch_bounds__(256, TReg<LOGM>::MINB)
     const bool ionize = tp.rate_form != UPPE_RATE_NONE;
     bool live = false;
     if (ionize) {
-        bool any = false;
+        // any sample with Em = fconv |e| + cutoff >= em_min: Em grows with |e| (fconv > 0), so the
+        // largest |e| of the lane decides (the same roundings as per sample)
+        float mx = 0.f;
 #pragma unroll
-        for (int r = 0; r < R1; ++r) {
-            const float em0 = fmaf(tp.fconv, fabsf(v[r].x * inv), tp.cutoff);
-            const float em1 = fmaf(tp.fconv, fabsf(v[r].y * inv), tp.cutoff);
-            any = any || em0 >= tp.em_min || em1 >= tp.em_min;
-        }
+        for (int r = 0; r < R1; ++r) mx = fmaxf(mx, fmaxf(fabsf(v[r].x), fabsf(v[r].y)));
+        const bool any = fmaf(tp.fconv, mx * inv, tp.cutoff) >= tp.em_min;
         live = __any_sync(0xffffffffu, any);  // warp-uniform (both columns of a warp when TC = 16)
     }
     // the column's parking place in the scratch array (ionizing columns only): [0, M) Jpl by m,
