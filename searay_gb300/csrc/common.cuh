@@ -6,6 +6,36 @@
 
 #define UPPE_DEV __device__ __forceinline__
 
+// Programmatic dependent launch.  A kernel launched with launch_pdl may start (its blocks resident,
+// their set-up done) while the kernel before it in the stream is still draining; it calls
+// pdl_begin() before its first global-memory access.  pdl_begin lets the next kernel of the stream
+// launch once every block of this one has begun (griddepcontrol.launch_dependents: all of this
+// grid's blocks are then resident, so the next grid's waiting blocks can never keep one of them
+// out), then waits for the previous kernel to complete with its memory visible
+// (griddepcontrol.wait; it returns at once when there is none, or the kernel was launched plainly).
+UPPE_DEV void pdl_begin() {
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+}
+
+#ifdef __CUDACC__
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                              Args... args) {
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr.val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+#endif
+
 UPPE_DEV float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 UPPE_DEV float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 UPPE_DEV float2 cmul(float2 a, float2 b) { return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }

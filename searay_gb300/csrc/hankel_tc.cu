@@ -138,6 +138,7 @@ __device__ __forceinline__ void tc_issue(uint32_t tmem_d, uint32_t st_a, uint32_
 // [nwt * 64][nkt * 64] grid; consecutive threads take consecutive k.
 template <int AMODE>
 __global__ void __launch_bounds__(256) k_hankel_tc_prep(TcArgs g, uint8_t* __restrict__ Atc) {
+    pdl_begin();
     const int m = blockIdx.y;
     const int KP = g.nkt * TC_K;
     const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -171,6 +172,7 @@ template <int AMODE, int CMODE, int TN>
 __global__ void __launch_bounds__(TcShape<TN>::THREADS, TcShape<TN>::MINB) k_hankel_tc(TcArgs g) {
     using SH = TcShape<TN>;
     constexpr int NST = SH::NSTAGE, TT = SH::THREADS, LD = SH::LD;
+    pdl_begin();
     static_assert(AMODE == TA_PRESPLIT, "the GEMM reads pre-split operand tiles");
     extern __shared__ __align__(1024) uint8_t smem_raw[];
     // NST pipeline stages of [A_hi | A_lo | B_hi | B_lo] (1024-byte aligned), reused afterwards
@@ -359,7 +361,7 @@ static cudaError_t run_tc_shape(UppeHandle* h, TcArgs& a) {
     }
     dim3 grid((a.NI + TN - 1) / TN, (a.N0 + TC_W - 1) / TC_W, a.N2);
     h->launches++;
-    k_hankel_tc<AMODE, CMODE, TN><<<grid, TcShape<TN>::THREADS, smem, h->stream>>>(a);
+    launch_pdl(k_hankel_tc<AMODE, CMODE, TN>, grid, dim3(TcShape<TN>::THREADS), smem, h->stream, a);
     return cudaGetLastError();
 }
 
@@ -416,13 +418,13 @@ cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* 
         dim3 grid((unsigned)((n + 255) / 256), h->N2);
         h->launches++;
         if (amode == TA_PLAIN)
-            k_hankel_tc_prep<TA_PLAIN><<<grid, 256, 0, h->stream>>>(a, h->Atc);
+            launch_pdl(k_hankel_tc_prep<TA_PLAIN>, grid, dim3(256), 0, h->stream, a, h->Atc);
         else if (amode == TA_QPHASE_IKZ)
-            k_hankel_tc_prep<TA_QPHASE_IKZ><<<grid, 256, 0, h->stream>>>(a, h->Atc);
+            launch_pdl(k_hankel_tc_prep<TA_QPHASE_IKZ>, grid, dim3(256), 0, h->stream, a, h->Atc);
         else if (amode == TA_SADJ)
-            k_hankel_tc_prep<TA_SADJ><<<grid, 256, 0, h->stream>>>(a, h->Atc);
+            launch_pdl(k_hankel_tc_prep<TA_SADJ>, grid, dim3(256), 0, h->stream, a, h->Atc);
         else
-            k_hankel_tc_prep<TA_QPHASE><<<grid, 256, 0, h->stream>>>(a, h->Atc);
+            launch_pdl(k_hankel_tc_prep<TA_QPHASE>, grid, dim3(256), 0, h->stream, a, h->Atc);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }

@@ -66,6 +66,7 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
     // blocks of at most 4 columns)
     const RowSwizzle sw{logC <= 2 ? M - 1 : 0, logC == 0 ? 4 : 3};
 
+    pdl_begin();
     // ---- 1. stage the half spectrum X[k][c], k in [0, M], with asynchronous copies ----
     if (C >= 2) {
         const int hC = C >> 1;  // 16-byte copies of two adjacent columns
@@ -385,20 +386,20 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
 #define UPPE_TIME_RCASE(A_, B_)                                                                                     \
         if (tp.logM == A_ && tp.logC == B_) {                                                                          \
             if (occ2)                                                                                                 \
-                k_time<8, A_, B_, 2><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w, \
+                launch_pdl(k_time<8, A_, B_, 2>, dim3(h->S / h->time_cols), dim3(Tr), smem_r, h->stream, mode, E, out0, out1, h->ng, h->w, \
                                                                                  h->nlfilt, h->tw, h->twLog, tr);    \
             else                                                                                                      \
-                k_time<8, A_, B_, 1><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w, \
+                launch_pdl(k_time<8, A_, B_, 1>, dim3(h->S / h->time_cols), dim3(Tr), smem_r, h->stream, mode, E, out0, out1, h->ng, h->w, \
                                                                                  h->nlfilt, h->tw, h->twLog, tr);    \
             return cudaGetLastError();                                                                             \
         }
         UPPE_TIME_CT(UPPE_TIME_RCASE)
 #undef UPPE_TIME_RCASE
         if (occ2)
-            k_time<8, 0, -1, 2><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w,
+            launch_pdl(k_time<8, 0, -1, 2>, dim3(h->S / h->time_cols), dim3(Tr), smem_r, h->stream, mode, E, out0, out1, h->ng, h->w,
                                                                               h->nlfilt, h->tw, h->twLog, tr);
         else
-            k_time<8, 0, -1, 1><<<h->S / h->time_cols, Tr, smem_r, h->stream>>>(mode, E, out0, out1, h->ng, h->w,
+            launch_pdl(k_time<8, 0, -1, 1>, dim3(h->S / h->time_cols), dim3(Tr), smem_r, h->stream, mode, E, out0, out1, h->ng, h->w,
                                                                               h->nlfilt, h->tw, h->twLog, tr);
         return cudaGetLastError();
     }
@@ -406,17 +407,17 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
     {
 #define UPPE_TIME_CASE(A_, B_)                                                                                      \
         if (tp.logM == A_ && tp.logC == B_) {                                                                          \
-            k_time<8, A_, B_><<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, \
+            launch_pdl(k_time<8, A_, B_>, dim3(h->S / h->time_cols), dim3(T), smem, h->stream, mode, E, out0, out1, h->ng, h->w, h->nlfilt, \
                                                                             h->tw, h->twLog, tp);                    \
             return cudaGetLastError();                                                                             \
         }
         UPPE_TIME_CT(UPPE_TIME_CASE)
 #undef UPPE_TIME_CASE
-        k_time<8><<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
+        launch_pdl(k_time<8>, dim3(h->S / h->time_cols), dim3(T), smem, h->stream, mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
                                                                h->twLog, tp);
     }
     else
-        k_time<16><<<h->S / h->time_cols, T, smem, h->stream>>>(mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
+        launch_pdl(k_time<16>, dim3(h->S / h->time_cols), dim3(T), smem, h->stream, mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
                                                                 h->twLog, tp);
     return cudaGetLastError();
 }

@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(256, TReg<LOGM>::MINB)
     const size_t S = (size_t)tp.S;
     const size_t col0 = (size_t)blockIdx.x * NC;
 
+    pdl_begin();
     // ---- stage the NC half spectra X[k][c] (k <= M) into the column buffers ----
     for (int i = tid; i < (M + 1) * NC; i += G::THREADS) {
         const int c = i & (NC - 1), k = i / NC;
@@ -275,16 +276,13 @@ cudaError_t launch_time_reg(UppeHandle* h, const float2* E, float2* J) {
     h->launches++;
     switch (h->M) {
         case 256:
-            k_time_reg<8><<<h->S / TReg<8>::NC, TReg<8>::THREADS, TReg<8>::SMEM, h->stream>>>(
-                E, J, h->ng, h->w, h->tw_reg, h->tscr, tp);
+            launch_pdl(k_time_reg<8>, dim3(h->S / TReg<8>::NC), dim3(TReg<8>::THREADS), TReg<8>::SMEM, h->stream, E, J, h->ng, h->w, h->tw_reg, h->tscr, tp);
             break;
         case 512:
-            k_time_reg<9><<<h->S / TReg<9>::NC, TReg<9>::THREADS, TReg<9>::SMEM, h->stream>>>(
-                E, J, h->ng, h->w, h->tw_reg, h->tscr, tp);
+            launch_pdl(k_time_reg<9>, dim3(h->S / TReg<9>::NC), dim3(TReg<9>::THREADS), TReg<9>::SMEM, h->stream, E, J, h->ng, h->w, h->tw_reg, h->tscr, tp);
             break;
         default:
-            k_time_reg<10><<<h->S / TReg<10>::NC, TReg<10>::THREADS, TReg<10>::SMEM, h->stream>>>(
-                E, J, h->ng, h->w, h->tw_reg, h->tscr, tp);
+            launch_pdl(k_time_reg<10>, dim3(h->S / TReg<10>::NC), dim3(TReg<10>::THREADS), TReg<10>::SMEM, h->stream, E, J, h->ng, h->w, h->tw_reg, h->tscr, tp);
             break;
     }
     return cudaGetLastError();

@@ -401,6 +401,7 @@ __global__ void k_adj_rk(int mode, const float2* __restrict__ lam_out, float2* _
 __global__ void k_spec_point(int mode, const float2* __restrict__ C, OpView opv, float2* __restrict__ q_out,
                              float2* __restrict__ qf, const float2* __restrict__ qi, float Cs, float Ce, StepArgs z,
                              size_t n, int S, TcNext nx) {
+    pdl_begin();
     const PhaseArgs pa{z.zhi, z.zlo, z.plain};
     const PhaseArgs pn{nx.z.zhi, nx.z.zlo, nx.z.plain};
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
@@ -422,8 +423,8 @@ cudaError_t launch_spec_point(UppeHandle* h, int mode, const float2* C, float2* 
     TcNext nx{};
     if (z_next) nx = hankel_tc_next(h, *z_next);
     h->launches++;
-    k_spec_point<<<reduce_blocks_host(h->P), 256, 0, h->stream>>>(mode, C, uppe_op_view(h), q_out, qf, qi, Cs, Ce, z,
-                                                                   h->P, h->S, nx);
+    launch_pdl(k_spec_point, dim3(reduce_blocks_host(h->P)), dim3(256), 0, h->stream, mode, C, uppe_op_view(h), q_out,
+               qf, qi, Cs, Ce, z, h->P, h->S, nx);
     cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && z_next) {
         h->atc_next = 1;
