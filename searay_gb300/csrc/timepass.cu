@@ -604,7 +604,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
                     chiR[2 * k] = chi0;
                     chiR[2 * k + 1] = chi1;
                 });
-    #pragma unroll
+#pragma unroll
             for (int k = 0; k < MPS; ++k) {
                 const float2 zv = Ze[sw(m0 + k) * C + c], gv = Zp[sw(m0 + k) * C + c];
                 ybar[2 * k] = gv.x * zv.x * inv;
@@ -612,7 +612,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
             }
             raman_adjoint_pass<16>(tp, Rs, tot, C, logC, T, tid, seg, ngc, ybar, Fbar);
             const float two_nt = 2.f * (float)Nt;
-    #pragma unroll
+#pragma unroll
             for (int k = 0; k < MPS; ++k) {
                 const float2 zv = Ze[sw(m0 + k) * C + c], gv = Zp[sw(m0 + k) * C + c];
                 Zr[sw(m0 + k) * C + c] = make_float2(fmaf(chiR[2 * k], gv.x, two_nt * zv.x * Fbar[2 * k]),
@@ -628,7 +628,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
             if (t1 <= Nt - 2) r_next = ion_rate(tp, Ze[sw(t1 >> 1) * C + c].x * inv);
             float rn = r_next;
             bool live = r_next != 0.f;
-    #pragma unroll 1
+#pragma unroll 1
             for (int j = MPS - 1; j >= 0; --j) {
                 const int m = m0 + j;
                 const float2 zv = Ze[sw(m) * C + c];
@@ -646,7 +646,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
         if (ion) {
             ffloat Sacc = later_segments_sum(part, ffloat{0.f, 0.f}, tot, C, logC, T, tid, ffsum);
             float rn = r_next;
-    #pragma unroll 1
+#pragma unroll 1
             for (int j = MPS - 1; j >= 0; --j) {
                 const int m = m0 + j;
                 const float2 rr = Zn[sw(m) * C + c];
@@ -672,7 +672,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
         ffloat carry = {0.f, 0.f};
         if (ion) {
             ffloat part = {0.f, 0.f};
-    #pragma unroll 1
+#pragma unroll 1
             for (int j = 0; j < MPS; ++j) {
                 const int m = m0 + j;
                 const float2 e2 = Ze[sw(m) * C + c], l2 = Zl[sw(m) * C + c], s2 = Zn[sw(m) * C + c];
@@ -687,7 +687,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
         float dred_part = 0.f;
         {
             ffloat Pprev = carry;  // Pfx(t - 1)
-    #pragma unroll 1
+#pragma unroll 1
             for (int j = 0; j < MPS; ++j) {
                 const int m = m0 + j;
                 const float2 e2 = Ze[sw(m) * C + c];
@@ -701,7 +701,7 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
                     l2 = Zl[sw(m) * C + c];
                     s2 = Zn[sw(m) * C + c];
                 }
-    #pragma unroll
+#pragma unroll
                 for (int h = 0; h < 2; ++h) {
                     const int t = 2 * m + h;
                     const float e = ev[h];
