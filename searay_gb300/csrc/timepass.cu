@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(ET == 16 ? 256 : 512,
         const int hC = C >> 1;  // 16-byte copies of two adjacent columns
         for (int it = tid; it < (M + 1) * hC; it += T) {
             const int c2 = it & (hC - 1);
-            const int k = it >> (logC - 1);
+            const int k = it >> (logC > 0 ? logC - 1 : 0);  // (this branch runs only with C >= 2)
             cp_async16_time(&Zj[sw(k) * C + 2 * c2], &E[(size_t)k * S + col0 + 2 * c2]);
         }
     } else {
@@ -370,8 +370,9 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
     // SEARAY_UPPE_TIME=smem selects the shared-memory form below for every grid
     if (mode == TIME_J && h->time_reg && h->tw_reg && time_reg_supported(h)) return launch_time_reg(h, E, out0);
     const TimeParams tp = uppe_time_params(h);
-    const int T = h->Nt * h->time_cols / h->time_spt;
-    const size_t smem = ((size_t)(h->M + 1) * 2 * h->time_cols + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
+    const int C = h->time_cols;
+    const int T = h->Nt * C / h->time_spt;
+    const size_t smem = ((size_t)(h->M + 1) * 2 * C + h->Nt / 2) * sizeof(float2) + (size_t)T * sizeof(ffloat);
     h->launches++;
     if (h->rot_pairs > 0) {  // 16 samples per thread; Zr and the pair tables after the segment totals
         TimeParams tr = tp;
@@ -407,17 +408,17 @@ cudaError_t launch_time_pass(UppeHandle* h, int mode, const float2* E, float2* o
     {
 #define UPPE_TIME_CASE(A_, B_)                                                                                      \
         if (tp.logM == A_ && tp.logC == B_) {                                                                          \
-            launch_pdl(k_time<8, A_, B_>, dim3(h->S / h->time_cols), dim3(T), smem, h->stream, mode, E, out0, out1, h->ng, h->w, h->nlfilt, \
+            launch_pdl(k_time<8, A_, B_>, dim3(h->S / C), dim3(T), smem, h->stream, mode, E, out0, out1, h->ng, h->w, h->nlfilt, \
                                                                             h->tw, h->twLog, tp);                    \
             return cudaGetLastError();                                                                             \
         }
         UPPE_TIME_CT(UPPE_TIME_CASE)
 #undef UPPE_TIME_CASE
-        launch_pdl(k_time<8>, dim3(h->S / h->time_cols), dim3(T), smem, h->stream, mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
+        launch_pdl(k_time<8>, dim3(h->S / C), dim3(T), smem, h->stream, mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
                                                                h->twLog, tp);
     }
     else
-        launch_pdl(k_time<16>, dim3(h->S / h->time_cols), dim3(T), smem, h->stream, mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
+        launch_pdl(k_time<16>, dim3(h->S / C), dim3(T), smem, h->stream, mode, E, out0, out1, h->ng, h->w, h->nlfilt, h->tw,
                                                                 h->twLog, tp);
     return cudaGetLastError();
 }
