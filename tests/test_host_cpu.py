@@ -201,3 +201,42 @@ def test_product_code_never_reaches_the_oracle():
     hits = [f"{p.relative_to(root)}:{i + 1}" for p in files
             for i, line in enumerate(p.read_text().splitlines()) if pat.search(line)]
     assert hits == []
+
+
+def test_programmatic_launches_wait_for_their_predecessor():
+    """Every kernel launched with the programmatic-dependent-launch attribute (launch_pdl) must call
+    pdl_begin() before touching global memory: without its griddepcontrol.wait it could read the
+    previous kernel's output before that kernel has finished.  Source check over csrc/: each such
+    kernel's body calls pdl_begin() ahead of its first loop, branch or asynchronous copy."""
+    import pathlib
+    import re
+    csrc = pathlib.Path(__file__).resolve().parent.parent / "searay_gb300" / "csrc"
+    sources = {p: p.read_text() for p in list(csrc.glob("*.cu")) + list(csrc.glob("*.cuh"))}
+    launched = set()
+    for text in sources.values():
+        launched.update(re.findall(r"launch_pdl\((k_\w+)", text))
+    assert launched, "no programmatic launches found"
+    for name in sorted(launched):
+        bodies = []
+        for text in sources.values():
+            for m in re.finditer(r"__global__[^;{]*?\b" + name + r"\s*\(", text):
+                depth, j = 0, m.end() - 1
+                while True:
+                    if text[j] == "(":
+                        depth += 1
+                    elif text[j] == ")":
+                        depth -= 1
+                        if depth == 0:
+                            break
+                    j += 1
+                k = text.index("{", j)
+                if ";" in text[j + 1:k]:
+                    continue  # a declaration
+                bodies.append(text[k + 1:])
+        assert bodies, name
+        for body in bodies:
+            head = body[:body.index("pdl_begin();")] if "pdl_begin();" in body else None
+            assert head is not None, f"{name} is launched with launch_pdl but never calls pdl_begin()"
+            # nothing before pdl_begin reads or writes global memory: no loops, no cp.async, no
+            # indexing of kernel arguments (declarations and shared-memory set-up only)
+            assert not re.search(r"\bfor\s*\(|cp_async|\bif\s*\(", head), (name, head[-300:])
