@@ -329,6 +329,7 @@ extern "C" int uppe_destroy(UppeHandle* h) {
 
 extern "C" int uppe_set_stream(UppeHandle* h, void* stream) {
     if (!h) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     h->stream = (cudaStream_t)stream;
     return UPPE_OK;
 }
@@ -340,6 +341,7 @@ extern "C" int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, 
         uppe_set_error(h, "UPPE propagator requires frequency range [0,...]");
         return UPPE_E_ARG;
     }
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     std::vector<float> wf(h->N0), filt(h->N0);
     for (int k = 0; k < h->N0; ++k) {
         wf[k] = (float)w[k];
@@ -410,6 +412,7 @@ extern "C" int uppe_set_grid(UppeHandle* h, const double* w, const double* kr2, 
 
 extern "C" int uppe_set_material(UppeHandle* h, const double* w2n2, const double* kg, const double* ng) {
     if (!h) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     if (!h->have_grid) {
         uppe_set_error(h, "uppe_set_material before uppe_set_grid");
         return UPPE_E_ARG;
@@ -498,6 +501,7 @@ static cudaError_t eval_to_J(UppeHandle* h, const float2* qsrc, StepArgs z) {
 
 extern "C" int uppe_load_field(UppeHandle* h, const void* a) {
     if (!h || !a) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     if (!h->have_grid) {
         uppe_set_error(h, "uppe_load_field before uppe_set_grid");
         return UPPE_E_ARG;
@@ -619,10 +623,12 @@ static int rk4_step_generic(UppeHandle* h, double z_phase, double L, double z_su
                            h->tc_next ? &zn : nullptr));
     }
     {
+        // the step's result is transformed next by the following step's first evaluation, at the
+        // same z (a later call checks the source, z and material before using the tiles)
         StepArgs z = split_z(h, z_phase + dz);
         CUDA_TRY(h, eval_to_J(h, h->q, z));
-        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD,
-                 spec_pass(h, SPEC_FINISH, h->J, h->qi, h->qf, nullptr, (float)(dz / 6), 0.f, z));
+        PROF_TRY(h, UPPE_CLASS_TRANSVERSE_FWD, spec_pass(h, SPEC_FINISH, h->J, h->qi, h->qf, nullptr, (float)(dz / 6),
+                                                         0.f, z, h->tc_next ? &z : nullptr));
     }
     *dz_out = dz;
     return UPPE_OK;
@@ -650,6 +656,7 @@ extern "C" int uppe_rk4_step(UppeHandle* h, double z_phase, double L, double z_s
 
 extern "C" int uppe_finish(UppeHandle* h, double z_phase, void* A, void* J, void* chi_w, void* ne_w) {
     if (!h) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     int rc = check_ready(h, true);
     if (rc) return rc;
     rc = check_range(h, z_phase);
@@ -664,6 +671,7 @@ extern "C" int uppe_finish(UppeHandle* h, double z_phase, void* A, void* J, void
 
 extern "C" int uppe_eval_rhs(UppeHandle* h, const void* q_in, double z_phase, void* S_out) {
     if (!h || !q_in || !S_out) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     int rc = check_ready(h, false);
     if (rc) return rc;
     rc = check_range(h, z_phase);
@@ -709,6 +717,7 @@ extern "C" int uppe_check_finite(UppeHandle* h, int* nonfinite) {
 // =============================================================================================
 extern "C" int uppe_set_chi3(UppeHandle* h, double chi3_over_nref) {
     if (!h) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     h->redchi3 = chi3_over_nref;
     return UPPE_OK;
 }
@@ -719,6 +728,7 @@ extern "C" int uppe_set_rotator(UppeHandle* h, int nstates, const double* Tj, co
         if (h) uppe_set_error(h, "uppe_set_rotator: invalid arguments");
         return UPPE_E_ARG;
     }
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     if (nstates > 0 && !(hbar > 0.0)) {
         uppe_set_error(h, "uppe_set_rotator: hbar must be positive (got %g)", hbar);
         return UPPE_E_ARG;
@@ -808,6 +818,7 @@ extern "C" int uppe_set_rotator(UppeHandle* h, int nstates, const double* Tj, co
 
 extern "C" int uppe_set_field(UppeHandle* h, const void* q) {
     if (!h || !q) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     if (!h->have_grid) {
         uppe_set_error(h, "uppe_set_field before uppe_set_grid");
         return UPPE_E_ARG;
@@ -931,6 +942,7 @@ static int reverse_sweep_generic(UppeHandle* h, const float2* lam_out, float2* l
 extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void* lam_out, void* lam_in, double z_phase,
                                      double dz, double* dred_out) {
     if (!h || !q0v || !lam_out || !lam_in) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     int rc = check_ready(h, false);
     if (rc) return rc;
     rc = ensure_adjoint(h);
@@ -1005,6 +1017,7 @@ extern "C" int uppe_adjoint_rk4_step(UppeHandle* h, const void* q0v, const void*
 // current are processed in every stage (their E is kept).
 extern "C" int uppe_rk4_step_keep(UppeHandle* h, double z_phase, double dz) {
     if (!h) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     int rc = check_ready(h, true);
     if (rc) return rc;
     if (!(dz > 0.0)) {
@@ -1087,6 +1100,7 @@ extern "C" int uppe_rk4_step_keep(UppeHandle* h, double z_phase, double dz) {
 // lam_out), from its kept stage fields: uppe_adjoint_rk4_step without the recompute.
 extern "C" int uppe_adjoint_rk4_step_kept(UppeHandle* h, const void* lam_out, void* lam_in, double* dred_out) {
     if (!h || !lam_out || !lam_in) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     if (!h->kept_valid || h->kept_mat != h->mat_version) {
         uppe_set_error(h, "uppe_adjoint_rk4_step_kept: no step kept by uppe_rk4_step_keep for the current material");
         return UPPE_E_ARG;
@@ -1099,6 +1113,7 @@ extern "C" int uppe_adjoint_rk4_step_kept(UppeHandle* h, const void* lam_out, vo
 
 extern "C" int uppe_adjoint_load(UppeHandle* h, const void* lam_q, void* lam_a) {
     if (!h || !lam_q || !lam_a) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     if (!h->have_grid) {
         uppe_set_error(h, "uppe_adjoint_load before uppe_set_grid");
         return UPPE_E_ARG;
@@ -1111,6 +1126,7 @@ extern "C" int uppe_adjoint_load(UppeHandle* h, const void* lam_q, void* lam_a) 
 
 extern "C" int uppe_adjoint_finish(UppeHandle* h, double z_phase, const void* lam_A, void* lam_q) {
     if (!h || !lam_A || !lam_q) return UPPE_E_ARG;
+    h->atc_next = 0;  // Atc tiles carried between rk4 steps are void after any other call
     int rc = check_ready(h, false);
     if (rc) return rc;
     rc = ensure_adjoint(h);

@@ -403,12 +403,13 @@ cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* 
     // the A operand once per transform (k_hankel_tc_prep), then the GEMM on pre-split tiles.  The
     // inverse transform of a stage estimate finds its operand already written when the spectral
     // update that produced the estimate was asked for it (k_spec_point with a TcNext): same source,
-    // same z, no transform in between (atc_next is cleared by every other use of the tiles).
+    // same z, same material, no transform in between (atc_next is cleared by every other use of the
+    // tiles and by every entry point other than uppe_rk4_step).
     if (!h->Atc || (size_t)h->N2 * a.nwt * a.nkt * 2 * TC_TILE_BYTES > h->Atc_bytes) return cudaErrorInvalidValue;
     // Likewise the forward transform of J finds its operand written by the time pass that formed J.
     const bool ready_inv = amode == TA_QPHASE_IKZ && which == 1 && h->atc_next && h->atc_next_src == A &&
                            h->atc_next_z.zhi == z.zhi && h->atc_next_z.zlo == z.zlo &&
-                           h->atc_next_z.plain == z.plain;
+                           h->atc_next_z.plain == z.plain && h->atc_next_mat == h->mat_version;
     const bool ready_fwd = amode == TA_PLAIN && which == 0 && h->atc_fwd && A == h->J;
     const bool ready = ready_inv || ready_fwd;
     h->atc_next = 0;

@@ -88,6 +88,7 @@ struct UppeHandle {
     int atc_next;                // Atc holds the operand of the inverse transform of atc_next_src at atc_next_z
     const void* atc_next_src;
     StepArgs atc_next_z;
+    long long atc_next_mat;      // the material version the tiles were formed with
     double* kr2_d;   // [S] transverse eigenvalues (FP64)
     double* w2n2_d;  // [N0] complex w^2 (1 + chi0) interleaved
     double* kg_d;    // [N0]

@@ -430,6 +430,7 @@ cudaError_t launch_spec_point(UppeHandle* h, int mode, const float2* C, float2* 
         h->atc_next = 1;
         h->atc_next_src = q_out;
         h->atc_next_z = *z_next;
+        h->atc_next_mat = h->mat_version;
     }
     return e;
 }
