@@ -496,6 +496,8 @@ static cudaError_t eval_to_J(UppeHandle* h, const float2* qsrc, StepArgs z) {
     e = launch_time_pass(h, TIME_J, h->E, h->J, nullptr);
     h->time_atc = 0;
     h->atc_fwd = (to_tc && e == cudaSuccess) ? 1 : 0;
+    h->atc_fwd_which = 0;
+    h->atc_fwd_src = h->J;
     return e;
 }
 
@@ -872,7 +874,20 @@ static int vjp_rhs(UppeHandle* h, const float2* qs, double zs, const float2* lam
         Es = h->E;
     }
     PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_S, lamk, h->J, z));
-    PROF_TRY(h, UPPE_CLASS_OTHER, launch_time_adjoint(h, Es, h->J, h->k1, h->dred_d));
+    // cylindrical mixed form, one azimuthal node: the cotangent of E goes straight into the operand
+    // tiles of the Minv^T transform that follows
+    const bool to_tc = h->cfg.cylindrical && h->cfg.precision == UPPE_PREC_MIXED && h->N2 == 1 && h->tc_next &&
+                       h->Atc && !h->cfg.envelope;
+    {
+        ProfScope ps(h, UPPE_CLASS_OTHER);
+        h->time_atc = to_tc ? 1 : 0;
+        const cudaError_t et = launch_time_adjoint(h, Es, h->J, h->k1, h->dred_d);
+        h->time_atc = 0;
+        CUDA_TRY(h, et);
+    }
+    h->atc_fwd = to_tc ? 1 : 0;
+    h->atc_fwd_which = 3;
+    h->atc_fwd_src = h->k1;
     PROF_TRY(h, UPPE_CLASS_OTHER, adj_pass(h, ADJ_E, h->k1, mu, z));
     return UPPE_OK;
 }

@@ -406,11 +406,12 @@ cudaError_t launch_hankel_tc(UppeHandle* h, int amode, int cmode, const float2* 
     // same z, same material, no transform in between (atc_next is cleared by every other use of the
     // tiles and by every entry point other than uppe_rk4_step).
     if (!h->Atc || (size_t)h->N2 * a.nwt * a.nkt * 2 * TC_TILE_BYTES > h->Atc_bytes) return cudaErrorInvalidValue;
-    // Likewise the forward transform of J finds its operand written by the time pass that formed J.
+    // Likewise the forward transform of J, and the adjoint's Minv^T transform of the cotangent of E,
+    // find their operand written by the time pass that formed it.
     const bool ready_inv = amode == TA_QPHASE_IKZ && which == 1 && h->atc_next && h->atc_next_src == A &&
                            h->atc_next_z.zhi == z.zhi && h->atc_next_z.zlo == z.zlo &&
                            h->atc_next_z.plain == z.plain && h->atc_next_mat == h->mat_version;
-    const bool ready_fwd = amode == TA_PLAIN && which == 0 && h->atc_fwd && A == h->J;
+    const bool ready_fwd = amode == TA_PLAIN && h->atc_fwd && which == h->atc_fwd_which && A == h->atc_fwd_src;
     const bool ready = ready_inv || ready_fwd;
     h->atc_next = 0;
     h->atc_fwd = 0;

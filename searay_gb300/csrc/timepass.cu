@@ -756,7 +756,10 @@ __global__ void __launch_bounds__(LOGM > 0 ? 256 : 512, RAMAN ? 1 : (LOGM > 0 ? 
             const int ka = k & (M - 1), kb = (M - k) & (M - 1);
             const float2 X = real_spectrum(Ze[sw(ka) * C + cc], Ze[sw(kb) * C + cc], tws.get(k));
             const float wt = (k == 0 || k == M) ? inv : 2.f * inv;
-            gE[(size_t)k * S + col0 + cc] = cscale(X, wt);
+            if (tp.atc)  // the operand tiles of the Minv^T transform that follows
+                tc_store_split(tp.atc, tp.atc_nwt, tp.atc_nkt, 0, k, (int)(col0 + cc), cscale(X, wt));
+            else
+                gE[(size_t)k * S + col0 + cc] = cscale(X, wt);
         }
         __syncthreads();  // the next group overwrites the shared arrays
     }

@@ -24,6 +24,7 @@
 // shared-memory column buffers and register budget as k_time_reg.
 #include <math.h>
 
+#include "hankel_tc.cuh"
 #include "time_common.cuh"
 #include "timepass_reg.cuh"
 #include "uppe_internal.h"
@@ -150,7 +151,11 @@ __global__ void __launch_bounds__(256, TReg<LOGM>::MINB)
     }
     for (int i = tid; i < (M + 1) * NC; i += G::THREADS) {
         const int c = i & (NC - 1), k = i / NC;
-        if (!grp_live[c / CA]) gE[(size_t)k * S + col0 + c] = sm[c * LD + k];
+        if (grp_live[c / CA]) continue;
+        if (tp.atc)  // the operand tiles of the Minv^T transform that follows
+            tc_store_split(tp.atc, tp.atc_nwt, tp.atc_nkt, 0, k, (int)(col0 + c), sm[c * LD + k]);
+        else
+            gE[(size_t)k * S + col0 + c] = sm[c * LD + k];
     }
 }
 

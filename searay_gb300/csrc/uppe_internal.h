@@ -84,7 +84,9 @@ struct UppeHandle {
     uint8_t* Atc;     // pre-split A operand tiles of the tensor-core Hankel transform (mixed form)
     size_t Atc_bytes;
     int time_atc;                // the next TIME_J pass writes J into Atc (the forward transform's operand)
-    int atc_fwd;                 // Atc holds the forward transform's operand of J (written by the time pass)
+    int atc_fwd;                 // Atc holds the operand of the transform `atc_fwd_which` (0: forward of J,
+    int atc_fwd_which;           // 3: the adjoint's Minv^T of gE) of atc_fwd_src, written by a time pass
+    const void* atc_fwd_src;
     int atc_next;                // Atc holds the operand of the inverse transform of atc_next_src at atc_next_z
     const void* atc_next_src;
     StepArgs atc_next_z;

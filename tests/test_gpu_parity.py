@@ -157,6 +157,44 @@ def test_operand_carried_between_steps_is_dropped_by_other_calls(monkeypatch):
     assert np.array_equal(out["fused"], out["prepass"])
 
 
+def test_adjoint_time_pass_writes_transform_operand(monkeypatch):
+    """Mixed form, one azimuthal node: in the vector-Jacobian product of a step the adjoint time
+    pass writes the cotangent of E straight into the operand tiles of the Minv^T transform that
+    follows (its pre-pass skipped).  Against SEARAY_UPPE_TC_NEXT=0: the same arithmetic on the same
+    values, so the cotangent of q agrees bit for bit and the chi3 derivative to its summation order,
+    with at least four launches fewer (one per stage)."""
+    import torch
+    out, launches = {}, {}
+    for form in ("fused", "prepass"):
+        if form == "prepass":
+            monkeypatch.setenv("SEARAY_UPPE_TC_NEXT", "0")
+        else:
+            monkeypatch.delenv("SEARAY_UPPE_TC_NEXT", raising=False)
+        vd, g, dev, mat, orc = _device_case("cyl_kerr", "mixed")
+        L = vd["size"][2] / 20
+        mat.UpdateMaterial(0.5 * L)
+        a = torch.from_numpy(vd["incoming wave"](g.w, g.x1, g.x2).astype(np.complex64)).cuda()
+        dev.load_field(a)
+        q = dev.empty_field()
+        dev.get_field(q)
+        rng = np.random.default_rng(5)
+        qn = q.cpu().numpy()
+        lam = torch.from_numpy(((rng.standard_normal(qn.shape) + 1j * rng.standard_normal(qn.shape)) *
+                                np.abs(qn)).astype(np.complex64)).cuda()
+        gq = dev.empty_field()
+        l0 = dev.launches()
+        dred = dev.adjoint_step(q, lam, gq, 0.0, L)
+        launches[form] = dev.launches() - l0
+        out[form] = (gq.cpu().numpy(), dred)
+        assert not dev.nonfinite()
+        dev.close()
+    print("adjoint launches", launches)
+    assert launches["prepass"] - launches["fused"] >= 4, launches
+    assert np.array_equal(out["fused"][0], out["prepass"][0])
+    # (the chi3 derivative is summed by atomics in a run-dependent order)
+    assert abs(out["fused"][1] - out["prepass"][1]) <= 1e-12 * abs(out["prepass"][1])
+
+
 @pytest.mark.parametrize("name", replay.CASE_NAMES)
 def test_transform_and_rhs_vs_oracle(name):
     """One kspacex of the incoming field and one load_source evaluation, against FP64."""
