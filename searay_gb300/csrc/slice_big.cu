@@ -96,6 +96,19 @@ __global__ void __launch_bounds__(16 << (LN1 - 4), KIND == BC_ADJ_STAGE ? 3 : 2)
     if constexpr (KIND == BC_FUSED || KIND == BC_SPEC || KIND == BC_ADJ_FWD || KIND == BC_ADJ_STAGE) {
 #pragma unroll
         for (int m = 0; m < 16; ++m) v[m] = a.src[base + (size_t)(i + R1 * m) * N2 + ky];
+        if constexpr (KIND == BC_FUSED || KIND == BC_ADJ_STAGE) {
+            // the pointwise operands of this thread's 16 points are asked into L2 while the column
+            // transform runs, so that their loads after it find them there
+            const bool pa = (KIND == BC_ADJ_STAGE) || mode != SPEC_FINISH;
+            const bool pb = (KIND == BC_ADJ_STAGE) || mode != SPEC_STAGE1;
+#pragma unroll
+            for (int r = 0; r < 16; ++r) {
+                const size_t idx = idx_of(r);
+                asm volatile("prefetch.global.L2 [%0];\n" ::"l"(opv.K + idx));
+                if (pa) asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.qi + idx));
+                if (pb) asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.qf + idx));
+            }
+        }
         reg_n2m<R1, LN1, false>(v, w, ex, i, twg, sync);
     }
     if constexpr (KIND == BC_FUSED || KIND == BC_ADJ_STAGE) {
