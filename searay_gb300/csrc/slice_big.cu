@@ -23,10 +23,14 @@
 template <int LN2, bool INV>
 __global__ void __launch_bounds__(256)
     k_rows_big(const float2* src, float2* dst, float scale, int finish, float2* __restrict__ A_out, OpView opv,
-               int N1, const float2* __restrict__ tw, int twLog) {
+               int N1, const float2* __restrict__ tw, int twLog, int ahead) {
     constexpr int N2 = 1 << LN2, R2 = N2 / 16, ROWS = 256 / R2;
     __shared__ float2 xb[8 * 544];
     const int tid = threadIdx.x;
+    // the rows of the block `ahead` places on (about one wave later) into L2: one 128-byte line per
+    // thread (ROWS N2 complex values = 32 KB)
+    if (blockIdx.x + ahead < gridDim.x)
+        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(src + (size_t)(blockIdx.x + ahead) * ROWS * N2 + 16 * tid));
     const size_t row = (size_t)blockIdx.x * ROWS + tid / R2;
     const int j = tid % R2;
     float2* ex = xb + (tid >> 5) * 544 + ((tid & 31) / R2) * 17 * R2;
@@ -70,7 +74,7 @@ __global__ void __launch_bounds__(256)
 // the compiler knows, which otherwise serialises every point behind a full memory latency.
 template <int LN1, int LN2, int KIND>
 __global__ void __launch_bounds__(16 << (LN1 - 4), KIND == BC_ADJ_STAGE ? 3 : 2) k_cols_big(BigColArgs a, OpView opv, const float2* __restrict__ tw,
-                                                              int twLog) {
+                                                              int twLog, int ahead) {
     constexpr int N1 = 1 << LN1, N2 = 1 << LN2, R1 = N1 / 16, T = 16 * R1, TILES = N2 / 16;
     constexpr int QC = 17 * R1 + 1;
     __shared__ float2 xb[16 * QC];
@@ -94,6 +98,13 @@ __global__ void __launch_bounds__(16 << (LN1 - 4), KIND == BC_ADJ_STAGE ? 3 : 2)
     };
 
     if constexpr (KIND == BC_FUSED || KIND == BC_SPEC || KIND == BC_ADJ_FWD || KIND == BC_ADJ_STAGE) {
+        // the source columns of the block `ahead` places on (about one wave later) into L2: one
+        // 128-byte line (16 columns) of one of its N1 = T rows per thread
+        const unsigned fb = blockIdx.x + (unsigned)ahead;
+        if (fb < gridDim.x) {
+            const size_t fbase = (size_t)(fb / TILES) * N1 * N2 + (size_t)(fb % TILES) * 16;
+            asm volatile("prefetch.global.L2 [%0];\n" ::"l"(a.src + fbase + (size_t)tid * N2));
+        }
 #pragma unroll
         for (int m = 0; m < 16; ++m) v[m] = a.src[base + (size_t)(i + R1 * m) * N2 + ky];
         if constexpr (KIND == BC_FUSED || KIND == BC_ADJ_STAGE) {
@@ -231,10 +242,10 @@ static cudaError_t rows(UppeHandle* h, const float2* src, float2* dst, float sca
     const OpView opv = uppe_op_view(h);
     if (h->N2 == 256) {
         k_rows_big<8, INV><<<(unsigned)(nrows / 16), 256, 0, h->stream>>>(src, dst, scale, finish, A_out, opv, h->N1,
-                                                                         h->tw, h->twLog);
+                                                                         h->tw, h->twLog, 2 * h->num_sms);
     } else {
         k_rows_big<7, INV><<<(unsigned)(nrows / 32), 256, 0, h->stream>>>(src, dst, scale, finish, A_out, opv, h->N1,
-                                                                         h->tw, h->twLog);
+                                                                         h->tw, h->twLog, 2 * h->num_sms);
     }
     return cudaGetLastError();
 }
@@ -242,11 +253,11 @@ static cudaError_t rows(UppeHandle* h, const float2* src, float2* dst, float sca
 template <int KIND>
 static void cols_kind(UppeHandle* h, const BigColArgs& a, const OpView& opv, unsigned grid) {
     if (h->N1 == 256 && h->N2 == 256)
-        k_cols_big<8, 8, KIND><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+        k_cols_big<8, 8, KIND><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog, 2 * h->num_sms);
     else if (h->N1 == 256)
-        k_cols_big<8, 7, KIND><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+        k_cols_big<8, 7, KIND><<<grid, 256, 0, h->stream>>>(a, opv, h->tw, h->twLog, 2 * h->num_sms);
     else
-        k_cols_big<7, 8, KIND><<<grid, 128, 0, h->stream>>>(a, opv, h->tw, h->twLog);
+        k_cols_big<7, 8, KIND><<<grid, 128, 0, h->stream>>>(a, opv, h->tw, h->twLog, 2 * h->num_sms);
 }
 
 // Column passes of the slices [0, nslices) (every slice when nslices < 0).
