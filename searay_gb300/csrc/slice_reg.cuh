@@ -729,6 +729,15 @@ __global__ void __launch_bounds__(RegSlice<LN1, LN2>::T, 1)
     const PhaseArgs ps{z_s.zhi, z_s.zlo, z_s.plain};
     const float2 kgw = opv.kg[iw];
     const float cond = (iw < opv.ncond) ? 0.f : 1.f;
+    // the pointwise operands of this thread's 16 points are asked into L2 while the forward slice
+    // transform runs, so that their loads after it find them there
+#pragma unroll
+    for (int r = 0; r < 16; ++r) {
+        const size_t idx = base + col_elem(c, r);
+        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(opv.K + idx));
+        asm volatile("prefetch.global.L2 [%0];\n" ::"l"(acc + idx));
+        if (mode != 2) asm volatile("prefetch.global.L2 [%0];\n" ::"l"(lam_f + idx));
+    }
     float2 w[16], v[16];
     slice_fwd_from_global<RS, LN1, LN2, false>(g + base, w, sm, c, twg);
     constexpr float scale = 1.0f / (float)RS::S;
