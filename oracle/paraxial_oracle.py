@@ -2,7 +2,7 @@
 product path.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU legs of ``bench.py`` may import this
-module, and only as the checker / the timed CPU baseline.  The CUDA path in ``searay_gb300`` does
+module, and only to check results against / as the timed CPU baseline.  The CUDA path in ``searay_gb300`` does
 not import it and has no CPU fallback.
 
 A NumPy restatement of SeaRay's paraxial propagator (``modules/paraxial_kernel.py``, kernels

@@ -1,7 +1,7 @@
 """FP64 CPU oracle for the UPPE z-step — TEST INFRASTRUCTURE, never part of the product path.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` may import
-this module, and only as the checker / the timed CPU baseline.  The CUDA path in ``searay_gb300``
+this module, and only to check results against / as the timed CPU baseline.  The CUDA path in ``searay_gb300``
 does not import it and has no CPU fallback.
 
 This is a NumPy restatement of SeaRay's UPPE algorithm (``modules/uppe_kernel.py``, kernels
