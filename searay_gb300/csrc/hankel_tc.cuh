@@ -37,8 +37,9 @@ __device__ __forceinline__ void tc_store_split(uint8_t* __restrict__ Atc, int nw
     __nv_bfloat16 rh, rl, ih, il;
     split_bf16(v.x, rh, rl);
     split_bf16(v.y, ih, il);
-    const int wl = w % TC_W, kk = k % TC_K;
-    uint8_t* tile = Atc + (((size_t)m * nwt + w / TC_W) * nkt + k / TC_K) * (size_t)(2 * TC_TILE_BYTES);
+    const unsigned uw = (unsigned)w, uk = (unsigned)k;  // both >= 0: shifts and masks
+    const int wl = (int)(uw % TC_W), kk = (int)(uk % TC_K);
+    uint8_t* tile = Atc + (((size_t)m * nwt + uw / TC_W) * nkt + uk / TC_K) * (size_t)(2 * TC_TILE_BYTES);
     const uint32_t ore = core_off(2 * wl, kk), oim = core_off(2 * wl + 1, kk);
     *reinterpret_cast<__nv_bfloat16*>(tile + ore) = rh;
     *reinterpret_cast<__nv_bfloat16*>(tile + oim) = ih;

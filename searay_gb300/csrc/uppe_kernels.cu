@@ -404,16 +404,25 @@ __global__ void k_spec_point(int mode, const float2* __restrict__ C, OpView opv,
     pdl_begin();
     const PhaseArgs pa{z.zhi, z.zlo, z.plain};
     const PhaseArgs pn{nx.z.zhi, nx.z.zlo, nx.z.plain};
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += (size_t)gridDim.x * blockDim.x) {
-        const int w = (int)(idx / (size_t)S);
+    // idx = w S + k: (w, k) advance with the grid stride (one division per thread, not per point)
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t idx0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int dw = (int)(stride / (size_t)S), dk = (int)(stride - (size_t)dw * S);
+    int w = (int)(idx0 / (size_t)S), k = (int)(idx0 - (size_t)w * S);
+    for (size_t idx = idx0; idx < n; idx += stride) {
         const float cond = (w < opv.ncond) ? 0.f : 1.f;
         const OpPoint o = op_at(opv, idx, opv.kg[w]);
         const float2 qw = spec_update(mode, idx, C[idx], o, cond, q_out, qf, qi, Cs, Ce, pa, true);
         if (nx.Atc) {
-            const int k = (int)(idx - (size_t)w * S);
             float2 a = make_float2(0.f, 0.f);
             if (k < nx.Nk) a = op_field(opv, o, cmul(propagator_factor(o, pn, 1.f), qw));
             tc_store_split(nx.Atc, nx.nwt, nx.nkt, 0, w, k, a);
+        }
+        w += dw;
+        k += dk;
+        if (k >= S) {
+            k -= S;
+            ++w;
         }
     }
 }
